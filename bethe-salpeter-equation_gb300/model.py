@@ -1,0 +1,182 @@
+"""Tight-binding model, k/G grids and BSE parameters (host side).
+
+Mirrors the data the reference keeps in Crystal_Lattice (bse.version13.cpp:45-141),
+K_points (145-291), G_points (294-405) and Hamiltonian_TB (407-906), as plain numpy
+arrays laid out for the C ABI of include/bse_gpu.h.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Optional
+
+import numpy as np
+
+from .constants import (MINVAL, BSE_V_BARE_3D, BSE_W_EMPIRICAL, BSE_FP64,
+                        BSE_EIG_OWN, INV_EPS_EMPIRICAL)
+
+
+def reciprocal_vectors(lattice: np.ndarray) -> np.ndarray:
+    """Columns b_i = 2 pi (a_j x a_k) / V, as Crystal_Lattice::Crystal_Lattice
+    (bse.version13.cpp:103-120).  `lattice` holds a1, a2, a3 as columns."""
+    a0, a1, a2 = lattice[:, 0], lattice[:, 1], lattice[:, 2]
+    vol = abs(np.linalg.det(lattice))
+    b = np.stack([np.cross(a1, a2), np.cross(a2, a0), np.cross(a0, a1)], axis=1)
+    return b * (2.0 * math.pi / vol)
+
+
+def cell_volume(lattice: np.ndarray) -> float:
+    """|det(a1 a2 a3)| (bse.version13.cpp:101)."""
+    return float(abs(np.linalg.det(lattice)))
+
+
+@dataclasses.dataclass
+class TBModel:
+    """Wannier tight-binding model.
+
+    h_r[s, R, l, m] = <w_l,0 | H | w_m,R> of spin channel s; H(k) = sum_R w_R h_r e^{i k.R}
+    (Hamiltonian_TB::FFT, bse.version13.cpp:647-705).  centres[s, l] is the Wannier centre
+    of orbital l in spin channel s (cartesian).  lattice columns are a1, a2, a3.
+    """
+    lattice: np.ndarray            # (3,3) columns a_i
+    r_cryst: np.ndarray            # (nR,3) integer lattice vectors
+    weights: np.ndarray            # (nR,)
+    h_r: np.ndarray                # (n_spin, nR, nw, nw) complex128
+    centres: np.ndarray            # (n_spin, nw, 3)
+    dim: int = 3                   # 2 for slab models (in-plane a1, a2)
+    name: str = "model"
+
+    @property
+    def nw(self) -> int:
+        return int(self.h_r.shape[2])
+
+    @property
+    def n_spin(self) -> int:
+        return int(self.h_r.shape[0])
+
+    @property
+    def n_r(self) -> int:
+        return int(self.h_r.shape[1])
+
+    @property
+    def r_cart(self) -> np.ndarray:
+        return self.r_cryst.astype(np.float64) @ self.lattice.T
+
+    @property
+    def volume(self) -> float:
+        return cell_volume(self.lattice)
+
+    def hk(self, k_cart: np.ndarray) -> np.ndarray:
+        """H(k) for an array of k (nk,3) -> (n_spin, nk, nw, nw), weights multiplied in."""
+        k_cart = np.atleast_2d(k_cart)
+        ph = np.exp(1j * (k_cart @ self.r_cart.T)) * self.weights[None, :]
+        return np.einsum("kr,srlm->sklm", ph, self.h_r)
+
+    def check_hermitian(self, tol: float = 1e-12) -> float:
+        """max |H(R) - H(-R)^dagger| over the R list (H(k) Hermitian for every k)."""
+        idx = {tuple(r): i for i, r in enumerate(self.r_cryst.tolist())}
+        err = 0.0
+        for i, r in enumerate(self.r_cryst.tolist()):
+            j = idx.get(tuple(-x for x in r))
+            if j is None:
+                err = max(err, float(np.abs(self.h_r[:, i]).max()))
+                continue
+            d = self.h_r[:, i] - np.conj(np.swapaxes(self.h_r[:, j], -1, -2))
+            err = max(err, float(np.abs(d).max()))
+        return err
+
+
+@dataclasses.dataclass
+class BSEParams:
+    """Run parameters; the names follow the local variables of main()
+    (bse.version13.cpp:3686-3848) and the fields of bse_params (include/bse_gpu.h)."""
+    nv: int
+    nc: int
+    fermi_energy: float = 0.0
+    scissor: float = 0.0
+    q: tuple = (MINVAL, 0.0, 0.0)
+    tamm_dancoff: int = 1
+    ipa: int = 0
+    small_momentum: int = 1
+    coulomb_kind: int = BSE_V_BARE_3D
+    coulomb_radius: float = 0.0
+    coulomb_min_k2: float = 0.0
+    w_kind: int = BSE_W_EMPIRICAL
+    inv_eps: float = INV_EPS_EMPIRICAL
+    rk_r0: float = 10.0
+    rk_eps: float = 1.0
+    spin_factor: float = -1.0
+    precision: int = BSE_FP64
+    eig_solver: int = BSE_EIG_OWN
+    n_refine: int = 256
+
+    def replace(self, **kw) -> "BSEParams":
+        return dataclasses.replace(self, **kw)
+
+
+@dataclasses.dataclass
+class Problem:
+    """A model plus its k-list, G-list and parameters: everything bse_create needs."""
+    model: TBModel
+    k_cart: np.ndarray       # (nk,3)
+    g_cart: np.ndarray       # (ng,3), G=0 at ng//2
+    params: BSEParams
+    k_cryst: Optional[np.ndarray] = None
+    grid: Optional[tuple] = None
+
+    @property
+    def nk(self) -> int:
+        return int(self.k_cart.shape[0])
+
+    @property
+    def ng(self) -> int:
+        return int(self.g_cart.shape[0])
+
+    @property
+    def n_bse(self) -> int:
+        return self.nk * self.params.nc * self.params.nv
+
+    @property
+    def spinorial(self) -> int:
+        return self.model.n_spin - 1
+
+
+def mp_grid(lattice: np.ndarray, n: tuple, shift=(0.0, 0.0, 0.0)):
+    """Gamma-centred (shift 0) or shifted Monkhorst-Pack grid, i1 slowest.
+
+    Returns (k_cart (nk,3), k_cryst (nk,3)).  The crystal->cartesian conversion is the
+    one of K_points::push_k_points_list_values (bse.version13.cpp:205-216): the shift
+    is added in crystal coordinates.  The reference has no grid generator (its one is
+    commented out, 243-271); this is the seeded, reproducible replacement of its
+    std::random_device list (Q19)."""
+    b = reciprocal_vectors(lattice)
+    n1, n2, n3 = n
+    ii = np.stack(np.meshgrid(np.arange(n1), np.arange(n2), np.arange(n3), indexing="ij"),
+                  axis=-1).reshape(-1, 3).astype(np.float64)
+    kc = ii / np.array([n1, n2, n3], dtype=np.float64) + np.asarray(shift, dtype=np.float64)
+    return kc @ b.T, kc
+
+
+def g_list(lattice: np.ndarray, cutoff: float, dim: int = 3, plane=(0, 1)) -> np.ndarray:
+    """Symmetric G list with n_i = int(cutoff / |b_i|) and G = 0 at index NG/2.
+
+    3-D: i over b1 (slowest), j over b2, k over b3 -- the order of G_points::G_points
+    (bse.version13.cpp:334-351).  2-D: the in-plane set i*b_p0 + j*b_p1, generated
+    correctly (the reference's 2-D branch, 352-379, miscounts: quirk Q3)."""
+    b = reciprocal_vectors(lattice)
+    if dim == 3:
+        ns = [int(cutoff / np.linalg.norm(b[:, i])) for i in range(3)]
+        out = []
+        for i in range(-ns[0], ns[0] + 1):
+            for j in range(-ns[1], ns[1] + 1):
+                for k in range(-ns[2], ns[2] + 1):
+                    out.append(i * b[:, 0] + j * b[:, 1] + k * b[:, 2])
+        return np.array(out, dtype=np.float64).reshape(-1, 3)
+    p0, p1 = plane
+    n0 = int(cutoff / np.linalg.norm(b[:, p0]))
+    n1 = int(cutoff / np.linalg.norm(b[:, p1]))
+    out = []
+    for i in range(-n0, n0 + 1):
+        for j in range(-n1, n1 + 1):
+            out.append(i * b[:, p0] + j * b[:, p1])
+    return np.array(out, dtype=np.float64).reshape(-1, 3)

@@ -1,0 +1,171 @@
+"""Readers and writers for the reference's input files.
+
+  lattice file   9 numbers; row i of the file is a_i
+                 (Crystal_Lattice ctor reads bravais_lattice(j, i), bse.version13.cpp:94-97)
+  atoms file     3 numbers per atom (bse.version13.cpp:99-102)
+  *_hr.dat       Wannier90 format: header, nw, nR, nR weights, nw*nw*nR lines
+                 "R1 R2 R3 l m Re Im" (crystal R); for collinear spin the file holds two
+                 complete blocks, up then down (Hamiltonian_TB ctor, bse.version13.cpp:485-580)
+  *_centres.xyz  count line, comment line, nw lines "X x y z", then the atoms
+                 (repeated per spin channel, bse.version13.cpp:608-634)
+  k list         3 numbers per line, crystal or cartesian (bse.version13.cpp:186-203)
+
+The reader keeps the reference's semantics: the R vectors of a block are the ones given
+on the first line of each group of nw*nw lines, converted crystal->cartesian with the
+lattice; weights are multiplied into H(k) by Hamiltonian_TB::FFT (quirk Q1 -- the
+synthetic models write weight 1, so the Wannier90 divide-vs-multiply question is moot).
+"""
+from __future__ import annotations
+
+import datetime
+import os
+from typing import Optional
+
+import numpy as np
+
+from .model import TBModel
+
+
+def write_lattice(path, lattice: np.ndarray):
+    with open(path, "w") as f:
+        for i in range(3):
+            f.write(" ".join(f"{x:.16e}" for x in lattice[:, i]) + "\n")
+
+
+def read_lattice(path) -> np.ndarray:
+    v = np.loadtxt(path).reshape(-1)[:9]
+    lat = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            lat[j, i] = v[3 * i + j]
+    return lat
+
+
+def write_atoms(path, atoms: np.ndarray):
+    with open(path, "w") as f:
+        for a in np.atleast_2d(atoms):
+            f.write(" ".join(f"{x:.16e}" for x in a) + "\n")
+
+
+def read_atoms(path, n_atoms: int) -> np.ndarray:
+    return np.loadtxt(path).reshape(-1)[:3 * n_atoms].reshape(n_atoms, 3)
+
+
+def write_hr(path, model: TBModel):
+    nw, nr = model.nw, model.n_r
+    with open(path, "w") as f:
+        for s in range(model.n_spin):
+            f.write(f"written on {datetime.date(2026, 1, 1).isoformat()} (synthetic model {model.name}, spin {s})\n")
+            f.write(f"{nw:12d}\n{nr:12d}\n")
+            for i in range(0, nr, 15):
+                f.write("".join(f"{int(w):5d}" for w in model.weights[i:i + 15]) + "\n")
+            for ir in range(nr):
+                R = model.r_cryst[ir]
+                for m in range(nw):
+                    for l in range(nw):
+                        h = model.h_r[s, ir, l, m]
+                        f.write(f"{R[0]:5d}{R[1]:5d}{R[2]:5d}{l + 1:5d}{m + 1:5d} "
+                                f"{h.real: .16e} {h.imag: .16e}\n")
+
+
+def read_hr(path, nw: int, n_r: int, n_spin: int = 1):
+    """Parse a (one- or two-block) hr.dat.  Returns (r_cryst (nR,3) int, weights (nR,),
+    h_r (n_spin,nR,nw,nw)) and raises ValueError on a header mismatch (the reference
+    prints "ERROR!!!!!!!" and continues, bse.version13.cpp:499-501)."""
+    with open(path) as f:
+        lines = f.read().split("\n")
+    pos = 0
+    h_r = np.zeros((n_spin, n_r, nw, nw), np.complex128)
+    r_cryst = np.zeros((n_r, 3), np.int64)
+    weights = np.zeros(n_r)
+    for s in range(n_spin):
+        while pos < len(lines) and not lines[pos].strip():
+            pos += 1
+        pos += 1                                 # header / date line
+        toks = []
+        while len(toks) < 2:
+            toks += lines[pos].split()
+            pos += 1
+        nw_f, nr_f = int(toks[0]), int(toks[1])
+        if nw_f != nw or nr_f != n_r:
+            raise ValueError(f"hr.dat header mismatch: file has nw={nw_f} nR={nr_f}, expected {nw} {n_r}")
+        w = []
+        while len(w) < n_r:
+            w += [float(x) for x in lines[pos].split()]
+            pos += 1
+        weights[:] = w[:n_r]
+        total = nw * nw * n_r
+        for cnt in range(total):
+            t = lines[pos].split()
+            pos += 1
+            R = [int(float(x)) for x in t[:3]]
+            l, m = int(t[3]), int(t[4])
+            ir = cnt // (nw * nw)
+            if cnt % (nw * nw) == 0:
+                r_cryst[ir] = R
+            h_r[s, ir, l - 1, m - 1] = float(t[5]) + 1j * float(t[6])
+    return r_cryst, weights, h_r
+
+
+def write_centres(path, model: TBModel, atoms: Optional[np.ndarray] = None):
+    atoms = np.zeros((0, 3)) if atoms is None else np.atleast_2d(atoms)
+    with open(path, "w") as f:
+        for s in range(model.n_spin):
+            f.write(f"{model.nw + len(atoms):6d}\n")
+            f.write(f" Wannier centres, synthetic model {model.name}, spin {s}\n")
+            for c in model.centres[s]:
+                f.write("X " + " ".join(f"{x: .16e}" for x in c) + "\n")
+            for a in atoms:
+                f.write("A " + " ".join(f"{x: .16e}" for x in a) + "\n")
+
+
+def read_centres(path, nw: int, n_atoms: int, n_spin: int = 1) -> np.ndarray:
+    with open(path) as f:
+        lines = [ln for ln in f.read().split("\n")]
+    pos = 0
+    out = np.zeros((n_spin, nw, 3))
+    for s in range(n_spin):
+        while pos < len(lines) and not lines[pos].strip():
+            pos += 1
+        pos += 2                                   # count line, comment line
+        for i in range(nw):
+            t = lines[pos].split()
+            pos += 1
+            out[s, i] = [float(x) for x in t[1:4]]
+        pos += n_atoms
+    return out
+
+
+def write_klist(path, k: np.ndarray):
+    np.savetxt(path, np.atleast_2d(k), fmt="%.16e")
+
+
+def read_klist(path, n_k: int, shift=(0.0, 0.0, 0.0)) -> np.ndarray:
+    k = np.loadtxt(path).reshape(-1, 3)[:n_k]
+    return k + np.asarray(shift)[None, :]
+
+
+def write_model_files(model: TBModel, directory, seedname: str, atoms=None):
+    """Write lattice, atoms, hr.dat and centres.xyz for a model; returns the paths."""
+    os.makedirs(directory, exist_ok=True)
+    atoms = model.centres[0] if atoms is None else atoms
+    paths = {
+        "lattice": os.path.join(directory, f"bravais.lattice_{seedname}.data"),
+        "atoms": os.path.join(directory, f"atoms_{seedname}.data"),
+        "hr": os.path.join(directory, f"{seedname}_hr.dat"),
+        "centres": os.path.join(directory, f"{seedname}_centres.xyz"),
+    }
+    write_lattice(paths["lattice"], model.lattice)
+    write_atoms(paths["atoms"], atoms)
+    write_hr(paths["hr"], model)
+    write_centres(paths["centres"], model, atoms)
+    return paths
+
+
+def read_model_files(paths, nw: int, n_r: int, n_atoms: int, n_spin: int = 1,
+                     dim: int = 3, name: str = "model") -> TBModel:
+    lat = read_lattice(paths["lattice"])
+    r_cryst, weights, h_r = read_hr(paths["hr"], nw, n_r, n_spin)
+    centres = read_centres(paths["centres"], nw, n_atoms, n_spin)
+    return TBModel(lattice=lat, r_cryst=r_cryst, weights=weights, h_r=h_r,
+                   centres=centres, dim=dim, name=name)

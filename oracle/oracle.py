@@ -1,0 +1,166 @@
+"""Python driver of the CPU FP64 oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm use
+this module, as the checker.  It calls the C++ restatement in bse_oracle.cpp for the
+band states, pair densities and kernel build, and LAPACK zheevd through
+scipy.linalg.eigh(driver="evd") for the dense solve -- the routine Armadillo's
+eig_sym dispatches to in Excitonic_Hamiltonian::common_diagonalization
+(bse.version13.cpp:3330).  Parity against the reference binary is UNPINNED (the
+reference cannot be built here); see the header of bse_oracle.cpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import importlib.util
+import os
+import sys
+import time
+
+import numpy as np
+import scipy.linalg
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, HERE)
+import build_oracle  # noqa: E402
+
+
+def _pkg():
+    if "bse_gb300" in sys.modules:
+        return sys.modules["bse_gb300"]
+    pdir = os.path.join(ROOT, "bethe-salpeter-equation_gb300")
+    spec = importlib.util.spec_from_file_location("bse_gb300", os.path.join(pdir, "__init__.py"),
+                                                  submodule_search_locations=[pdir])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["bse_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = build_oracle.build()
+        L = C.CDLL(path)
+        dp = C.POINTER(C.c_double)
+        capi = _pkg().capi
+        L.oracle_bands.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams), dp, dp, dp, dp]
+        L.oracle_build.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams), dp, dp, dp, dp, dp, dp]
+        L.oracle_prefactor.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams)]
+        L.oracle_prefactor.restype = C.c_double
+        L.oracle_oscillators.argtypes = [C.c_int64, C.c_int64, dp, dp, dp]
+        L.oracle_eps.argtypes = [C.c_int64, dp, dp, C.c_double, dp, C.c_int32, C.c_double, dp, dp]
+        L.oracle_num_threads.restype = C.c_int
+        _LIB = L
+    return _LIB
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _check(st):
+    if st != 0:
+        raise OracleError(f"oracle status {st}")
+
+
+def bands(prob, **overrides):
+    """(e_c [2,nk,nc], e_v [2,nk,nv], c_c [nk,nc,nb], c_v [nk,nv,nb]); c at k, v at k-q."""
+    M = _pkg().capi.Marshalled(prob, **overrides)
+    ec, ev, cc, cv = M.band_buffers()
+    p = _pkg().capi.ptr
+    _check(lib().oracle_bands(C.byref(M.model), C.byref(M.params), p(ec), p(ev), p(cc), p(cv)))
+    return ec, ev, cc, cv
+
+
+def build(prob, band_states=None, **overrides):
+    """Full BSE matrix (n_h x n_h, spin-rotated for collinear models) and rho_cv (n_rho x ng)."""
+    M = _pkg().capi.Marshalled(prob, **overrides)
+    if band_states is None:
+        band_states = bands(prob, **overrides)
+    ec, ev, cc, cv = [np.ascontiguousarray(x) for x in band_states]
+    H = np.zeros((M.n_h, M.n_h), np.complex128, order="F")
+    rho = np.zeros((M.ng, M.n_rho), np.complex128)      # C order (ng, n_rho) == column-major n_rho x ng
+    p = _pkg().capi.ptr
+    Hc = np.zeros((M.n_h, M.n_h), np.complex128)         # C buffer, filled column-major
+    _check(lib().oracle_build(C.byref(M.model), C.byref(M.params), p(ec), p(ev), p(cc), p(cv),
+                              p(Hc), p(rho)))
+    H = Hc.T                                             # column-major -> numpy (row, col)
+    return H, rho.T
+
+
+def prefactor(prob, **overrides):
+    M = _pkg().capi.Marshalled(prob, **overrides)
+    return float(lib().oracle_prefactor(C.byref(M.model), C.byref(M.params)))
+
+
+def split_blocks(H, n_bse):
+    """Collinear models: H0 = rotated spin-flip blocks {1,2}, H1 = spin-conserving {0,3}
+    (common_diagonalization, bse.version13.cpp:3143-3149)."""
+    N = n_bse
+    idx0 = np.r_[N:3 * N]
+    idx1 = np.r_[0:N, 3 * N:4 * N]
+    return H[np.ix_(idx0, idx0)], H[np.ix_(idx1, idx1)]
+
+
+def eigh(H, eigvals_only=False):
+    """LAPACK zheevd (or cheevd for complex64), ascending."""
+    if eigvals_only:
+        return scipy.linalg.eigh(H, eigvals_only=True, driver="evd", check_finite=False)
+    return scipy.linalg.eigh(H, driver="evd", check_finite=False)
+
+
+def oscillators(rho_g0, A):
+    A = np.asfortranarray(A, dtype=np.complex128)
+    r = np.ascontiguousarray(rho_g0, dtype=np.complex128)
+    f = np.zeros(A.shape[1], np.complex128)
+    p = _pkg().capi.ptr
+    # column-major A has the same bytes as the C-ordered transpose
+    At = np.ascontiguousarray(A.T)
+    _check(lib().oracle_oscillators(A.shape[0], A.shape[1], p(r), p(At), p(f)))
+    return f
+
+
+def eps(E, f, F, omega, gamma):
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    f = np.ascontiguousarray(f, dtype=np.complex128)
+    omega = np.ascontiguousarray(omega, dtype=np.float64)
+    e2 = np.zeros(len(omega))
+    e1 = np.zeros(len(omega))
+    p = _pkg().capi.ptr
+    _check(lib().oracle_eps(len(E), p(E), p(f), F, p(omega), len(omega), gamma, p(e2), p(e1)))
+    return e2, e1
+
+
+def solve(prob, omega, gamma, band_states=None, want_vectors=True, timings=None, **overrides):
+    """Whole reference path on the CPU: bands -> build -> zheevd -> oscillators -> eps."""
+    t0 = time.perf_counter()
+    if band_states is None:
+        band_states = bands(prob, **overrides)
+    t1 = time.perf_counter()
+    H, rho = build(prob, band_states, **overrides)
+    t2 = time.perf_counter()
+    N = prob.n_bse
+    ng0 = prob.ng // 2
+    out = {"bands": band_states, "H": H, "rho": rho}
+    if prob.model.n_spin == 2:
+        H0, H1 = split_blocks(H, N)
+        E0 = eigh(H0, eigvals_only=True)
+        E1, A1 = eigh(H1)
+        E_all = np.concatenate([E0, E1])
+        E_opt, A = E1, A1
+    else:
+        E_opt, A = eigh(H)
+        E_all = E_opt
+    t3 = time.perf_counter()
+    f = oscillators(rho[:, ng0], A)
+    F = prefactor(prob, **overrides)
+    e2, e1 = eps(E_opt, f, F, omega, gamma)
+    t4 = time.perf_counter()
+    out.update(E=E_all, E_opt=E_opt, A=A, f=f, F=F, eps2=e2, eps1=e1)
+    if timings is not None:
+        timings.update(bands=t1 - t0, build=t2 - t1, eig=t3 - t2, eps=t4 - t3)
+    return out
