@@ -1,0 +1,129 @@
+// Internal declarations of the GB300 BSE library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuComplex.h>
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/bse_gpu.h"
+
+namespace bse {
+
+constexpr double kMinval = 1.0e-5;                               // bse.version13.cpp:28
+constexpr double kPi = 3.1415926535897932384626433832;           // bse.version13.cpp:29
+constexpr double kConv = (1.602176634 * 1000) / (8.8541878176);  // bse.version13.cpp:32
+constexpr int kMaxNw = 16;        // orbitals per spin channel handled by the band kernel
+constexpr int kStages = 7;
+
+// Geometry derived once from the lattice (Crystal_Lattice, bse.version13.cpp:85-124).
+struct Geometry {
+    double vol, area, lz;
+    double normal[3];
+};
+
+// Interaction parameters the device needs (Coulomb_Potential::pull + model W).
+struct Interaction {
+    int coulomb_kind, w_kind;
+    double radius, min_k2, inv_eps, rk_r0, rk_eps;
+    double nx, ny, nz, lz;   // plane normal and cell height for the 2-D kinds
+    double cell_avg;         // W at Delta k = 0, G = G0
+};
+
+// k-list structure: a lattice in crystal coordinates lets Delta k be tabulated by integer offset.
+struct DeltaMap {
+    bool on_grid = false;
+    int m[3] = {1, 1, 1};          // distinct values per crystal axis
+    double step[3] = {0, 0, 0};    // spacing per axis (crystal units)
+    int64_t n_delta = 0;           // (2m0-1)(2m1-1)(2m2-1) or nk*nk
+    std::vector<int32_t> idx;      // per k: packed integer grid coordinates (on_grid)
+};
+
+}  // namespace bse
+
+struct bse_ctx {
+    // sizes
+    int nw, ns, nb, nk, ng, nv, nc, S, nr;
+    int64_t N, n_h, n_rho, n_exc, n_opt;
+    bse_params p;
+    bse::Geometry geo;
+    bse::Interaction itx;
+    bse::DeltaMap dmap;
+    int device;
+    cudaStream_t stream = nullptr;
+    cublasHandle_t cublas = nullptr;
+    cusolverDnHandle_t cusolver = nullptr;
+    cudaEvent_t ev[2 * bse::kStages] = {};
+    double stage_ms[bse::kStages] = {};
+    int64_t launches = 0;
+    std::string err;
+
+    // model on the device
+    double* d_rcart = nullptr;   // 3 x nr
+    double* d_weights = nullptr;
+    double2* d_hr = nullptr;     // nw x nw x nr x ns
+    double* d_centres = nullptr; // 3 x nw x ns
+    double* d_k = nullptr;       // 3 x nk
+    double* d_bmat = nullptr;    // reciprocal vectors b1 b2 b3 as columns
+    int32_t* d_kidx = nullptr;   // packed grid index per k (on_grid)
+    double* d_g = nullptr;       // 3 x ng
+    int* d_status = nullptr;     // device-side status word
+
+    // band subset (conduction at k, valence at k-q)
+    double* d_ec = nullptr;      // [2][nk][nc]
+    double* d_ev = nullptr;      // [2][nk][nv]
+    double2* d_cc = nullptr;     // [nk][nc][nb]
+    double2* d_cv = nullptr;     // [nk][nv][nb]
+    bool bands_valid = false;
+
+    // kernel tables
+    double2* d_phi = nullptr;    // [n_delta][nblk][nw][nw] direct-kernel lattice sums (FP64)
+    float2* d_phi32 = nullptr;   // the same in FP32 for the mixed build
+    double2* d_X = nullptr;      // [ns][ns][nw][nw] exchange lattice sums
+    double2* d_qx = nullptr;     // [ns][ns][nw][n_rho/ns] exchange row factors  Qx[s1][s2][beta][r]
+    float2* d_qx32 = nullptr;
+    double2* d_rho = nullptr;    // n_rho x ng pair densities (column-major)
+    bool tables_valid = false;
+
+    // BSE matrix and its spectrum
+    void* d_H = nullptr;         // n_h x n_h, complex64 (MIXED) or complex128 (FP64)
+    size_t h_elem = 0;
+    double2* d_H64 = nullptr;    // MIXED refinement: FP64 lower triangle of the solved block(s)
+    void* d_blk = nullptr;       // collinear: the two 2N x 2N diagonal blocks (H0, H1)
+    bool h_valid = false;
+    double* d_E = nullptr;       // n_exc eigenvalues
+    void* d_A = nullptr;         // eigenvectors of the optically active block (n_opt x n_opt)
+    bool eig_valid = false;
+    double2* d_f = nullptr;      // n_opt oscillator strengths
+    bool osc_valid = false;
+    // workspaces
+    void* d_work = nullptr;
+    size_t work_bytes = 0;
+};
+
+namespace bse {
+
+// --- helpers (host) ---
+int fail(bse_ctx* c, int code, const std::string& msg);
+int cuda_check(bse_ctx* c, cudaError_t e, const char* what);
+int ensure_work(bse_ctx* c, size_t bytes);
+void stage_begin(bse_ctx* c, int s);
+void stage_end(bse_ctx* c, int s);
+
+// --- stages (each returns a bse_status) ---
+int run_bands(bse_ctx* c);
+int run_tables(bse_ctx* c);
+int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out);
+int run_eig(bse_ctx* c);
+int run_refine(bse_ctx* c);
+int run_oscillators(bse_ctx* c);
+int run_eps(bse_ctx* c, const double* omega, int n_omega, double gamma, double* eps2, double* eps1);
+
+// own dense eigensolver (eigensolve.cu)
+int own_heevd(bse_ctx* c, int n, void* dA, int lda, bool fp64, double* dW, bool vectors);
+
+}  // namespace bse

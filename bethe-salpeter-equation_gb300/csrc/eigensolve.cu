@@ -1,0 +1,195 @@
+// Stage c: dense Hermitian eigensolve of the BSE matrix and the FP64 refinement.
+//
+// Replaces Excitonic_Hamiltonian::common_diagonalization (bse.version13.cpp:3120-3368):
+// eig_sym (LAPACK zheevd) on the TDA matrix, ascending order, unit eigenvectors; for
+// collinear spin the rotated spin-flip block H0 and the spin-conserving block H1 are
+// solved separately (3143-3149, 3195-3204).
+//
+// Solvers: BSE_EIG_OWN runs this library's tridiagonal reduction + bisection + inverse
+// iteration (tridiag.cu); BSE_EIG_CUSOLVER calls cuSOLVER's heevd (the plain library path,
+// used as the FP64 GPU baseline).  In BSE_MIXED the solve runs on the complex64 matrix
+// and the lowest n_refine eigenpairs are then refined in FP64 by one Rayleigh-Ritz step
+// on the FP64 matrix (CholeskyQR2 orthonormalisation, H*X, projected m x m solve).
+#include "bse_internal.h"
+
+namespace bse {
+namespace {
+
+const int kGuard = 32;   // extra Ritz vectors above n_refine so the last refined ones converge
+
+__global__ void widen_kernel(int64_t n, const float2* __restrict__ a, double2* __restrict__ b) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < n) b[t] = make_double2(a[t].x, a[t].y);
+}
+__global__ void narrow_kernel(int64_t n, const double2* __restrict__ a, float2* __restrict__ b) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < n) b[t] = make_float2((float)a[t].x, (float)a[t].y);
+}
+__global__ void f2d_kernel(int64_t n, const float* __restrict__ a, double* __restrict__ b) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < n) b[t] = a[t];
+}
+
+int cusolver_check(bse_ctx* c, cusolverStatus_t s, const char* what) {
+    if (s == CUSOLVER_STATUS_SUCCESS) return BSE_OK;
+    if (s == CUSOLVER_STATUS_ALLOC_FAILED) return fail(c, BSE_ERR_OOM, std::string(what) + ": cuSOLVER allocation failed");
+    return fail(c, BSE_ERR_CUDA, std::string(what) + ": cuSOLVER status " + std::to_string((int)s));
+}
+int cublas_check(bse_ctx* c, cublasStatus_t s, const char* what) {
+    if (s == CUBLAS_STATUS_SUCCESS) return BSE_OK;
+    return fail(c, BSE_ERR_CUDA, std::string(what) + ": cuBLAS status " + std::to_string((int)s));
+}
+
+// cuSOLVER heevd on one matrix; eigenvalues always returned as double in dW.
+int library_heevd(bse_ctx* c, int64_t n, void* A, int64_t lda, bool fp64, double* dW, bool vectors) {
+    int st;
+    cusolverDnParams_t prm;
+    if ((st = cusolver_check(c, cusolverDnCreateParams(&prm), "params"))) return st;
+    const cudaDataType ta = fp64 ? CUDA_C_64F : CUDA_C_32F, tw = fp64 ? CUDA_R_64F : CUDA_R_32F;
+    const cusolverEigMode_t jobz = vectors ? CUSOLVER_EIG_MODE_VECTOR : CUSOLVER_EIG_MODE_NOVECTOR;
+    void* W = dW;
+    size_t wbytes = fp64 ? 0 : (size_t)n * sizeof(float);
+    size_t dws = 0, hws = 0;
+    st = cusolver_check(c, cusolverDnXsyevd_bufferSize(c->cusolver, prm, jobz, CUBLAS_FILL_MODE_LOWER, n, ta, A, lda,
+                                                       tw, W, ta, &dws, &hws), "heevd buffer size");
+    if (st) { cusolverDnDestroyParams(prm); return st; }
+    size_t need = dws + wbytes + sizeof(int) + 256;
+    if ((st = ensure_work(c, need))) { cusolverDnDestroyParams(prm); return st; }
+    char* w = (char*)c->d_work;
+    int* dinfo = (int*)w;
+    float* W32 = (float*)(w + 256);
+    void* dbuf = w + 256 + ((wbytes + 255) / 256) * 256;
+    if (!fp64) W = W32;
+    std::vector<char> hbuf(hws > 0 ? hws : 1);
+    st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, jobz, CUBLAS_FILL_MODE_LOWER, n, ta, A, lda, tw, W, ta,
+                                            dbuf, dws, hbuf.data(), hws, dinfo), "heevd");
+    cusolverDnDestroyParams(prm);
+    if (st) return st;
+    if (!fp64) {
+        f2d_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, W32, dW);
+        c->launches++;
+    }
+    int info = 0;
+    if ((st = cuda_check(c, cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "heevd info"))) return st;
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "heevd sync"))) return st;
+    if (info > 0) return fail(c, BSE_ERR_NOT_CONVERGED, "heevd did not converge");
+    if (info < 0) return fail(c, BSE_ERR_BAD_INPUT, "heevd: invalid argument " + std::to_string(-info));
+    return BSE_OK;
+}
+
+int solve_one(bse_ctx* c, int64_t n, void* A, int64_t lda, bool fp64, double* dW, bool vectors) {
+    if (c->p.eig_solver == BSE_EIG_OWN) return own_heevd(c, (int)n, A, (int)lda, fp64, dW, vectors);
+    return library_heevd(c, n, A, lda, fp64, dW, vectors);
+}
+
+}  // namespace
+
+int run_eig(bse_ctx* c) {
+    int st;
+    if (!c->h_valid) return fail(c, BSE_ERR_STATE, "BSE matrix not built (diagonalize consumes it; rebuild first)");
+    stage_begin(c, 3);
+    const bool fp64 = c->p.precision == BSE_FP64;
+    if (c->S == 0) {
+        st = solve_one(c, c->N, c->d_H, c->N, fp64, c->d_E, true);
+        if (st) return st;
+        c->d_A = c->d_H;
+    } else {
+        const int64_t n2 = 2 * c->N;
+        char* b0 = (char*)c->d_blk;
+        char* b1 = b0 + (size_t)n2 * n2 * c->h_elem;
+        if ((st = solve_one(c, n2, b0, n2, fp64, c->d_E, false))) return st;          // H0: values only (3317)
+        if ((st = solve_one(c, n2, b1, n2, fp64, c->d_E + n2, true))) return st;      // H1: optically active
+        c->d_A = b1;
+    }
+    stage_end(c, 3);
+    c->h_valid = false;
+    if (!fp64 && !c->p.ipa && c->p.n_refine > 0) {
+        if ((st = run_refine(c))) return st;
+    }
+    c->eig_valid = true;
+    c->osc_valid = false;
+    return BSE_OK;
+}
+
+// One FP64 Rayleigh-Ritz step on the lowest m FP32 Ritz vectors of the optically active block.
+int run_refine(bse_ctx* c) {
+    int st;
+    stage_begin(c, 4);
+    const int64_t n = c->n_opt;
+    const int64_t m = std::min<int64_t>(n, (int64_t)c->p.n_refine + kGuard);
+    const int64_t nref = std::min<int64_t>(n, c->p.n_refine);
+    // FP64 matrix of the solved block, lower triangle
+    double2* H64 = c->d_H64;
+    size_t off = 0;
+    auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    const size_t oX = carve(n * m * sizeof(double2)), oY = carve(n * m * sizeof(double2));
+    const size_t oG = carve(m * m * sizeof(double2)), oT = carve(m * sizeof(double));
+    const size_t oB = c->S ? carve((size_t)n * n * sizeof(double2)) : 0;
+    // potrf / heevd workspaces on top
+    cusolverDnParams_t prm;
+    if ((st = cusolver_check(c, cusolverDnCreateParams(&prm), "params"))) return st;
+    size_t dws1 = 0, hws1 = 0, dws2 = 0, hws2 = 0;
+    if ((st = cusolver_check(c, cusolverDnXpotrf_bufferSize(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, nullptr, m,
+                                                            CUDA_C_64F, &dws1, &hws1), "potrf size"))) return st;
+    if ((st = cusolver_check(c, cusolverDnXsyevd_bufferSize(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m,
+                                                            CUDA_C_64F, nullptr, m, CUDA_R_64F, nullptr, CUDA_C_64F, &dws2, &hws2),
+                             "heevd size"))) return st;
+    const size_t oW = carve(std::max(dws1, dws2) + 256);
+    if ((st = ensure_work(c, off))) return st;
+    char* base = (char*)c->d_work;
+    double2* X = (double2*)(base + oX);
+    double2* Y = (double2*)(base + oY);
+    double2* G = (double2*)(base + oG);
+    double* theta = (double*)(base + oT);
+    int* dinfo = (int*)(base + oW);
+    void* dws = base + oW + 256;
+    std::vector<char> hws(std::max<size_t>(std::max(hws1, hws2), 1));
+    if (c->S) {
+        // collinear: FP64 H1 = blocks {0,3} of the rotated FP64 matrix
+        double2* B = (double2*)(base + oB);
+        const int64_t N = c->N, ld = 4 * N;
+        for (int bj = 0; bj < 2; bj++)
+            for (int bi = 0; bi < 2; bi++) {
+                const double2* src = H64 + (bi * 3 * N) + ld * (bj * 3 * N);
+                double2* dst = B + bi * N + n * (bj * N);
+                if ((st = cuda_check(c, cudaMemcpy2DAsync(dst, n * sizeof(double2), src, ld * sizeof(double2), N * sizeof(double2), N,
+                                                          cudaMemcpyDeviceToDevice, c->stream), "H1 gather"))) return st;
+            }
+        H64 = B;
+    }
+    // X = widen(A[:, :m])
+    widen_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, c->stream>>>(n * m, (const float2*)c->d_A, X);
+    c->launches++;
+    const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
+    const double done = 1.0, dzero = 0.0;
+    cublasSetStream(c->cublas, c->stream);
+    cusolverDnSetStream(c->cusolver, c->stream);
+    for (int pass = 0; pass < 2; pass++) {   // CholeskyQR2
+        if ((st = cublas_check(c, cublasZherk(c->cublas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, m, n, &done, (cuDoubleComplex*)X, n,
+                                              &dzero, (cuDoubleComplex*)G, m), "herk"))) return st;
+        if ((st = cusolver_check(c, cusolverDnXpotrf(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m, CUDA_C_64F,
+                                                     dws, dws1, hws.data(), hws1, dinfo), "potrf"))) return st;
+        if ((st = cublas_check(c, cublasZtrsm(c->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
+                                              n, m, &one, (cuDoubleComplex*)G, m, (cuDoubleComplex*)X, n), "trsm"))) return st;
+    }
+    // Y = H X (Hermitian, lower triangle);  G = X^H Y
+    if ((st = cublas_check(c, cublasZhemm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, n, m, &one, (cuDoubleComplex*)H64, n,
+                                          (cuDoubleComplex*)X, n, &zero, (cuDoubleComplex*)Y, n), "hemm"))) return st;
+    if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, m, m, n, &one, (cuDoubleComplex*)X, n,
+                                          (cuDoubleComplex*)Y, n, &zero, (cuDoubleComplex*)G, m), "gemm XhY"))) return st;
+    if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m,
+                                                 CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo), "heevd m"))) return st;
+    cusolverDnDestroyParams(prm);
+    // Y = X Z  (refined Ritz vectors)
+    if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, (cuDoubleComplex*)X, n,
+                                          (cuDoubleComplex*)G, m, &zero, (cuDoubleComplex*)Y, n), "gemm XZ"))) return st;
+    // write back the lowest nref pairs
+    double* E = c->S ? c->d_E + 2 * c->N : c->d_E;
+    if ((st = cuda_check(c, cudaMemcpyAsync(E, theta, nref * sizeof(double), cudaMemcpyDeviceToDevice, c->stream), "theta"))) return st;
+    narrow_kernel<<<(unsigned)((n * nref + 255) / 256), 256, 0, c->stream>>>(n * nref, Y, (float2*)c->d_A);
+    c->launches++;
+    stage_end(c, 4);
+    return cuda_check(c, cudaGetLastError(), "refine");
+}
+
+}  // namespace bse

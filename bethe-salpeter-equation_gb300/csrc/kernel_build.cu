@@ -1,0 +1,585 @@
+// Stage b: pair densities and the excitonic kernel build.
+//
+// Replaces Excitonic_Hamiltonian::pull_coulomb_potentials (model-W modes,
+// bse.version13.cpp:2547-2766), Dipole_Elements::pull_values with the point-like M
+// (1459-1501, 1922-2158) and pull_resonant_part_and_rcv (2767-2928).
+//
+// With point-like Wannier centres tau the pair densities of the reference factor:
+//   rho_cv(k,G)          = sum_a P[r,(aa)] e^{i(G+q).tau_a},     P[r,(ab)] = conj(c_ca(k)) c_vb(k-q)
+//   rho_cc(k2,k1,G)*     = sum_a c_c2a(k2) conj(c_c1a(k1)) e^{-i(G+dk).tau_a}   (dk = k2 - k1)
+// so the direct and exchange kernels become small lattice sums per Delta k:
+//   H_d[r1,r2] = -1/(V nk) sum_ab P[r1,(ab)] Phi_ab(dk) conj(P[r2,(ab)]),
+//                Phi_ab(dk) = sum_G W_G(dk) e^{-i(G+dk).(tau_a - tau_b)}
+//   H_x[r1,r2] = sf/(V nk) sum_ab P[r1,(aa)] X_ab conj(P[r2,(bb)]),
+//                X_ab = sum_{G != G0} v(q+G) e^{i(G+q).(tau_a - tau_b)}
+// (same values as the reference's G-sums over stored all-pairs densities -- the oracle
+// keeps those loops).  Phi is tabulated once per distinct Delta k (on a k-grid there are
+// (2n-1)^d of them); the build kernel then writes each element of H exactly once, k1
+// fastest so that a warp stores 32 consecutive elements of one column: the kernel is
+// bound by the N^2 store of H, not by arithmetic (inner dimension nw <= 16).
+#include "bse_internal.h"
+
+namespace bse {
+namespace {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+
+// Coulomb_Potential::pull (bse.version13.cpp:1273-1309) and the 2-D kinds.
+__device__ double dev_coulomb(const Interaction& it, double x, double y, double z) {
+    if (it.coulomb_kind == BSE_V_BARE_3D) {
+        double k2 = x * x + y * y + z * z;
+        if (k2 < it.min_k2) return 0.0;
+        return kConv / (k2 + it.radius);
+    }
+    double qn = x * it.nx + y * it.ny + z * it.nz;
+    double px = x - qn * it.nx, py = y - qn * it.ny, pz = z - qn * it.nz;
+    double k2 = px * px + py * py + pz * pz;
+    if (k2 < it.min_k2 || k2 == 0.0) return 0.0;
+    return kConv * it.lz / (2.0 * sqrt(k2));
+}
+
+__device__ double dev_rk(const Interaction& it, double x, double y, double z) {
+    double qn = x * it.nx + y * it.ny + z * it.nz;
+    double px = x - qn * it.nx, py = y - qn * it.ny, pz = z - qn * it.nz;
+    double k2 = px * px + py * py + pz * pz;
+    if (k2 < it.min_k2 || k2 == 0.0) return 0.0;
+    double a = sqrt(k2);
+    return kConv * it.lz / (2.0 * a * (it.rk_eps + it.rk_r0 * a));
+}
+
+// W_GG(dk) of the model-W modes, diagonal in G (bse.version13.cpp:2573-2728, Q7/Q8).
+__device__ double dev_w(const Interaction& it, double dx, double dy, double dz,
+                        const double* G, bool is_g0) {
+    const double x = dx + G[0], y = dy + G[1], z = dz + G[2];
+    if (it.w_kind == BSE_W_BARE) return dev_coulomb(it, x, y, z);
+    const double ndk = sqrt(dx * dx + dy * dy + dz * dz);
+    if (!(ndk > kMinval) && is_g0)
+        return it.w_kind == BSE_W_EMPIRICAL ? it.inv_eps * it.cell_avg : it.cell_avg;
+    if (it.w_kind == BSE_W_EMPIRICAL) {
+        double s = sqrt(dev_coulomb(it, x, y, z));
+        return it.inv_eps * s * s;
+    }
+    return dev_rk(it, x, y, z);
+}
+
+struct ExcSpin { int v, c; };
+__constant__ ExcSpin c_exc_spin[4] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};   // bse.version13.cpp:2522-2526
+
+// Delta-k of table entry d (grid offsets or explicit k pair), cartesian.
+__device__ void delta_k(int64_t d, bool on_grid, int m0, int m1, int m2, const double* step,
+                        const double* bmat, const double* kcart, int nk, double* dk) {
+    if (on_grid) {
+        const int w0 = 2 * m0 - 1, w1 = 2 * m1 - 1;
+        const int d0 = (int)(d % w0) - (m0 - 1);
+        const int d1 = (int)((d / w0) % w1) - (m1 - 1);
+        const int d2 = (int)(d / ((int64_t)w0 * w1)) - (m2 - 1);
+        const double c0 = d0 * step[0], c1 = d1 * step[1], c2 = d2 * step[2];
+        for (int x = 0; x < 3; x++) dk[x] = bmat[x] * c0 + bmat[3 + x] * c1 + bmat[6 + x] * c2;
+    } else {
+        const int k2 = (int)(d / nk), k1 = (int)(d % nk);
+        for (int x = 0; x < 3; x++) dk[x] = kcart[3 * k2 + x] - kcart[3 * k1 + x];
+    }
+}
+
+// Phi[d][blk][a][b] = sum_G W_G(dk) e^{-i (G + dk).(tau^{sc}_a - tau^{sv}_b)}
+__global__ void phi_table_kernel(int64_t n_delta, int nblk, int nw, int stride, int ng, Interaction it,
+                                 bool on_grid, int m0, int m1, int m2, double s0, double s1, double s2,
+                                 const double* __restrict__ bmat, const double* __restrict__ kcart, int nk,
+                                 const double* __restrict__ gcart, const double* __restrict__ centres,
+                                 double2* __restrict__ phi, float2* __restrict__ phi32) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t total = n_delta * nblk * nw * nw;
+    if (t >= total) return;
+    const int b = (int)(t % nw), a = (int)((t / nw) % nw);
+    const int blk = (int)((t / ((int64_t)nw * nw)) % nblk);
+    const int64_t d = t / ((int64_t)nw * nw * nblk);
+    const double step[3] = {s0, s1, s2};
+    double dk[3];
+    delta_k(d, on_grid, m0, m1, m2, step, bmat, kcart, nk, dk);
+    const double* ta = centres + 3 * ((size_t)c_exc_spin[blk].c * nw + a);
+    const double* tb = centres + 3 * ((size_t)c_exc_spin[blk].v * nw + b);
+    const double dx = ta[0] - tb[0], dy = ta[1] - tb[1], dz = ta[2] - tb[2];
+    const int g0 = ng / 2;
+    double re = 0, im = 0;
+    for (int g = 0; g < ng; g++) {
+        const double* G = gcart + 3 * g;
+        double w = dev_w(it, dk[0], dk[1], dk[2], G, g == g0);
+        double ph = -((G[0] + dk[0]) * dx + (G[1] + dk[1]) * dy + (G[2] + dk[2]) * dz);
+        double sn, cs;
+        sincos(ph, &sn, &cs);
+        re += w * cs;
+        im += w * sn;
+    }
+    const size_t o = (((size_t)d * nblk + blk) * stride + a) * stride + b;
+    phi[o] = make_double2(re, im);
+    if (phi32) phi32[o] = make_float2((float)re, (float)im);
+}
+
+// X[s1][s2][a][b] = sum_{G != G0} v(q+G) e^{i (G+q).(tau^{s1}_a - tau^{s2}_b)}
+__global__ void exchange_table_kernel(int ns, int nw, int ng, Interaction it, double q0, double q1, double q2,
+                                      const double* __restrict__ gcart, const double* __restrict__ centres,
+                                      double2* __restrict__ X) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns * ns * nw * nw) return;
+    const int b = t % nw, a = (t / nw) % nw, s2 = (t / (nw * nw)) % ns, s1 = t / (nw * nw * ns);
+    const double* ta = centres + 3 * ((size_t)s1 * nw + a);
+    const double* tb = centres + 3 * ((size_t)s2 * nw + b);
+    const double dx = ta[0] - tb[0], dy = ta[1] - tb[1], dz = ta[2] - tb[2];
+    const int g0 = ng / 2;
+    double re = 0, im = 0;
+    for (int g = 0; g < ng; g++) {
+        if (g == g0) continue;                                        // bse.version13.cpp:2811-2816
+        const double* G = gcart + 3 * g;
+        double v = dev_coulomb(it, q0 + G[0], q1 + G[1], q2 + G[2]);   // bse.version13.cpp:2566-2567
+        double ph = (G[0] + q0) * dx + (G[1] + q1) * dy + (G[2] + q2) * dz;
+        double sn, cs;
+        sincos(ph, &sn, &cs);
+        re += v * cs;
+        im += v * sn;
+    }
+    X[t] = make_double2(re, im);
+}
+
+// rho_cv[s*N + r, g] (Dipole_Elements::pull_values, k-diagonal branch, 1951-2066; Q12/Q13)
+__global__ void rho_cv_kernel(int nk, int nc, int nv, int nw, int ns, int ng, int small_q,
+                              double q0, double q1, double q2,
+                              const double* __restrict__ gcart, const double* __restrict__ centres,
+                              const double2* __restrict__ cc, const double2* __restrict__ cv,
+                              double2* __restrict__ rho) {
+    const int64_t N = (int64_t)nk * nc * nv, nrho = N * ns;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nrho * ng) return;
+    const int64_t i = t % nrho;
+    const int g = (int)(t / nrho);
+    const int s = (int)(i / N);
+    const int64_t r = i % N;
+    const int k = (int)(r % nk), v = (int)((r / nk) % nv), c = (int)(r / ((int64_t)nk * nv));
+    const int nb = nw * ns;
+    const double qn = sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+    const double* G = gcart + 3 * g;
+    const bool dip = (g == ng / 2) && small_q;
+    double2 acc = make_double2(0, 0);
+    for (int a = 0; a < nw; a++) {
+        const double* ta = centres + 3 * ((size_t)s * nw + a);
+        double2 mel;
+        if (dip) {
+            mel = make_double2(0.0, (q0 * ta[0] + q1 * ta[1] + q2 * ta[2]) / qn);
+        } else {
+            double ph = ta[0] * (G[0] + q0) + ta[1] * (G[1] + q1) + ta[2] * (G[2] + q2);
+            double sn, cs;
+            sincos(ph, &sn, &cs);
+            mel = make_double2(cs, sn);
+        }
+        double2 x = cmul(cmul(cconj(cc[((size_t)k * nc + c) * nb + s * nw + a]), mel),
+                         cv[((size_t)k * nv + v) * nb + s * nw + a]);
+        acc.x += x.x;
+        acc.y += x.y;
+    }
+    rho[i + nrho * g] = acc;
+}
+
+// Qx[s1][s2][b][r] = fx sum_a P[r,(aa)] X[s1][s2][a][b]  (exchange row factors)
+__global__ void exchange_rows_kernel(int nk, int nc, int nv, int nw, int ns, double fx,
+                                     const double2* __restrict__ cc, const double2* __restrict__ cv,
+                                     const double2* __restrict__ X, double2* __restrict__ qx,
+                                     float2* __restrict__ qx32) {
+    const int64_t N = (int64_t)nk * nc * nv;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= N * nw * ns * ns) return;
+    const int64_t r = t % N;
+    const int b = (int)((t / N) % nw);
+    const int s2 = (int)((t / (N * nw)) % ns), s1 = (int)(t / (N * nw * ns));
+    const int k = (int)(r % nk), v = (int)((r / nk) % nv), c = (int)(r / ((int64_t)nk * nv));
+    const int nb = nw * ns;
+    double2 acc = make_double2(0, 0);
+    for (int a = 0; a < nw; a++) {
+        double2 pr = cmul(cconj(cc[((size_t)k * nc + c) * nb + s1 * nw + a]), cv[((size_t)k * nv + v) * nb + s1 * nw + a]);
+        double2 x = cmul(pr, X[((s1 * ns + s2) * nw + a) * nw + b]);
+        acc.x += x.x;
+        acc.y += x.y;
+    }
+    acc.x *= fx;
+    acc.y *= fx;
+    qx[t] = acc;
+    if (qx32) qx32[t] = make_float2((float)acc.x, (float)acc.y);
+}
+
+template <typename T> struct cplx;
+template <> struct cplx<float> { typedef float2 t; };
+template <> struct cplx<double> { typedef double2 t; };
+
+template <typename T2> __device__ __forceinline__ T2 mk(double x, double y);
+template <> __device__ __forceinline__ float2 mk<float2>(double x, double y) { return make_float2((float)x, (float)y); }
+template <> __device__ __forceinline__ double2 mk<double2>(double x, double y) { return make_double2(x, y); }
+
+template <typename T2>
+__device__ __forceinline__ void cfma(T2& acc, T2 a, T2 b) {   // acc += a * b
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+template <typename T2>
+__device__ __forceinline__ void cfma_conjb(T2& acc, T2 a, T2 b) {   // acc += a * conj(b)
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.y, b.x, acc.y);
+    acc.y = fma(-a.x, b.y, acc.y);
+}
+template <typename T2>
+__device__ __forceinline__ T2 tmul(T2 a, T2 b) {
+    T2 r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+
+struct BuildArgs {
+    int nk, nc, nv, nw, ns;
+    int64_t N, ld;
+    int br, bc;                 // row / column spin block of this launch
+    int do_direct, do_exch, do_diag, lower;
+    float fw_f;
+    double fw;
+    bool on_grid;
+    int m0, m1, m2;
+    int nblk;
+    const int32_t* kidx;
+    const double* ec;
+    const double* ev;
+    const double2* cc;
+    const double2* cv;
+};
+
+// One thread per (k1, k2): lane = k1 (consecutive rows of one column), warp = k2.
+template <int NW, typename T>
+__global__ void __launch_bounds__(256) build_kernel(BuildArgs a, const typename cplx<T>::t* __restrict__ phi,
+                                                    const typename cplx<T>::t* __restrict__ qx,
+                                                    typename cplx<T>::t* __restrict__ H) {
+    typedef typename cplx<T>::t T2;
+    extern __shared__ unsigned char smem_raw[];
+    const int lane = threadIdx.x, warp = threadIdx.y, KW = blockDim.y;
+    const int nb = a.nw * a.ns;
+    T2* sC = reinterpret_cast<T2*>(smem_raw) + (size_t)warp * (a.nc + a.nv) * nb;   // [nc+nv][nb] of k2
+    const int k1 = blockIdx.x * 32 + lane;
+    const int k2 = blockIdx.y * KW + warp;
+    if (k2 < a.nk) {
+        for (int i = lane; i < a.nc * nb; i += 32) {
+            double2 x = a.cc[(size_t)k2 * a.nc * nb + i];
+            sC[i] = mk<T2>(x.x, x.y);
+        }
+        for (int i = lane; i < a.nv * nb; i += 32) {
+            double2 x = a.cv[(size_t)k2 * a.nv * nb + i];
+            sC[a.nc * nb + i] = mk<T2>(x.x, x.y);
+        }
+    }
+    __syncwarp();
+    if (k1 >= a.nk || k2 >= a.nk) return;
+
+    const int sc = c_exc_spin[a.br].c, sv = c_exc_spin[a.br].v;   // direct: diagonal spin block br
+    const int s1 = a.br / 3, s2 = a.bc / 3;                        // exchange: blocks 0 / 3
+    int64_t d;
+    if (a.on_grid) {
+        const int x1 = a.kidx[k1], x2 = a.kidx[k2];
+        const int i0 = (x2 & 1023) - (x1 & 1023), i1 = ((x2 >> 10) & 1023) - ((x1 >> 10) & 1023);
+        const int i2 = ((x2 >> 20) & 1023) - ((x1 >> 20) & 1023);
+        d = (int64_t)(i0 + a.m0 - 1) + (int64_t)(2 * a.m0 - 1) * ((i1 + a.m1 - 1) + (int64_t)(2 * a.m1 - 1) * (i2 + a.m2 - 1));
+    } else {
+        d = (int64_t)k2 * a.nk + k1;
+    }
+    const T2* ph = phi ? phi + ((size_t)d * a.nblk + a.br) * NW * NW : nullptr;
+    const T2* sCc2 = sC;
+    const T2* sCv2 = sC + (size_t)a.nc * nb;
+    const T fw = (T)a.fw;
+
+    for (int c1 = 0; c1 < a.nc; c1++) {
+        T2 ca[NW];
+        for (int al = 0; al < NW; al++) {
+            double2 x = al < a.nw ? a.cc[((size_t)k1 * a.nc + c1) * nb + sc * a.nw + al] : make_double2(0, 0);
+            ca[al] = mk<T2>(x.x, -x.y);                              // conj(c_c1(k1))
+        }
+        for (int c2 = 0; c2 < a.nc; c2++) {
+            T2 S[NW];
+            for (int b = 0; b < NW; b++) S[b] = mk<T2>(0, 0);
+            if (a.do_direct) {
+                for (int al = 0; al < a.nw; al++) {
+                    const T2 coef = tmul(ca[al], sCc2[c2 * nb + sc * a.nw + al]);
+                    const T2* prow = ph + al * NW;
+#pragma unroll
+                    for (int b = 0; b < NW; b++)
+                        if (b < a.nw) cfma(S[b], coef, prow[b]);
+                }
+            }
+            for (int v1 = 0; v1 < a.nv; v1++) {
+                const int64_t r1 = (int64_t)c1 * a.nv * a.nk + (int64_t)v1 * a.nk + k1;
+                T2 tt[NW], qq[NW];
+#pragma unroll
+                for (int b = 0; b < NW; b++) {
+                    tt[b] = mk<T2>(0, 0);
+                    qq[b] = mk<T2>(0, 0);
+                }
+                if (a.do_direct) {
+#pragma unroll
+                    for (int b = 0; b < NW; b++)
+                        if (b < a.nw) {
+                            double2 x = a.cv[((size_t)k1 * a.nv + v1) * nb + sv * a.nw + b];
+                            tt[b] = tmul(S[b], mk<T2>(x.x, x.y));
+                        }
+                }
+                if (a.do_exch) {
+#pragma unroll
+                    for (int b = 0; b < NW; b++)
+                        if (b < a.nw) qq[b] = qx[((size_t)(s1 * a.ns + s2) * a.nw + b) * a.N + r1];
+                }
+                for (int v2 = 0; v2 < a.nv; v2++) {
+                    const int cv1 = c1 * a.nv + v1, cv2 = c2 * a.nv + v2;
+                    if (a.lower && (cv1 < cv2 || (cv1 == cv2 && k1 < k2))) continue;
+                    const int64_t r2 = (int64_t)c2 * a.nv * a.nk + (int64_t)v2 * a.nk + k2;
+                    T2 acc = mk<T2>(0, 0), accx = mk<T2>(0, 0);
+                    if (a.do_direct) {
+#pragma unroll
+                        for (int b = 0; b < NW; b++)
+                            if (b < a.nw) cfma_conjb(acc, tt[b], sCv2[v2 * nb + sv * a.nw + b]);
+                    }
+                    if (a.do_exch) {
+#pragma unroll
+                        for (int b = 0; b < NW; b++)
+                            if (b < a.nw) {
+                                // D2 = conj(c_c2b(k2)) c_v2b(k2-q);  H_x += qx * conj(D2)
+                                const T2 d2 = tmul(mk<T2>(sCc2[c2 * nb + s2 * a.nw + b].x, -sCc2[c2 * nb + s2 * a.nw + b].y),
+                                                   sCv2[v2 * nb + s2 * a.nw + b]);
+                                cfma_conjb(accx, qq[b], d2);
+                            }
+                    }
+                    T2 out;
+                    out.x = fw * acc.x + accx.x;
+                    out.y = fw * acc.y + accx.y;
+                    if (a.do_diag && k1 == k2 && c1 == c2 && v1 == v2) {
+                        const int cs = c_exc_spin[a.br].c, vs = c_exc_spin[a.br].v;
+                        out.x += (T)(a.ec[((size_t)cs * a.nk + k1) * a.nc + c1] - a.ev[((size_t)vs * a.nk + k1) * a.nv + v1]);
+                    }
+                    H[(a.br * a.N + r1) + a.ld * (a.bc * a.N + r2)] = out;
+                }
+            }
+        }
+    }
+}
+
+// Collinear spin rotation U H U (spin_transformation, bse.version13.cpp:3048-3117), in place per
+// (row, col) position across the 4x4 spin blocks, so no block reads an already rotated one (Q24).
+template <typename T2>
+__global__ void spin_rotate_kernel(int64_t N, T2* __restrict__ H) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= N * N) return;
+    const int64_t rr = t % N, cc = t / N, ld = 4 * N;
+    const double h = 0.70710678118654752440;
+    const double U[4][4] = {{1, 0, 0, 0}, {0, h, h, 0}, {0, h, -h, 0}, {0, 0, 0, 1}};
+    double xr[4][4], xi[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            T2 v = H[(i * N + rr) + ld * (j * N + cc)];
+            xr[i][j] = v.x;
+            xi[i][j] = v.y;
+        }
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            double sr = 0, si = 0;
+            for (int l = 0; l < 4; l++)
+                for (int k = 0; k < 4; k++) {
+                    double w = U[i][l] * U[k][j];
+                    sr += w * xr[l][k];
+                    si += w * xi[l][k];
+                }
+            T2 o;
+            o.x = sr;
+            o.y = si;
+            H[(i * N + rr) + ld * (j * N + cc)] = o;
+        }
+}
+
+// Gather the collinear diagonal blocks: H0 = rotated blocks {1,2}, H1 = blocks {0,3}
+// (common_diagonalization, bse.version13.cpp:3143-3149).
+template <typename T2>
+__global__ void gather_blocks_kernel(int64_t N, const T2* __restrict__ H, T2* __restrict__ H0, T2* __restrict__ H1) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t n2 = 2 * N;
+    if (t >= n2 * n2) return;
+    const int64_t i = t % n2, j = t / n2, ld = 4 * N;
+    const int64_t i0 = i + N, j0 = j + N;                       // blocks 1,2
+    const int64_t i1 = i < N ? i : i + 2 * N, j1 = j < N ? j : j + 2 * N;   // blocks 0,3
+    H0[t] = H[i0 + ld * j0];
+    H1[t] = H[i1 + ld * j1];
+}
+
+template <int NW, typename T>
+int launch_build_nw(bse_ctx* c, void* H, int64_t ld, bool lower, const void* phi, const void* qx,
+                    int br, int bc, int do_direct, int do_exch, int do_diag) {
+    BuildArgs a;
+    a.nk = c->nk; a.nc = c->nc; a.nv = c->nv; a.nw = c->nw; a.ns = c->ns;
+    a.N = c->N; a.ld = ld; a.br = br; a.bc = bc;
+    a.do_direct = do_direct; a.do_exch = do_exch; a.do_diag = do_diag; a.lower = lower ? 1 : 0;
+    a.fw = -1.0 / (c->geo.vol * c->nk);   // bse.version13.cpp:2845
+    a.fw_f = (float)a.fw;
+    a.on_grid = c->dmap.on_grid;
+    a.m0 = c->dmap.m[0]; a.m1 = c->dmap.m[1]; a.m2 = c->dmap.m[2];
+    a.nblk = 3 * c->S + 1;
+    a.kidx = c->d_kidx;
+    a.ec = c->d_ec; a.ev = c->d_ev; a.cc = c->d_cc; a.cv = c->d_cv;
+    const int KW = 8;
+    dim3 block(32, KW), grid((c->nk + 31) / 32, (c->nk + KW - 1) / KW, 1);
+    size_t smem = (size_t)KW * (c->nc + c->nv) * c->nb * sizeof(typename cplx<T>::t);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(build_kernel<NW, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_check(c, e, "build smem attribute");
+    }
+    build_kernel<NW, T><<<grid, block, smem, c->stream>>>(
+        a, (const typename cplx<T>::t*)phi, (const typename cplx<T>::t*)qx, (typename cplx<T>::t*)H);
+    c->launches++;
+    return cuda_check(c, cudaGetLastError(), "build kernel launch");
+}
+
+template <typename T>
+int launch_build(bse_ctx* c, void* H, int64_t ld, bool lower, const void* phi, const void* qx,
+                 int br, int bc, int dd, int de, int dg) {
+    // phi rows are padded to NW entries: the table is laid out with stride NW == the template
+    if (c->nw <= 2) return launch_build_nw<2, T>(c, H, ld, lower, phi, qx, br, bc, dd, de, dg);
+    if (c->nw <= 4) return launch_build_nw<4, T>(c, H, ld, lower, phi, qx, br, bc, dd, de, dg);
+    if (c->nw <= 8) return launch_build_nw<8, T>(c, H, ld, lower, phi, qx, br, bc, dd, de, dg);
+    return launch_build_nw<16, T>(c, H, ld, lower, phi, qx, br, bc, dd, de, dg);
+}
+
+}  // namespace
+
+int table_stride(int nw) { return nw <= 2 ? 2 : nw <= 4 ? 4 : nw <= 8 ? 8 : 16; }
+
+int run_tables(bse_ctx* c) {
+    int st;
+    stage_begin(c, 1);
+    const int ns = c->ns, nw = c->nw, ng = c->ng;
+    // rho_cv
+    {
+        const int64_t total = c->n_rho * ng;
+        const int thr = 256;
+        rho_cv_kernel<<<(unsigned)((total + thr - 1) / thr), thr, 0, c->stream>>>(
+            c->nk, c->nc, c->nv, nw, ns, ng, c->p.small_momentum, c->p.q[0], c->p.q[1], c->p.q[2],
+            c->d_g, c->d_centres, c->d_cc, c->d_cv, c->d_rho);
+        c->launches++;
+        if ((st = cuda_check(c, cudaGetLastError(), "rho kernel"))) return st;
+    }
+    if (!c->p.ipa) {
+        const int NWs = table_stride(nw);
+        // exchange lattice sums and row factors
+        exchange_table_kernel<<<(ns * ns * nw * nw + 127) / 128, 128, 0, c->stream>>>(
+            ns, nw, ng, c->itx, c->p.q[0], c->p.q[1], c->p.q[2], c->d_g, c->d_centres, c->d_X);
+        c->launches++;
+        const double sf = c->p.spin_factor >= 0 ? c->p.spin_factor : (double)(2 - c->S);
+        const double fx = sf / (c->nk * c->geo.vol);                     // bse.version13.cpp:2801
+        const int64_t nq = c->N * nw * ns * ns;
+        exchange_rows_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, c->stream>>>(
+            c->nk, c->nc, c->nv, nw, ns, fx, c->d_cc, c->d_cv, c->d_X, c->d_qx,
+            c->p.precision == BSE_MIXED ? c->d_qx32 : nullptr);
+        c->launches++;
+        // direct lattice sums, one per distinct Delta k, rows padded to the kernel's stride
+        const int nblk = 3 * c->S + 1;
+        const int64_t total = c->dmap.n_delta * nblk * NWs * NWs;
+        if ((st = cuda_check(c, cudaMemsetAsync(c->d_phi, 0, total * sizeof(double2), c->stream), "phi clear"))) return st;
+        if (c->d_phi32 && (st = cuda_check(c, cudaMemsetAsync(c->d_phi32, 0, total * sizeof(float2), c->stream), "phi32 clear"))) return st;
+        const int64_t tk = c->dmap.n_delta * nblk * nw * nw;
+        phi_table_kernel<<<(unsigned)((tk + 255) / 256), 256, 0, c->stream>>>(
+            c->dmap.n_delta, nblk, nw, NWs, ng, c->itx, c->dmap.on_grid, c->dmap.m[0], c->dmap.m[1], c->dmap.m[2],
+            c->dmap.step[0], c->dmap.step[1], c->dmap.step[2], c->d_bmat, c->d_k, c->nk,
+            c->d_g, c->d_centres, c->d_phi, c->p.precision == BSE_MIXED ? c->d_phi32 : nullptr);
+        c->launches++;
+        if ((st = cuda_check(c, cudaGetLastError(), "phi kernel"))) return st;
+    }
+    stage_end(c, 1);
+    if ((st = cuda_check(c, cudaGetLastError(), "tables"))) return st;
+    c->tables_valid = true;
+    return BSE_OK;
+}
+
+int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
+    int st;
+    if (!c->bands_valid) return fail(c, BSE_ERR_STATE, "bands not computed");
+    if (!c->tables_valid && (st = run_tables(c))) return st;
+    stage_begin(c, 2);
+    const bool mixed = c->p.precision == BSE_MIXED;
+    const bool coll = c->S == 1;
+    const bool lower = !full && !coll && h_out == nullptr;
+    const int64_t ld = c->n_h;
+    if ((st = cuda_check(c, cudaMemsetAsync(c->d_H, 0, (size_t)ld * ld * c->h_elem, c->stream), "H clear"))) return st;
+    const int dd = c->p.ipa ? 0 : 1, de = c->p.ipa ? 0 : 1;
+    const void* phi = mixed ? (const void*)c->d_phi32 : (const void*)c->d_phi;
+    const void* qx = mixed ? (const void*)c->d_qx32 : (const void*)c->d_qx;
+    // spin-block pairs: direct + diagonal on (b,b), exchange on (0|3, 0|3)
+    int pairs[6][2] = {{0, 0}, {1, 1}, {2, 2}, {3, 3}, {0, 3}, {3, 0}};
+    const int npairs = coll ? 6 : 1;
+    for (int pi = 0; pi < npairs; pi++) {
+        const int br = pairs[pi][0], bc = pairs[pi][1];
+        const int direct = (br == bc) ? dd : 0;
+        const int exch = ((br == 0 || br == 3) && (bc == 0 || bc == 3)) ? de : 0;
+        const int diag = br == bc;
+        st = mixed ? launch_build<float>(c, c->d_H, ld, lower, phi, qx, br, bc, direct, exch, diag)
+                   : launch_build<double>(c, c->d_H, ld, lower, phi, qx, br, bc, direct, exch, diag);
+        if (st) return st;
+    }
+    if (coll) {
+        const int64_t nn = c->N * c->N;
+        if (mixed) spin_rotate_kernel<float2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, (float2*)c->d_H);
+        else spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, (double2*)c->d_H);
+        c->launches++;
+    }
+    stage_end(c, 2);
+    if ((st = cuda_check(c, cudaGetLastError(), "build"))) return st;
+    if (mixed && !c->p.ipa && c->p.n_refine > 0) {
+        // FP64 copy of the optically active block for the Rayleigh-Ritz refinement
+        const int64_t n64 = coll ? 4 * c->N : c->N;
+        if ((st = cuda_check(c, cudaMemsetAsync(c->d_H64, 0, (size_t)n64 * n64 * sizeof(double2), c->stream), "H64 clear"))) return st;
+        for (int pi = 0; pi < npairs; pi++) {
+            const int br = pairs[pi][0], bc = pairs[pi][1];
+            const int direct = (br == bc) ? dd : 0;
+            const int exch = ((br == 0 || br == 3) && (bc == 0 || bc == 3)) ? de : 0;
+            if ((st = launch_build<double>(c, c->d_H64, n64, !coll, c->d_phi, c->d_qx, br, bc, direct, exch, br == bc))) return st;
+        }
+        if (coll) {
+            const int64_t nn = c->N * c->N;
+            spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, c->d_H64);
+            c->launches++;
+        }
+    }
+    if (coll) {
+        const int64_t n2 = 2 * c->N;
+        const size_t bb = (size_t)n2 * n2 * c->h_elem;
+        if (mixed)
+            gather_blocks_kernel<float2><<<(unsigned)((n2 * n2 + 255) / 256), 256, 0, c->stream>>>(
+                c->N, (const float2*)c->d_H, (float2*)c->d_blk, (float2*)((char*)c->d_blk + bb));
+        else
+            gather_blocks_kernel<double2><<<(unsigned)((n2 * n2 + 255) / 256), 256, 0, c->stream>>>(
+                c->N, (const double2*)c->d_H, (double2*)c->d_blk, (double2*)((char*)c->d_blk + bb));
+        c->launches++;
+    }
+    if ((st = cuda_check(c, cudaGetLastError(), "build post"))) return st;
+    if (h_out) {
+        const size_t n = (size_t)ld * ld;
+        if (mixed) {
+            std::vector<float2> tmp(n);
+            if ((st = cuda_check(c, cudaMemcpyAsync(tmp.data(), c->d_H, n * sizeof(float2), cudaMemcpyDeviceToHost, c->stream), "H copy"))) return st;
+            if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "H copy sync"))) return st;
+            for (size_t i = 0; i < n; i++) { h_out[2 * i] = tmp[i].x; h_out[2 * i + 1] = tmp[i].y; }
+        } else {
+            if ((st = cuda_check(c, cudaMemcpyAsync(h_out, c->d_H, n * sizeof(double2), cudaMemcpyDeviceToHost, c->stream), "H copy"))) return st;
+        }
+    }
+    if (rho_out) {
+        if ((st = cuda_check(c, cudaMemcpyAsync(rho_out, c->d_rho, (size_t)c->n_rho * c->ng * sizeof(double2), cudaMemcpyDeviceToHost, c->stream), "rho copy"))) return st;
+    }
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "build sync"))) return st;
+    c->h_valid = true;
+    c->eig_valid = c->osc_valid = false;
+    return BSE_OK;
+}
+
+}  // namespace bse

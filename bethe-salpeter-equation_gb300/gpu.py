@@ -1,0 +1,171 @@
+"""ctypes binding of libbse_gb300.so (the C ABI of include/bse_gpu.h).
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is present, the
+calls raise.  ``BSEContext`` owns one bse_ctx and exposes every entry point of the
+header with numpy buffers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+from .capi import BseModel, BseParams, Marshalled, ptr
+from .constants import STATUS
+from .model import Problem
+
+_LIB = None
+_dp = C.POINTER(C.c_double)
+
+EXPORTS = [
+    "bse_status_string", "bse_last_error", "bse_version", "bse_sizes", "bse_set_device",
+    "bse_create", "bse_destroy", "bse_compute_bands", "bse_get_bands", "bse_set_bands",
+    "bse_build_kernel", "bse_diagonalize", "bse_oscillators", "bse_eps", "bse_solve",
+    "bse_stage_times", "bse_kernel_launches", "bse_reset_kernel_launches",
+]
+
+
+class BSEError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the CUDA library (building it with nvcc when absent)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError(f"{path} not built")
+        _build.build()
+    L = C.CDLL(path)
+    L.bse_status_string.restype = C.c_char_p
+    L.bse_status_string.argtypes = [C.c_int]
+    L.bse_last_error.restype = C.c_char_p
+    L.bse_last_error.argtypes = [C.c_void_p]
+    L.bse_sizes.argtypes = [C.POINTER(BseModel), C.POINTER(BseParams)] + [C.POINTER(C.c_int64)] * 4
+    L.bse_set_device.argtypes = [C.c_int]
+    L.bse_create.argtypes = [C.POINTER(BseModel), C.POINTER(BseParams), C.POINTER(C.c_void_p)]
+    L.bse_destroy.argtypes = [C.c_void_p]
+    L.bse_destroy.restype = None
+    L.bse_compute_bands.argtypes = [C.c_void_p]
+    L.bse_get_bands.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+    L.bse_set_bands.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+    L.bse_build_kernel.argtypes = [C.c_void_p, _dp, _dp]
+    L.bse_diagonalize.argtypes = [C.c_void_p, _dp, _dp]
+    L.bse_oscillators.argtypes = [C.c_void_p, _dp]
+    L.bse_eps.argtypes = [C.c_void_p, _dp, C.c_int32, C.c_double, _dp, _dp]
+    L.bse_solve.argtypes = [C.c_void_p, _dp, C.c_int32, C.c_double, _dp, _dp, _dp]
+    L.bse_stage_times.argtypes = [C.c_void_p, _dp, C.c_int32]
+    L.bse_kernel_launches.argtypes = [C.c_void_p]
+    L.bse_kernel_launches.restype = C.c_int64
+    L.bse_reset_kernel_launches.argtypes = [C.c_void_p]
+    L.bse_reset_kernel_launches.restype = None
+    _LIB = L
+    return L
+
+
+STAGES = ("bands", "tables", "build", "eig", "refine", "oscillators", "eps")
+
+
+class BSEContext:
+    """One bse_ctx: the model uploaded once, then the stages of the reference path."""
+
+    def __init__(self, prob: Problem, **overrides):
+        self.lib = load()
+        self.m = Marshalled(prob, **overrides)
+        self.prob = prob
+        h = C.c_void_p()
+        st = self.lib.bse_create(C.byref(self.m.model), C.byref(self.m.params), C.byref(h))
+        if st != 0:
+            raise BSEError(st, self.lib.bse_last_error(None).decode())
+        self.h = h
+
+    def _check(self, st):
+        if st != 0:
+            raise BSEError(st, self.lib.bse_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bse_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # --- stages ---------------------------------------------------------------
+    def compute_bands(self):
+        self._check(self.lib.bse_compute_bands(self.h))
+
+    def get_bands(self):
+        ec, ev, cc, cv = self.m.band_buffers()
+        self._check(self.lib.bse_get_bands(self.h, ptr(ec), ptr(ev), ptr(cc), ptr(cv)))
+        return ec, ev, cc, cv
+
+    def set_bands(self, ec, ev, cc, cv):
+        arrs = [np.ascontiguousarray(x, dtype=t) for x, t in
+                ((ec, np.float64), (ev, np.float64), (cc, np.complex128), (cv, np.complex128))]
+        self._check(self.lib.bse_set_bands(self.h, *[ptr(a) for a in arrs]))
+
+    def build_kernel(self, want_h: bool = False, want_rho: bool = False):
+        """extract_hbse_and_rcv: returns (H or None, rho_cv or None) as numpy (row, col) arrays."""
+        Hc = np.zeros((self.m.n_h, self.m.n_h), np.complex128) if want_h else None
+        rho = np.zeros((self.m.ng, self.m.n_rho), np.complex128) if want_rho else None
+        self._check(self.lib.bse_build_kernel(self.h, ptr(Hc), ptr(rho)))
+        return (Hc.T if want_h else None), (rho.T if want_rho else None)
+
+    def diagonalize(self, want_vectors: bool = False):
+        E = np.zeros(self.m.n_exc)
+        A = np.zeros((self.m.n_opt, self.m.n_opt), np.complex128) if want_vectors else None
+        self._check(self.lib.bse_diagonalize(self.h, ptr(E), ptr(A)))
+        return E, (A.T if want_vectors else None)
+
+    def oscillators(self):
+        f = np.zeros(self.m.n_opt, np.complex128)
+        self._check(self.lib.bse_oscillators(self.h, ptr(f)))
+        return f
+
+    def eps(self, omega, gamma):
+        om = np.ascontiguousarray(omega, dtype=np.float64)
+        e2 = np.zeros(len(om))
+        e1 = np.zeros(len(om))
+        self._check(self.lib.bse_eps(self.h, ptr(om), len(om), float(gamma), ptr(e2), ptr(e1)))
+        return e2, e1
+
+    def solve(self, omega, gamma):
+        om = np.ascontiguousarray(omega, dtype=np.float64)
+        E = np.zeros(self.m.n_exc)
+        e2 = np.zeros(len(om))
+        e1 = np.zeros(len(om))
+        self._check(self.lib.bse_solve(self.h, ptr(om), len(om), float(gamma), ptr(E), ptr(e2), ptr(e1)))
+        return E, e2, e1
+
+    def stage_times(self):
+        ms = np.zeros(len(STAGES))
+        self._check(self.lib.bse_stage_times(self.h, ptr(ms), len(STAGES)))
+        return dict(zip(STAGES, ms.tolist()))
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.bse_kernel_launches(self.h))
+
+    def reset_kernel_launches(self):
+        self.lib.bse_reset_kernel_launches(self.h)

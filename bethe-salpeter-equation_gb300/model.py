@@ -13,7 +13,7 @@ from typing import Optional
 import numpy as np
 
 from .constants import (MINVAL, BSE_V_BARE_3D, BSE_W_EMPIRICAL, BSE_FP64,
-                        BSE_EIG_OWN, INV_EPS_EMPIRICAL)
+                        BSE_EIG_OWN, BSE_EIG_CUSOLVER, INV_EPS_EMPIRICAL)
 
 
 def reciprocal_vectors(lattice: np.ndarray) -> np.ndarray:
@@ -107,7 +107,7 @@ class BSEParams:
     rk_eps: float = 1.0
     spin_factor: float = -1.0
     precision: int = BSE_FP64
-    eig_solver: int = BSE_EIG_OWN
+    eig_solver: int = BSE_EIG_CUSOLVER
     n_refine: int = 256
 
     def replace(self, **kw) -> "BSEParams":

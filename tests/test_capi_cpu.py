@@ -1,0 +1,89 @@
+"""CPU tests of the C ABI: the library loads, exports every function include/bse_gpu.h
+declares, and rejects bad inputs before touching a device (no compute without a GPU)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "bse_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(bse_\w+)\s*\(", src)))
+
+
+def test_library_exports_header(gpu):
+    lib = gpu.load()
+    names = _declared()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(gpu.EXPORTS) == set(names)
+
+
+def test_status_strings(gpu):
+    lib = gpu.load()
+    assert lib.bse_status_string(0) == b"BSE_OK"
+    assert lib.bse_status_string(-4) == b"BSE_ERR_NOT_CONVERGED"
+
+
+def _create(gpu, prob, **kw):
+    lib = gpu.load()
+    from bse_gb300.capi import Marshalled
+    m = Marshalled(prob, **kw)
+    h = C.c_void_p()
+    st = lib.bse_create(C.byref(m.model), C.byref(m.params), C.byref(h))
+    if st == 0:
+        lib.bse_destroy(h)
+    return st, lib.bse_last_error(None).decode()
+
+
+def test_rejects_too_many_bands(synth, gpu):
+    st, msg = _create(gpu, synth.hbn_problem(grid=2), nv=2)
+    assert st == -1 and "nv + nc" in msg
+
+
+def test_rejects_non_hermitian(synth, gpu):
+    prob = synth.hbn_problem(grid=2)
+    prob.model.h_r = prob.model.h_r.copy()
+    prob.model.h_r[0, 1, 0, 1] += 0.3j
+    st, msg = _create(gpu, prob)
+    assert st == -1 and "Hermitian" in msg
+
+
+def test_rejects_nan(synth, gpu):
+    prob = synth.hbn_problem(grid=2)
+    prob.k_cart = prob.k_cart.copy()
+    prob.k_cart[1, 0] = np.nan
+    st, msg = _create(gpu, prob)
+    assert st == -1 and "NaN" in msg
+
+
+def test_rejects_coupling_block(synth, gpu):
+    st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0)
+    assert st == -1 and "Tamm" in msg
+
+
+def test_rejects_zero_q(synth, gpu):
+    st, msg = _create(gpu, synth.hbn_problem(grid=2), q=(0.0, 0.0, 0.0))
+    assert st == -1
+
+
+def test_no_device_is_an_error_not_a_crash(synth, gpu):
+    """Here (no GPU) a valid problem yields BSE_ERR_NO_DEVICE; on a GPU machine it succeeds."""
+    st, msg = _create(gpu, synth.hbn_problem(grid=2))
+    assert st in (0, -2)
+
+
+def test_sizes(synth, gpu):
+    lib = gpu.load()
+    from bse_gb300.capi import Marshalled
+    m = Marshalled(synth.collinear_problem(grid=3))
+    vals = [C.c_int64() for _ in range(4)]
+    assert lib.bse_sizes(C.byref(m.model), C.byref(m.params), *[C.byref(v) for v in vals]) == 0
+    N = 9
+    assert [v.value for v in vals] == [N, 4 * N, 2 * N, 4 * N]
