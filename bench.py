@@ -1,0 +1,316 @@
+"""Benchmark: q->0 Tamm-Dancoff BSE build + diagonalization + eps2 on one GB300.
+
+Workload (one "step" = one BSE solve): the magnetic spinful 4-orbital honeycomb model
+(2 sites x 2 spins, exchange splitting 0.5 eV, SOC 0.05 eV, random NNN hoppings
+sigma = 0.1 eV, seed 1234) on a 24x24 grid, 2 valence x 2 conduction bands, N_BSE = 2304,
+Rytova-Keldysh W + bare 2-D exchange, eps2 on 2000 points over 0-8 eV with 0.05 eV
+broadening.  Mixed precision: complex64 kernel build and FP32 eigensolve, FP64
+Rayleigh-Ritz refinement of the lowest 256 excitons.  Inputs are synthetic (seeded).
+
+value  = device time per solve (CUDA events on the library's stream), inputs resident
+e2e    = the same solve through the C ABI with host buffers: context creation (model
+         upload), solve, copy-back of eigenvalues and eps, destroy -- wall clock
+Other keys: the plain FP64 GPU path (cuSOLVER zheevd) on the same problem, the max
+eigenvalue error of the mixed path against it, the roofline of the build kernel, the
+CPU oracle baseline and the SM clocks sampled during the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as entry  # noqa: E402
+
+OMEGA = np.arange(2000) * 8.0 / 2000
+GAMMA = 0.05
+WORKLOAD = "magnetic4_24x24_2v2c"
+METRIC = "BSE build+diag wall time and eps2 grad time at N_BSE; error vs FP64"
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        self.dev = device_index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [ln.split(",") for ln in open(self.f.name).read().strip().splitlines() if ln.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _l2_flush_buffer():
+    import torch
+    return torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
+
+
+def _flush(buf):
+    buf.zero_()
+    import torch
+    torch.cuda.synchronize()
+
+
+def _problem(pkg_synth, grid=24, **kw):
+    return pkg_synth.magnetic4_problem(grid=grid, **kw)
+
+
+def _model_bytes(m):
+    return int(sum(a.nbytes for a in (m.r_cart, m.weights, m.h_r, m.centres, m.lattice, m.k_cart, m.g_cart)))
+
+
+def cpu_oracle_solve_ms(orc, prob, reps=1):
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        orc.solve(prob, OMEGA, GAMMA)
+        ts.append((time.perf_counter() - t0) * 1e3)
+    return min(ts)
+
+
+def run_reference(args):
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return 0
+    entry.load_package()
+    from importlib import import_module
+    synth = import_module("bse_gb300.synth")
+    orc = entry.load_oracle()
+    prob = _problem(synth)
+    cores = int(orc.lib().oracle_num_threads())
+    for _ in range(args.warmup):
+        orc.solve(prob, OMEGA, GAMMA)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.solve(prob, OMEGA, GAMMA)
+        ts.append((time.perf_counter() - t0) * 1e3)
+    total = sum(ts)
+    ms = total / args.steps
+    line = {
+        "impl": "reference", "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_bse": prob.n_bse, "n_g": prob.ng, "precision": "fp64",
+                   "l2": "inputs resident in host memory; CPU run"},
+        "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port",
+                         "sample": f"full solve of the {WORKLOAD} workload (N_BSE={prob.n_bse}) per step: "
+                                   "C++ OpenMP restatement of the reference loops + LAPACK zheevd (scipy)"},
+        "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    ws, rank, local = _dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BSE_BENCH_GLOO") is None else "gloo")
+    import torch
+    torch.cuda.set_device(local)
+    entry.load_package()
+    from importlib import import_module
+    synth = import_module("bse_gb300.synth")
+    gpu = import_module("bse_gb300.gpu")
+    gpu.load().bse_set_device(local)
+    solver = {"own": 0, "cusolver": 1}[args.solver]
+    prob = _problem(synth)
+    mixed = dict(precision=1, n_refine=256, eig_solver=solver)
+    flush = _l2_flush_buffer()
+
+    # --- device-resident timing (value) ---
+    ctx = gpu.BSEContext(prob, **mixed)
+    for _ in range(args.warmup):
+        ctx.solve(OMEGA, GAMMA)
+    ctx.reset_kernel_launches()
+    step_ms, build_ms, eig_ms = [], [], []
+    _barrier(ws)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_host0 = time.perf_counter()
+    for _ in range(args.steps):
+        _flush(flush)                                 # outside the solve's events
+        E_mixed, e2_mixed, _ = ctx.solve(OMEGA, GAMMA)
+        st = ctx.stage_times()
+        step_ms.append(st["solve"])
+        build_ms.append(st["build"])
+        eig_ms.append(st["eig"])
+    torch.cuda.synchronize()
+    host_s = time.perf_counter() - t_host0
+    clk = clocks.stop()
+    launches = ctx.kernel_launches()
+    stage = ctx.stage_times()
+    ctx.close()
+    _barrier(ws)
+    dev_total = _max_over_ranks(ws, sum(step_ms))
+    ms_per_step = dev_total / args.steps
+    value = ms_per_step / ws          # whole-job time per solve (each rank solves one problem per step)
+
+    # --- end to end through the C ABI with host buffers (e2e) ---
+    e2e_ms = []
+    for _ in range(max(1, args.steps)):
+        _flush(flush)
+        t0 = time.perf_counter()
+        with gpu.BSEContext(prob, **mixed) as c2:
+            c2.solve(OMEGA, GAMMA)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_value = _max_over_ranks(ws, sum(e2e_ms)) / len(e2e_ms) / ws
+    from bse_gb300.capi import Marshalled
+    mm = Marshalled(prob)
+    h2d = _model_bytes(mm) + OMEGA.nbytes
+    d2h = mm.n_exc * 8 + 2 * OMEGA.nbytes
+
+    # --- plain FP64 GPU path (cuSOLVER zheevd) and the error of the mixed path ---
+    with gpu.BSEContext(prob, precision=0, eig_solver=1) as c64:
+        c64.solve(OMEGA, GAMMA)
+        t64 = []
+        for _ in range(max(1, min(3, args.steps))):
+            _flush(flush)
+            E64, e2_64, _ = c64.solve(OMEGA, GAMMA)
+            t64.append(c64.stage_times()["solve"])
+    fp64_ms = float(np.median(t64))
+    nref = 256
+    err_ref = float(np.abs(E_mixed[:nref] - E64[:nref]).max())
+    err_all = float(np.abs(E_mixed - E64).max())
+    eps2_err = float(np.linalg.norm(e2_mixed - e2_64) / np.linalg.norm(e2_64))
+
+    # --- roofline of the build kernel (lower triangle, complex64 store) ---
+    N = prob.n_bse
+    nb = prob.model.nw * prob.model.n_spin
+    alg_bytes = N * (N + 1) // 2 * 8 + 16 * prob.nk * nb * (prob.params.nv + prob.params.nc)
+    build_avg_ms = float(np.mean(build_ms))
+    achieved = alg_bytes / (build_avg_ms * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    # --- CPU baseline (oracle, rank 0) ---
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        orc = entry.load_oracle()
+        cpu_ms = cpu_oracle_solve_ms(orc, prob)
+        cpu = {"value": cpu_ms, "unit": "ms", "cores": int(orc.lib().oracle_num_threads()), "kind": "port",
+               "sample": f"one full CPU solve of {WORKLOAD} (N_BSE={N}): C++ OpenMP restatement of the "
+                         "reference loops + LAPACK zheevd (scipy)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64+fp64-refine", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_bse": N, "n_k": prob.nk, "n_g": prob.ng, "nw": prob.model.nw,
+                       "nv": prob.params.nv, "nc": prob.params.nc, "n_omega": len(OMEGA), "gamma": GAMMA,
+                       "precision": "mixed", "n_refine": nref, "eig_solver": args.solver,
+                       "parallelism": f"replicas x{ws}",
+                       "l2": "flushed between steps (256 MB write); H is 42 MB"},
+            "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": {"kernel": "build_kernel<8,float>", "bound": "hbm", "achieved": achieved, "peak": peak,
+                         "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "alg_bytes_per_launch": int(alg_bytes), "avg_launch_ms": build_avg_ms},
+            "stages_ms": stage,
+            "fp64_gpu_ms": fp64_ms,
+            "speedup_vs_fp64_gpu": fp64_ms / ms_per_step,
+            "max_eig_err_ev": {"refined_lowest_256": err_ref, "all": err_all},
+            "eps2_rel_l2_vs_fp64": eps2_err,
+            "host_wall_s": host_s,
+            "clocks": clk,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--solver", default="cusolver", choices=["own", "cusolver"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

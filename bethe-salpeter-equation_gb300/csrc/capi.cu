@@ -455,11 +455,13 @@ int bse_solve(bse_ctx* c, const double* omega, int32_t n_omega, double gamma, do
     if (!c) return BSE_ERR_BAD_INPUT;
     cudaSetDevice(c->device);
     int st;
+    stage_begin(c, 7);
     if ((st = run_bands(c))) return st;
     if ((st = run_build(c, false, nullptr, nullptr))) return st;
     if ((st = run_eig(c))) return st;
     if ((st = run_oscillators(c))) return st;
     if ((st = run_eps(c, omega, n_omega, gamma, eps2, eps1))) return st;
+    stage_end(c, 7);
     if (e_out && (st = cuda_check(c, cudaMemcpyAsync(e_out, c->d_E, c->n_exc * 8, cudaMemcpyDeviceToHost, c->stream), "E copy"))) return st;
     return cuda_check(c, cudaStreamSynchronize(c->stream), "solve");
 }

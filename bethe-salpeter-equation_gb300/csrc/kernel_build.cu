@@ -510,7 +510,9 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     const bool coll = c->S == 1;
     const bool lower = !full && !coll && h_out == nullptr;
     const int64_t ld = c->n_h;
-    if ((st = cuda_check(c, cudaMemsetAsync(c->d_H, 0, (size_t)ld * ld * c->h_elem, c->stream), "H clear"))) return st;
+    // every element the solver reads is written by the build (lower triangle, or all of it);
+    // only the collinear layout has blocks the build never touches
+    if (coll && (st = cuda_check(c, cudaMemsetAsync(c->d_H, 0, (size_t)ld * ld * c->h_elem, c->stream), "H clear"))) return st;
     const int dd = c->p.ipa ? 0 : 1, de = c->p.ipa ? 0 : 1;
     const void* phi = mixed ? (const void*)c->d_phi32 : (const void*)c->d_phi;
     const void* qx = mixed ? (const void*)c->d_qx32 : (const void*)c->d_qx;

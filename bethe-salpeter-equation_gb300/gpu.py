@@ -75,7 +75,7 @@ def load(build_if_missing: bool = True):
     return L
 
 
-STAGES = ("bands", "tables", "build", "eig", "refine", "oscillators", "eps")
+STAGES = ("bands", "tables", "build", "eig", "refine", "oscillators", "eps", "solve")
 
 
 class BSEContext:

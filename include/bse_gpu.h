@@ -160,7 +160,8 @@ int bse_solve(bse_ctx* ctx, const double* omega, int32_t n_omega, double gamma,
               double* e_out, double* eps2, double* eps1);
 
 /* Device time (ms, CUDA events on the context stream) of the stages of the last calls:
- * [0] bands, [1] tables, [2] build, [3] eigensolve, [4] refinement, [5] oscillators, [6] eps. */
+ * [0] bands, [1] tables, [2] build, [3] eigensolve, [4] refinement, [5] oscillators, [6] eps,
+ * [7] the whole of the last bse_solve. */
 int bse_stage_times(const bse_ctx* ctx, double* ms, int32_t n);
 
 /* Launch/kernel statistics of the context: number of this library's kernel launches since

@@ -4,7 +4,8 @@ Tolerances (eV for energies, relative for matrices / spectra):
   FP64 path:   band energies 1e-11, gauge-fixed band vectors 1e-9, H elements 1e-11 * max|H|,
                BSE eigenvalues 1e-8 eV (the 1e-6 eV FP64 target with margin), eps2 rel L2 1e-8
   MIXED path:  H elements 2e-6 * max|H| (complex64 storage), refined eigenvalues 1e-6 eV,
-               all eigenvalues 1e-5 eV, eps2 rel L2 1e-4
+               unrefined eigenvalues 1e-6 * ||H||_2 (the backward error class of an FP32
+               eigensolver; ||H||_2 = max |E|), eps2 rel L2 1e-4
 """
 import numpy as np
 import pytest
@@ -88,7 +89,7 @@ def test_solve_mixed(problems, oracle, gpu, name, n_refine):
     n_opt = len(ref["E_opt"])
     E_opt = E[-n_opt:]
     assert np.abs(E_opt[:n_refine] - ref["E_opt"][:n_refine]).max() < 1e-6
-    assert np.abs(E - ref["E"]).max() < 1e-5
+    assert np.abs(E - ref["E"]).max() < max(1e-5, 1e-6 * np.abs(ref["E"]).max())
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-4 * np.linalg.norm(ref["eps2"])
 
 
