@@ -94,6 +94,14 @@ int run_oscillators(bse_ctx* c) {
     return BSE_OK;
 }
 
+// Launch of eps_kernel on caller-provided device buffers (used by the allocation-free entry point).
+cudaError_t launch_eps_raw(int64_t n, const double* E, const double2* f, const double* omega, int n_omega,
+                           double gamma, double F, double* eps2, double* eps1, cudaStream_t stream) {
+    eps_kernel<<<(unsigned)(((int64_t)n_omega * 32 + 255) / 256), 256, 0, stream>>>(n, E, f, omega, n_omega, gamma, F,
+                                                                                eps2, eps1);
+    return cudaGetLastError();
+}
+
 double eps_prefactor(const bse_ctx* c) {
     if (c->p.small_momentum) return kConv / (c->geo.vol * c->nk);
     return kConv / (kMinval * kMinval * c->geo.vol * c->nk);

@@ -24,7 +24,7 @@ EXPORTS = [
     "bse_status_string", "bse_last_error", "bse_version", "bse_sizes", "bse_set_device",
     "bse_create", "bse_destroy", "bse_compute_bands", "bse_get_bands", "bse_set_bands",
     "bse_build_kernel", "bse_diagonalize", "bse_oscillators", "bse_eps", "bse_solve",
-    "bse_stage_times", "bse_kernel_launches", "bse_reset_kernel_launches",
+    "bse_stage_times", "bse_kernel_launches", "bse_reset_kernel_launches", "bse_eps_noalloc",
 ]
 
 
@@ -71,6 +71,7 @@ def load(build_if_missing: bool = True):
     L.bse_kernel_launches.restype = C.c_int64
     L.bse_reset_kernel_launches.argtypes = [C.c_void_p]
     L.bse_reset_kernel_launches.restype = None
+    L.bse_eps_noalloc.argtypes = [C.c_int64, _dp, _dp, C.c_double, _dp, C.c_int32, C.c_double, _dp, _dp, C.c_void_p]
     _LIB = L
     return L
 

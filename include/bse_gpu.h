@@ -164,6 +164,22 @@ int bse_solve(bse_ctx* ctx, const double* omega, int32_t n_omega, double gamma,
  * [7] the whole of the last bse_solve. */
 int bse_stage_times(const bse_ctx* ctx, double* ms, int32_t n);
 
+/* Allocation-free dielectric function (no counterpart in the reference).  For callers that
+ * cannot call cudaMalloc -- a framework that has reserved the device memory for its own pool,
+ * or a pipeline that must not synchronise the device (cudaMalloc/cudaFree can) -- this computes
+ * eps(w) = 1 - prefactor * sum_l |f_l|^2 / (w - e_l + i gamma) from HOST arrays e[n_exc],
+ * f[n_exc] (complex128) and omega[n_omega] into eps2/eps1 (host, either nullable), staging them
+ * in one fixed 3.4 MiB file-scope device array that every GPU loading the library keeps until
+ * exit.  Limits below; larger sizes return BSE_ERR_BAD_INPUT.  The first call on a device
+ * resolves the array's address: make it before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race.  stream: a cudaStream_t, or NULL for the default stream.
+ * prefactor is F = conv / (V nk) of bse_eps. */
+#define BSE_EPS_NOALLOC_MAX_EXCITONS 131072
+#define BSE_EPS_NOALLOC_MAX_OMEGA 16384
+int bse_eps_noalloc(int64_t n_exc, const double* e, const double* f, double prefactor,
+                    const double* omega, int32_t n_omega, double gamma,
+                    double* eps2, double* eps1, void* stream);
+
 /* Launch/kernel statistics of the context: number of this library's kernel launches since
  * creation or the last reset. */
 int64_t bse_kernel_launches(const bse_ctx* ctx);
