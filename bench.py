@@ -304,7 +304,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--solver", default="cusolver", choices=["own", "cusolver"])
+    ap.add_argument("--solver", default="own", choices=["own", "cusolver"])
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

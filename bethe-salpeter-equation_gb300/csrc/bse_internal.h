@@ -100,6 +100,9 @@ struct bse_ctx {
     bool eig_valid = false;
     double2* d_f = nullptr;      // n_opt oscillator strengths
     bool osc_valid = false;
+    int64_t n_vec_valid = 0;     // leading eigenvector columns of d_A that are formed
+    bool f_from_eig = false;     // the own solver produced f for every exciton
+    int64_t n_refined = 0;       // leading columns replaced by the FP64 refinement
     // workspaces
     void* d_work = nullptr;
     size_t work_bytes = 0;
@@ -118,12 +121,15 @@ void stage_end(bse_ctx* c, int s);
 int run_bands(bse_ctx* c);
 int run_tables(bse_ctx* c);
 int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out);
-int run_eig(bse_ctx* c);
+int run_eig(bse_ctx* c, bool want_vectors);
 int run_refine(bse_ctx* c);
 int run_oscillators(bse_ctx* c);
 int run_eps(bse_ctx* c, const double* omega, int n_omega, double gamma, double* eps2, double* eps1);
 
 // own dense eigensolver (eigensolve.cu)
-int own_heevd(bse_ctx* c, int n, void* dA, int lda, bool fp64, double* dW, bool vectors);
+// Eigenvalues of the Hermitian n x n matrix dA (full storage) into dW; the first n_vec
+// eigenvectors overwrite dA's first columns; with rho0 given, f_out[l] = rho0^H x_l for all l.
+int own_heevd(bse_ctx* c, int n, void* dA, int lda, bool fp64, double* dW, int n_vec, const double2* rho0,
+              double2* f_out);
 
 }  // namespace bse

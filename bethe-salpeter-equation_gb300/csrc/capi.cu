@@ -418,8 +418,10 @@ int bse_diagonalize(bse_ctx* c, double* e_out, double* a_out) {
     cudaSetDevice(c->device);
     int st;
     if (!c->eig_valid || c->h_valid) {
-        if ((st = run_eig(c))) return st;
+        if ((st = run_eig(c, a_out != nullptr))) return st;
     }
+    if (a_out && c->n_vec_valid < c->n_opt)
+        return fail(c, BSE_ERR_STATE, "eigenvectors were not formed: rebuild, then call bse_diagonalize with a_out");
     if (e_out && (st = cuda_check(c, cudaMemcpyAsync(e_out, c->d_E, c->n_exc * 8, cudaMemcpyDeviceToHost, c->stream), "E copy"))) return st;
     if (a_out) {
         const size_t n = (size_t)c->n_opt * c->n_opt;
@@ -458,7 +460,7 @@ int bse_solve(bse_ctx* c, const double* omega, int32_t n_omega, double gamma, do
     stage_begin(c, 7);
     if ((st = run_bands(c))) return st;
     if ((st = run_build(c, false, nullptr, nullptr))) return st;
-    if ((st = run_eig(c))) return st;
+    if ((st = run_eig(c, false))) return st;
     if ((st = run_oscillators(c))) return st;
     if ((st = run_eps(c, omega, n_omega, gamma, eps2, eps1))) return st;
     stage_end(c, 7);

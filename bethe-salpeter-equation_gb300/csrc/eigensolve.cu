@@ -77,33 +77,53 @@ int library_heevd(bse_ctx* c, int64_t n, void* A, int64_t lda, bool fp64, double
     return BSE_OK;
 }
 
-int solve_one(bse_ctx* c, int64_t n, void* A, int64_t lda, bool fp64, double* dW, bool vectors) {
-    if (c->p.eig_solver == BSE_EIG_OWN) return own_heevd(c, (int)n, A, (int)lda, fp64, dW, vectors);
-    return library_heevd(c, n, A, lda, fp64, dW, vectors);
+// n_vec: eigenvectors the caller needs (leading columns); rho0/f: optical vector and oscillators.
+int solve_one(bse_ctx* c, int64_t n, void* A, int64_t lda, bool fp64, double* dW, int64_t n_vec,
+              const double2* rho0, double2* f) {
+    if (c->p.eig_solver == BSE_EIG_OWN) {
+        int st = own_heevd(c, (int)n, A, (int)lda, fp64, dW, (int)n_vec, rho0, f);
+        if (!st && rho0) {
+            c->n_vec_valid = n_vec;
+            c->f_from_eig = f != nullptr;
+        }
+        return st;
+    }
+    // the library path forms oscillators from eigenvectors: the optical block always needs them
+    int st = library_heevd(c, n, A, lda, fp64, dW, n_vec > 0 || rho0 != nullptr);
+    if (!st && rho0) {
+        c->n_vec_valid = n;
+        c->f_from_eig = false;
+    }
+    return st;
 }
 
 }  // namespace
 
-int run_eig(bse_ctx* c) {
+int run_eig(bse_ctx* c, bool want_vectors) {
     int st;
     if (!c->h_valid) return fail(c, BSE_ERR_STATE, "BSE matrix not built (diagonalize consumes it; rebuild first)");
     stage_begin(c, 3);
     const bool fp64 = c->p.precision == BSE_FP64;
+    const bool refine = !fp64 && !c->p.ipa && c->p.n_refine > 0;
+    const int64_t n_opt = c->n_opt;
+    const int64_t n_vec = want_vectors ? n_opt : (refine ? std::min<int64_t>(n_opt, (int64_t)c->p.n_refine + kGuard) : 0);
+    const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
+    c->n_refined = 0;
     if (c->S == 0) {
-        st = solve_one(c, c->N, c->d_H, c->N, fp64, c->d_E, true);
+        st = solve_one(c, c->N, c->d_H, c->N, fp64, c->d_E, n_vec, rho0, c->d_f);
         if (st) return st;
         c->d_A = c->d_H;
     } else {
         const int64_t n2 = 2 * c->N;
         char* b0 = (char*)c->d_blk;
         char* b1 = b0 + (size_t)n2 * n2 * c->h_elem;
-        if ((st = solve_one(c, n2, b0, n2, fp64, c->d_E, false))) return st;          // H0: values only (3317)
-        if ((st = solve_one(c, n2, b1, n2, fp64, c->d_E + n2, true))) return st;      // H1: optically active
+        if ((st = solve_one(c, n2, b0, n2, fp64, c->d_E, 0, nullptr, nullptr))) return st;      // H0: values only (3317)
+        if ((st = solve_one(c, n2, b1, n2, fp64, c->d_E + n2, n_vec, rho0, c->d_f))) return st;  // H1: optically active
         c->d_A = b1;
     }
     stage_end(c, 3);
     c->h_valid = false;
-    if (!fp64 && !c->p.ipa && c->p.n_refine > 0) {
+    if (refine) {
         if ((st = run_refine(c))) return st;
     }
     c->eig_valid = true;
@@ -188,6 +208,7 @@ int run_refine(bse_ctx* c) {
     if ((st = cuda_check(c, cudaMemcpyAsync(E, theta, nref * sizeof(double), cudaMemcpyDeviceToDevice, c->stream), "theta"))) return st;
     narrow_kernel<<<(unsigned)((n * nref + 255) / 256), 256, 0, c->stream>>>(n * nref, Y, (float2*)c->d_A);
     c->launches++;
+    c->n_refined = nref;
     stage_end(c, 4);
     return cuda_check(c, cudaGetLastError(), "refine");
 }

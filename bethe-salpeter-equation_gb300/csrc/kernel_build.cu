@@ -508,7 +508,8 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     stage_begin(c, 2);
     const bool mixed = c->p.precision == BSE_MIXED;
     const bool coll = c->S == 1;
-    const bool lower = !full && !coll && h_out == nullptr;
+    // the own eigensolver reads full Hermitian storage; cuSOLVER reads the lower triangle
+    const bool lower = !full && !coll && h_out == nullptr && c->p.eig_solver != BSE_EIG_OWN;
     const int64_t ld = c->n_h;
     // every element the solver reads is written by the build (lower triangle, or all of it);
     // only the collinear layout has blocks the build never touches

@@ -82,12 +82,16 @@ int run_oscillators(bse_ctx* c) {
     stage_begin(c, 5);
     const int64_t n = c->n_opt;
     const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
-    const unsigned blocks = (unsigned)((n * 32 + 255) / 256);
-    if (c->p.precision == BSE_MIXED)
-        oscillator_kernel<float2, float><<<blocks, 256, 0, c->stream>>>(n, n, n, rho0, (const float2*)c->d_A, c->d_f);
-    else
-        oscillator_kernel<double2, double><<<blocks, 256, 0, c->stream>>>(n, n, n, rho0, (const double2*)c->d_A, c->d_f);
-    c->launches++;
+    // the own solver already produced f = y^H z for every exciton; only refined vectors need a new dot
+    const int64_t ncols = c->f_from_eig ? c->n_refined : n;
+    if (ncols > 0) {
+        const unsigned blocks = (unsigned)((ncols * 32 + 255) / 256);
+        if (c->p.precision == BSE_MIXED)
+            oscillator_kernel<float2, float><<<blocks, 256, 0, c->stream>>>(n, n, ncols, rho0, (const float2*)c->d_A, c->d_f);
+        else
+            oscillator_kernel<double2, double><<<blocks, 256, 0, c->stream>>>(n, n, ncols, rho0, (const double2*)c->d_A, c->d_f);
+        c->launches++;
+    }
     stage_end(c, 5);
     if ((st = cuda_check(c, cudaGetLastError(), "oscillator kernel"))) return st;
     c->osc_valid = true;

@@ -107,7 +107,7 @@ class BSEParams:
     rk_eps: float = 1.0
     spin_factor: float = -1.0
     precision: int = BSE_FP64
-    eig_solver: int = BSE_EIG_CUSOLVER
+    eig_solver: int = BSE_EIG_OWN
     n_refine: int = 256
 
     def replace(self, **kw) -> "BSEParams":

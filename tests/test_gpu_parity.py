@@ -66,11 +66,15 @@ def test_build_matches_oracle_mixed(problems, oracle, gpu, name):
     assert np.abs(H - H_ref).max() < 2e-6 * np.abs(H_ref).max()
 
 
+SOLVERS = {"own": 0, "cusolver": 1}
+
+
+@pytest.mark.parametrize("solver", ["own", "cusolver"])
 @pytest.mark.parametrize("name", ["hbn12", "mag8", "coll6", "cubic4", "orb8_4"])
-def test_solve_fp64(problems, oracle, gpu, name):
+def test_solve_fp64(problems, oracle, gpu, name, solver):
     prob = problems[name]
     ref = oracle.solve(prob, OMEGA, GAMMA)
-    with gpu.BSEContext(prob) as ctx:
+    with gpu.BSEContext(prob, eig_solver=SOLVERS[solver]) as ctx:
         E, e2, e1 = ctx.solve(OMEGA, GAMMA)
         f = ctx.oscillators()
     assert np.abs(E - ref["E"]).max() < 1e-8
@@ -80,11 +84,12 @@ def test_solve_fp64(problems, oracle, gpu, name):
     assert abs(np.sum(np.abs(f) ** 2) - np.sum(np.abs(ref["f"]) ** 2)) < 1e-9 * np.sum(np.abs(ref["f"]) ** 2)
 
 
+@pytest.mark.parametrize("solver", ["own", "cusolver"])
 @pytest.mark.parametrize("name,n_refine", [("hbn12", 64), ("mag8", 64), ("coll6", 32)])
-def test_solve_mixed(problems, oracle, gpu, name, n_refine):
+def test_solve_mixed(problems, oracle, gpu, name, n_refine, solver):
     prob = problems[name]
     ref = oracle.solve(prob, OMEGA, GAMMA)
-    with gpu.BSEContext(prob, precision=1, n_refine=n_refine) as ctx:
+    with gpu.BSEContext(prob, precision=1, n_refine=n_refine, eig_solver=SOLVERS[solver]) as ctx:
         E, e2, _ = ctx.solve(OMEGA, GAMMA)
     n_opt = len(ref["E_opt"])
     E_opt = E[-n_opt:]
@@ -93,11 +98,12 @@ def test_solve_mixed(problems, oracle, gpu, name, n_refine):
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-4 * np.linalg.norm(ref["eps2"])
 
 
-def test_ipa_limit_exact(synth, gpu):
+@pytest.mark.parametrize("solver", ["own", "cusolver"])
+def test_ipa_limit_exact(synth, gpu, solver):
     """ipa = 1: H = diag(E_c(k) - E_v(k-q)) and the eigenvalues are those transitions, sorted
     (common_diagonalization ipa branch, bse.version13.cpp:3346-3365)."""
     prob = synth.magnetic4_problem(grid=8)
-    with gpu.BSEContext(prob, ipa=1) as ctx:
+    with gpu.BSEContext(prob, ipa=1, eig_solver=SOLVERS[solver]) as ctx:
         ctx.compute_bands()
         ec, ev, _, _ = ctx.get_bands()
         E, _, _ = ctx.solve(OMEGA, GAMMA)
@@ -121,16 +127,19 @@ def test_random_k_list_pair_tables(synth, oracle, gpu):
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
 
 
-def test_stage_api_sequence(synth, oracle, gpu):
+@pytest.mark.parametrize("solver", ["own", "cusolver"])
+def test_stage_api_sequence(synth, oracle, gpu, solver):
     """build -> diagonalize -> oscillators -> eps through the separate entry points."""
     prob = synth.hbn_problem(grid=8)
     ref = oracle.solve(prob, OMEGA, GAMMA)
-    with gpu.BSEContext(prob) as ctx:
+    with gpu.BSEContext(prob, eig_solver=SOLVERS[solver]) as ctx:
         ctx.build_kernel()
         E, A = ctx.diagonalize(want_vectors=True)
         f = ctx.oscillators()
         e2, e1 = ctx.eps(OMEGA, GAMMA)
     assert np.abs(E - ref["E"]).max() < 1e-8
-    # eigenvectors: unit norm, orthogonal
-    assert np.abs(A.conj().T @ A - np.eye(A.shape[0])).max() < 1e-10
+    # eigenvectors: unit norm, orthogonal, and A^H H A = diag(E)
+    assert np.abs(A.conj().T @ A - np.eye(A.shape[0])).max() < 1e-9
+    H = ref["H"]
+    assert np.abs(A.conj().T @ H @ A - np.diag(E)).max() < 1e-8 * np.abs(E).max()
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
