@@ -18,7 +18,8 @@ constexpr double kMinval = 1.0e-5;                               // bse.version1
 constexpr double kPi = 3.1415926535897932384626433832;           // bse.version13.cpp:29
 constexpr double kConv = (1.602176634 * 1000) / (8.8541878176);  // bse.version13.cpp:32
 constexpr int kMaxNw = 16;        // orbitals per spin channel handled by the band kernel
-constexpr int kStages = 8;   // bands, tables, build, eig, refine, oscillators, eps, whole solve
+constexpr int kStages = 13;  // bands, tables, build, eig, refine, oscillators, eps, whole solve,
+                              // own solver: tridiagonal, eigenvalues, inverse iteration, back-transform, clusters
 
 // Geometry derived once from the lattice (Crystal_Lattice, bse.version13.cpp:85-124).
 struct Geometry {
@@ -103,6 +104,7 @@ struct bse_ctx {
     int64_t n_vec_valid = 0;     // leading eigenvector columns of d_A that are formed
     bool f_from_eig = false;     // the own solver produced f for every exciton
     int64_t n_refined = 0;       // leading columns replaced by the FP64 refinement
+    int last_clusters = 0;       // clusters the own eigensolver resolved in FP64 in its last call
     // workspaces
     void* d_work = nullptr;
     size_t work_bytes = 0;

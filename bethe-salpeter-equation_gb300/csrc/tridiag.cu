@@ -11,15 +11,21 @@
 //     reflector; two grid barriers per reflector finish p and the scalar of w.  The same
 //     pass applies Q^H to the optical pair-density vector (y = Q^H rho), so oscillator
 //     strengths never need the eigenvectors of A: f_l = y^H z_l with z_l real.
-//  2. bisect_kernel: eigenvalues of T by Sturm-count bisection, one thread per eigenvalue;
-//     an FP32 bracket first, then FP64 bisection to full precision.
-//  3. invit_kernel: eigenvectors z_l of T by inverse iteration (FP64 LU with partial
-//     pivoting, dlagtf/dlagts style), one thread per eigenvalue, giving f_l on the fly.
-//  4. apply_q_kernel: X = Q Z only for the eigenvectors that are asked for (the FP64
-//     refinement subspace, or all of them when the caller wants A).
+//  2. bisect32_kernel: eigenvalues of T by FP32 Sturm-count bisection, one thread per
+//     eigenvalue; cluster_bisect_kernel repeats it in FP64 only for eigenvalues that FP32
+//     cannot separate (FP64 division is slow on this part).
+//  3. invit_kernel: eigenvectors z_l of T by inverse iteration (LU with partial pivoting,
+//     dlagtf/dlagts style): three FP32 iterations, then one FP64 Rayleigh-quotient iteration
+//     that also gives the FP64 eigenvalue; one thread per eigenvalue, f_l on the fly.
+//  4. larft_kernel + apply_wy_kernel: X = Q Z, in compact-WY panels of 32 reflectors, only
+//     for the eigenvectors that are asked for (the FP64 refinement subspace, or all of them
+//     when the caller wants A).
 // Every wait on another block is bounded: a barrier that times out sets an error word and
 // the kernel returns; the host reports BSE_ERR_NOT_CONVERGED.
 #include <cooperative_groups.h>
+
+#include <cstdlib>
+#include <string>
 
 #include "bse_internal.h"
 
@@ -101,6 +107,21 @@ __device__ __forceinline__ R block_sum(R v, R* red) {
     return t;
 }
 
+// Block-wide sums of NV real values at once (one reduction round); every thread gets them.
+template <typename R, int NV>
+__device__ __forceinline__ void block_sums(R (&v)[NV], R* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; j++) v[j] = warp_sum(v[j]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NV; j++) red[j * 32 + wid] = v[j];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NV; j++) v[j] = warp_sum(lane < nw ? red[j * 32 + lane] : R(0));
+}
+
 template <typename T2>
 struct TriArgs {
     int n;
@@ -109,17 +130,21 @@ struct TriArgs {
     typename Real<T2>::t* d;   // n
     typename Real<T2>::t* e;   // n-1
     T2* tau;                   // n-1
-    T2* vbuf;                  // [2][n] reflectors (v[k+1] = 1)
-    T2* pbuf;                  // [2][n] p = tau A v
+    T2* vbuf;                  // reflectors: [2][n] shared, or [B][n] per block (redundant mode)
+    T2* pbuf;                  // p = tau A v: [2][n] shared, or [B][n] per block
     T2* ppart;                 // [nt][n] column partial sums of the fused pass
-    T2* dpart;                 // [2][gridDim] block partial dots
-    T2* y;                     // n: Q^H applied in place (may be null)
+    T2* dpart;                 // [2][gridDim] block partial dots (shared mode)
+    T2* y;                     // Q^H applied in place: [n] shared, or [B][n] per block (may be null)
     unsigned* bar;
     int* err;
     int TR;                    // rows per tile
+    int redundant;             // 1: one barrier per reflector, every block finishes p itself
 };
 
 // Householder tridiagonalization (lower), full Hermitian storage.  See the file comment.
+// Shared mode: v/p/y live once in global memory, two grid barriers per reflector.
+// Redundant mode: every block keeps its own v/p/y (identical arithmetic in every block) and
+// reduces the column partial sums of all columns itself, so one barrier per reflector suffices.
 template <typename T2>
 __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
     typedef typename Real<T2>::t R;
@@ -127,35 +152,38 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
     T2* sv = reinterpret_cast<T2*>(smraw);          // pending v (tile rows)
     T2* sw = sv + a.TR;                             // pending w (tile rows)
     T2* sv1 = sw + a.TR;                            // new reflector (tile rows)
-    R* red = reinterpret_cast<R*>(sv1 + a.TR);      // 64 R for reductions
+    R* red = reinterpret_cast<R*>(sv1 + a.TR);      // 4 x 32 R for reductions
     const int n = a.n, tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5;
     const int nwarp = nthr >> 5, B = gridDim.x, b = blockIdx.x;
+    const bool rd = a.redundant != 0;
     const int64_t lda = a.lda;
     T2* A = a.A;
     T2 alpha_prev = C2<T2>(0, 0);
     bool have_prev = false;
     const T2 zero = C2<T2>(0, 0);
+    T2* yb = a.y ? (rd ? a.y + (size_t)b * n : a.y) : nullptr;
 
     for (int k = 0; k <= n - 2; k++) {
-        const T2* vp = a.vbuf + (size_t)((k + 1) & 1) * n;   // v_{k-1}
-        const T2* pp = a.pbuf + (size_t)((k + 1) & 1) * n;   // p_{k-1}
-        T2* vk = a.vbuf + (size_t)(k & 1) * n;
-        T2* pk = a.pbuf + (size_t)(k & 1) * n;
+        const T2* vp = rd ? a.vbuf + (size_t)b * n : a.vbuf + (size_t)((k + 1) & 1) * n;   // v_{k-1}
+        const T2* pp = rd ? a.pbuf + (size_t)b * n : a.pbuf + (size_t)((k + 1) & 1) * n;   // p_{k-1}
+        T2* vk = rd ? a.vbuf + (size_t)b * n : a.vbuf + (size_t)(k & 1) * n;
+        T2* pk = rd ? a.pbuf + (size_t)b * n : a.pbuf + (size_t)(k & 1) * n;
         auto wprev = [&](int r) -> T2 { return cadd(pp[r], cmul(alpha_prev, vp[r])); };
         // pending update of an element of column k (row r): a - v_r conj(w_k) - w_r conj(v_k)
-        T2 vkk = have_prev ? vp[k] : zero, wkk = have_prev ? wprev(k) : zero;
+        const T2 vkk = have_prev ? vp[k] : zero, wkk = have_prev ? wprev(k) : zero;
         auto upd_colk = [&](int r) -> T2 {
             T2 x = A[r + (int64_t)k * lda];
             if (have_prev) x = csub(csub(x, cmulc(vp[r], wkk)), cmulc(wprev(r), vkk));
             return x;
         };
         // ---- phase A: reflector of column k (every block, redundantly) ----
-        R loc = 0;
+        R loc[1] = {0};
         for (int r = k + 2 + tid; r < n; r += nthr) {
             T2 x = upd_colk(r);
-            loc += x.x * x.x + x.y * x.y;
+            loc[0] += x.x * x.x + x.y * x.y;
         }
-        const R xnorm2 = block_sum(loc, red);
+        block_sums<R, 1>(loc, red);
+        const R xnorm2 = loc[0];
         const T2 alpha = upd_colk(k + 1);
         const R dk = upd_colk(k).x;
         T2 tauk;
@@ -170,13 +198,10 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
             tauk = C2<T2>((beta - alpha.x) / beta, -alpha.y / beta);
             scal = cinv(csub(alpha, C2<T2>(beta, 0)));
         }
-        if (b == 0) {
-            for (int r = k + 1 + tid; r < n; r += nthr) vk[r] = (r == k + 1) ? C2<T2>(1, 0) : cmul(upd_colk(r), scal);
-            if (tid == 0) {
-                a.d[k] = dk;
-                a.e[k] = beta;
-                a.tau[k] = tauk;
-            }
+        if (b == 0 && tid == 0) {
+            a.d[k] = dk;
+            a.e[k] = beta;
+            a.tau[k] = tauk;
         }
         // ---- phase B: pending rank-2 update of A[k+1:, k+1:] and column sums of A_new^H v_k ----
         const int m = n - (k + 1);
@@ -199,7 +224,24 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
                 const T2 wc = have_prev ? wprev(c) : zero;
                 T2* col = A + (int64_t)c * lda;
                 R accx = 0, accy = 0;
-                for (int r = r0 + lane; r < r1; r += 32) {
+                int r = r0 + lane;
+                for (; r + 96 < r1; r += 128) {          // four independent loads in flight per lane
+                    T2 x[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) x[u] = col[r + 32 * u];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int i = r + 32 * u - r0;
+                        if (have_prev) {
+                            x[u] = csub(csub(x[u], cmulc(sv[i], wc)), cmulc(sw[i], vc));
+                            col[r + 32 * u] = x[u];
+                        }
+                        const T2 q = cconjmul(x[u], sv1[i]);
+                        accx += q.x;
+                        accy += q.y;
+                    }
+                }
+                for (; r < r1; r += 32) {
                     T2 x = col[r];
                     if (have_prev) {
                         x = csub(csub(x, cmulc(sv[r - r0], wc)), cmulc(sw[r - r0], vc));
@@ -215,58 +257,91 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
             }
         }
         if (!grid_barrier(a.bar, a.err)) return;
-        // ---- phase C1: p_c = tau * sum_t ppart, partial p^H v and v^H y per block ----
-        {
-            R dx = 0, dy = 0, yx = 0, yy = 0;
+        if (rd) {
+            // ---- every block: v_k, p_k = tau sum_t ppart, alpha_k and y <- H_k^H y over all columns ----
+            // Column k is still read below by every block, so block 0 stores reflector k-1 (held in
+            // its v buffer until the loop below overwrites it) into column k-1, which nobody reads now.
+            if (b == 0 && k >= 1) {
+                for (int r = k + 1 + tid; r < n; r += nthr) A[r + (int64_t)(k - 1) * lda] = vk[r];
+                __syncthreads();
+            }
+            R acc[4] = {0, 0, 0, 0};
+            for (int c = k + 1 + tid; c < n; c += nthr) {
+                T2 s = zero;
+                for (int t = 0; t < nt; t++) s = cadd(s, a.ppart[(size_t)t * n + c]);
+                const T2 p = cmul(tauk, s);
+                const T2 v = (c == k + 1) ? C2<T2>(1, 0) : cmul(upd_colk(c), scal);
+                pk[c] = p;
+                vk[c] = v;
+                const T2 q = cconjmul(p, v);
+                acc[0] += q.x;
+                acc[1] += q.y;
+                if (yb) {
+                    const T2 u = cconjmul(v, yb[c]);
+                    acc[2] += u.x;
+                    acc[3] += u.y;
+                }
+            }
+            block_sums<R, 4>(acc, red);
+            alpha_prev = cmul(C2<T2>(-0.5 * tauk.x, -0.5 * tauk.y), C2<T2>(acc[0], acc[1]));
+            if (yb) {
+                const T2 coef = cmulc(C2<T2>(acc[2], acc[3]), tauk);   // conj(tau) (v^H y)
+                for (int c = k + 1 + tid; c < n; c += nthr) yb[c] = csub(yb[c], cmul(coef, vk[c]));
+            }
+            __syncthreads();
+        } else {
+            if (b == 0)
+                for (int r = k + 1 + tid; r < n; r += nthr) vk[r] = (r == k + 1) ? C2<T2>(1, 0) : cmul(upd_colk(r), scal);
+            // ---- C1: p_c = tau * sum_t ppart on this block's column slice, partial dots ----
+            R acc[4] = {0, 0, 0, 0};
             for (int c = k + 1 + b * nthr + tid; c < n; c += B * nthr) {
                 T2 s = zero;
                 for (int t = 0; t < nt; t++) s = cadd(s, a.ppart[(size_t)t * n + c]);
                 const T2 p = cmul(tauk, s);
+                const T2 v = (c == k + 1) ? C2<T2>(1, 0) : cmul(upd_colk(c), scal);
                 pk[c] = p;
-                const T2 v = vk[c];
                 const T2 q = cconjmul(p, v);
-                dx += q.x;
-                dy += q.y;
-                if (a.y) {
-                    const T2 u = cconjmul(v, a.y[c]);
-                    yx += u.x;
-                    yy += u.y;
+                acc[0] += q.x;
+                acc[1] += q.y;
+                if (yb) {
+                    const T2 u = cconjmul(v, yb[c]);
+                    acc[2] += u.x;
+                    acc[3] += u.y;
                 }
             }
-            dx = block_sum(dx, red);
-            dy = block_sum(dy, red);
-            if (a.y) {
-                yx = block_sum(yx, red);
-                yy = block_sum(yy, red);
-            }
+            block_sums<R, 4>(acc, red);
             if (tid == 0) {
-                a.dpart[b] = C2<T2>(dx, dy);
-                a.dpart[B + b] = C2<T2>(yx, yy);
+                a.dpart[b] = C2<T2>(acc[0], acc[1]);
+                a.dpart[B + b] = C2<T2>(acc[2], acc[3]);
             }
-        }
-        if (!grid_barrier(a.bar, a.err)) return;
-        // ---- phase C2: alpha_k, y <- H_k^H y on this block's slice, reflector storage ----
-        {
-            T2 s = zero, sy = zero;
-            for (int i = 0; i < B; i++) {
-                s = cadd(s, a.dpart[i]);
-                sy = cadd(sy, a.dpart[B + i]);
+            if (!grid_barrier(a.bar, a.err)) return;
+            // ---- C2: alpha_k, y <- H_k^H y on this block's slice, reflector storage ----
+            R s4[4] = {0, 0, 0, 0};
+            for (int i = tid; i < B; i += nthr) {
+                const T2 u = a.dpart[i], q = a.dpart[B + i];
+                s4[0] += u.x;
+                s4[1] += u.y;
+                s4[2] += q.x;
+                s4[3] += q.y;
             }
-            alpha_prev = cmul(C2<T2>(-0.5 * tauk.x, -0.5 * tauk.y), s);
-            have_prev = true;
-            if (a.y) {
-                // y -= conj(tau) (v^H y) v  on the same column slice as C1 (next C1 reads it after a barrier)
-                const T2 coef = cmulc(sy, tauk);   // conj(tau) * (v^H y)
-                for (int c = k + 1 + b * nthr + tid; c < n; c += B * nthr) a.y[c] = csub(a.y[c], cmul(coef, vk[c]));
+            block_sums<R, 4>(s4, red);
+            alpha_prev = cmul(C2<T2>(-0.5 * tauk.x, -0.5 * tauk.y), C2<T2>(s4[0], s4[1]));
+            if (yb) {
+                // v_k from the buffer block 0 published before the first barrier (column k is being
+                // overwritten by block 0 below)
+                const T2 coef = cmulc(C2<T2>(s4[2], s4[3]), tauk);
+                for (int c = k + 1 + b * nthr + tid; c < n; c += B * nthr) yb[c] = csub(yb[c], cmul(coef, vk[c]));
             }
+            __syncthreads();
             if (b == 0)
                 for (int r = k + 2 + tid; r < n; r += nthr) A[r + (int64_t)k * lda] = vk[r];
         }
+        have_prev = true;
     }
     if (b == 0 && tid == 0) {
         if (n >= 2) {
-            const T2* vp = a.vbuf + (size_t)((n - 2) & 1) * n;
-            const T2* pp = a.pbuf + (size_t)((n - 2) & 1) * n;
+            const T2* vp = rd ? a.vbuf : a.vbuf + (size_t)((n - 2) & 1) * n;
+            const T2* pp = rd ? a.pbuf : a.pbuf + (size_t)((n - 2) & 1) * n;
             const T2 v = vp[n - 1], w = cadd(pp[n - 1], cmul(alpha_prev, vp[n - 1]));
             T2 x = A[(n - 1) + (int64_t)(n - 1) * lda];
             x = csub(csub(x, cmulc(v, w)), cmulc(w, v));
@@ -291,33 +366,22 @@ __device__ __forceinline__ int sturm(int n, const R* __restrict__ d, const R* __
     return c;
 }
 
-// i-th smallest eigenvalue of T: FP32 bisection to a bracket, verified and finished in FP64.
-__global__ void __launch_bounds__(128) bisect_kernel(int n, const double* __restrict__ d, const double* __restrict__ e2,
-                                                     const float* __restrict__ df, const float* __restrict__ e2f,
-                                                     double glo, double ghi, double pivmin, float pivminf,
-                                                     double* __restrict__ w) {
+// i-th smallest eigenvalue of T by FP32 bisection to FP32 resolution.  cl[i] = 1 marks an
+// eigenvalue whose FP32 estimate lies within `ctol` of a neighbour's (a cluster at FP32
+// resolution); those get FP64 bisection in cluster_bisect_kernel.  FP64 division is slow on
+// this part, so the FP64 work is spent only where FP32 cannot separate eigenvalues.
+__global__ void __launch_bounds__(32) bisect32_kernel(int n, const float* __restrict__ df, const float* __restrict__ e2f,
+                                                      float glo, float ghi, float pivminf, double* __restrict__ w) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double tnorm = fmax(fabs(glo), fabs(ghi));
-    float a = (float)glo, b = (float)ghi;
-    for (int it = 0; it < 22; it++) {
+    float a = glo, b = ghi;
+    for (int it = 0; it < 40; it++) {
         const float mid = 0.5f * (a + b);
+        if (!(mid > a && mid < b)) break;
         if (sturm<float>(n, df, e2f, mid, pivminf) > i) b = mid;
         else a = mid;
     }
-    const double margin = 64.0 * 1.1920929e-7 * (tnorm + fabs((double)a) + fabs((double)b));
-    double lo = (double)a - margin, hi = (double)b + margin;
-    if (!(sturm<double>(n, d, e2, lo, pivmin) <= i && sturm<double>(n, d, e2, hi, pivmin) > i)) {
-        lo = glo;
-        hi = ghi;
-    }
-    for (int it = 0; it < 100; it++) {
-        const double mid = 0.5 * (lo + hi);
-        if (hi - lo <= 4.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 2.0 * pivmin || mid <= lo || mid >= hi) break;
-        if (sturm<double>(n, d, e2, mid, pivmin) > i) hi = mid;
-        else lo = mid;
-    }
-    w[i] = 0.5 * (lo + hi);
+    w[i] = 0.5 * ((double)a + (double)b);
 }
 
 __device__ __forceinline__ double start_value(unsigned i, unsigned k) {
@@ -330,151 +394,456 @@ __device__ __forceinline__ double start_value(unsigned i, unsigned k) {
     return 0.5 + (double)(h & 0xFFFFFF) / (double)0x1000000;   // (0.5, 1.5)
 }
 
-// Eigenvector of T for eigenvalue w[i] by inverse iteration; f_i = sum_k conj(y_k) z_k.
-// Scratch is interleaved ([k][count]) so the threads of a warp touch consecutive words.
-template <typename TZ>
-__global__ void __launch_bounds__(128) invit_kernel(int n, const double* __restrict__ d, const double* __restrict__ e,
-                                                    const double* __restrict__ w, int i0, int count, double tnorm,
-                                                    const double2* __restrict__ y, double2* __restrict__ f,
-                                                    TZ* __restrict__ z, int64_t ldz, int n_store,
-                                                    double* __restrict__ scr, signed char* __restrict__ piv) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= count) return;
-    const int i = i0 + t;
-    const double lam = w[i];
-    const size_t S = (size_t)count;
-    double* Ua = scr;                  // pivots (diagonal of U)
-    double* Ub = scr + (size_t)n * S;  // first superdiagonal of U
-    double* Ud = scr + 2 * (size_t)n * S;   // second superdiagonal of U (fill-in)
-    double* Lc = scr + 3 * (size_t)n * S;   // multipliers
-    double* Y = scr + 4 * (size_t)n * S;    // iterate
-    const double pert = 2.220446049250313e-16 * fmax(tnorm, 1e-300);
-    // LU of T - lam I with partial pivoting (dlagtf)
-    double ak = d[0] - lam;
-    double bk = n > 1 ? e[0] : 0.0;      // super of the current pivot row
+// Sequential sweeps over per-thread vectors are latency-bound (one warp per SM on the GPU):
+// element k of a thread's vector lives at p[k * RS], and the loops prefetch the line PD rows
+// ahead into L1 so the dependent recurrences do not wait on L2.
+__device__ __forceinline__ void pf_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// LU with partial pivoting of the tridiagonal T - s I (dlagtf); pivots stored as reciprocals so
+// the solves need no division.
+template <typename F, int RS, int PD>
+__device__ __forceinline__ void tri_factor(int n, const F* __restrict__ d, const F* __restrict__ e, F s, F pert,
+                                           F* __restrict__ Ur, F* __restrict__ Ub, F* __restrict__ Ud,
+                                           F* __restrict__ Lc, signed char* __restrict__ piv) {
+    F ak = d[0] - s;
+    F bk = n > 1 ? e[0] : F(0);
     for (int k = 0; k < n - 1; k++) {
-        const double ck = e[k];            // sub-diagonal entry below the pivot
-        const double anext = d[k + 1] - lam;
-        const double bnext = (k + 1 < n - 1) ? e[k + 1] : 0.0;
+        if (k + PD < n) {
+            pf_l1(d + k + PD);
+            pf_l1(e + k + PD);
+        }
+        const F ck = e[k];
+        const F anext = d[k + 1] - s;
+        const F bnext = (k + 1 < n - 1) ? e[k + 1] : F(0);
         if (fabs(ck) <= fabs(ak)) {
-            const double mult = ak != 0.0 ? ck / ak : 0.0;
-            Ua[k * S + t] = ak;
-            Ub[k * S + t] = bk;
-            Ud[k * S + t] = 0.0;
-            Lc[k * S + t] = mult;
-            piv[k * S + t] = 0;
+            const F u = fabs(ak) < pert ? (ak < 0 ? -pert : pert) : ak;
+            const F r = F(1) / u;
+            const F mult = ck * r;
+            Ur[(size_t)k * RS] = r;
+            Ub[(size_t)k * RS] = bk;
+            Ud[(size_t)k * RS] = F(0);
+            Lc[(size_t)k * RS] = mult;
+            piv[(size_t)k * RS] = 0;
             ak = anext - mult * bk;
             bk = bnext;
         } else {
-            const double mult = ak / ck;
-            Ua[k * S + t] = ck;
-            Ub[k * S + t] = anext;
-            Ud[k * S + t] = bnext;
-            Lc[k * S + t] = mult;
-            piv[k * S + t] = 1;
+            const F r = F(1) / ck;
+            const F mult = ak * r;
+            Ur[(size_t)k * RS] = r;
+            Ub[(size_t)k * RS] = anext;
+            Ud[(size_t)k * RS] = bnext;
+            Lc[(size_t)k * RS] = mult;
+            piv[(size_t)k * RS] = 1;
             ak = bk - mult * anext;
             bk = -mult * bnext;
         }
     }
-    Ua[(size_t)(n - 1) * S + t] = ak;
-    for (int k = 0; k < n; k++) Y[k * S + t] = start_value(i, k);
-    for (int iter = 0; iter < 3; iter++) {
-        // forward: apply L (with interchanges)
-        for (int k = 0; k < n - 1; k++) {
-            const double mult = Lc[k * S + t];
-            const double y0 = Y[k * S + t], y1 = Y[(k + 1) * S + t];
-            if (piv[k * S + t] == 0) {
-                Y[(k + 1) * S + t] = y1 - mult * y0;
-            } else {
-                Y[k * S + t] = y1;
-                Y[(k + 1) * S + t] = y0 - mult * y1;
-            }
-        }
-        // back substitution with U (zero pivots perturbed)
-        double x1 = 0.0, x2 = 0.0, mx = 0.0;
-        for (int k = n - 1; k >= 0; k--) {
-            double u = Ua[k * S + t];
-            if (fabs(u) < pert) u = u < 0 ? -pert : pert;
-            const double x = (Y[k * S + t] - Ub[k * S + t] * x1 - Ud[k * S + t] * x2) / u;
-            Y[k * S + t] = x;
-            x2 = x1;
-            x1 = x;
-            mx = fmax(mx, fabs(x));
-        }
-        const double sc = mx > 0 ? 1.0 / mx : 1.0;
-        for (int k = 0; k < n; k++) Y[k * S + t] *= sc;
-    }
-    double nrm = 0.0, fx = 0.0, fy = 0.0;
-    for (int k = 0; k < n; k++) {
-        const double v = Y[k * S + t];
-        nrm += v * v;
-        if (y) {
-            const double2 yy = y[k];
-            fx += yy.x * v;
-            fy -= yy.y * v;
-        }
-    }
-    const double inv = 1.0 / sqrt(nrm);
-    if (f) f[i] = make_double2(fx * inv, fy * inv);
-    if (i < n_store)
-        for (int k = 0; k < n; k++) z[(size_t)k + (size_t)i * ldz] = (TZ)(Y[k * S + t] * inv);
+    const F u = fabs(ak) < pert ? (ak < 0 ? -pert : pert) : ak;
+    Ur[(size_t)(n - 1) * RS] = F(1) / u;
 }
 
-// X[:, c] <- Q X[:, c] (adjoint = false: H_{n-2} first ... H_0 last) or Q^H X (adjoint = true).
-// One block per group of CB columns; reflector k has v[k+1] = 1, v[r] = A[r, k] for r >= k+2.
-template <typename T2, int CB>
-__global__ void __launch_bounds__(256) apply_q_kernel(int n, const T2* __restrict__ A, int64_t lda,
-                                                      const T2* __restrict__ tau, T2* __restrict__ X, int64_t ldx,
-                                                      int ncols, bool adjoint) {
-    typedef typename Real<T2>::t R;
-    __shared__ R red[2 * CB][32];
-    __shared__ T2 coef[CB];
-    const int c0 = blockIdx.x * CB, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-    for (int s = 0; s < n - 1; s++) {
-        const int k = adjoint ? s : (n - 2 - s);
-        const T2 tk = tau[k];
-        if (tk.x == R(0) && tk.y == R(0)) continue;
-        R px[CB], py[CB];
-#pragma unroll
-        for (int j = 0; j < CB; j++) px[j] = py[j] = 0;
-        for (int r = k + 1 + tid; r < n; r += blockDim.x) {
-            const T2 v = (r == k + 1) ? C2<T2>(1, 0) : A[r + (int64_t)k * lda];
-#pragma unroll
-            for (int j = 0; j < CB; j++)
-                if (c0 + j < ncols) {
-                    const T2 q = cconjmul(v, X[r + (int64_t)(c0 + j) * ldx]);
-                    px[j] += q.x;
-                    py[j] += q.y;
+// One solve (T - s I) x = y in place on Y, the input scaled by `sin` on the fly; returns the
+// max-norm of the solution (the caller folds 1/max into the next sweep).
+template <typename F, int RS, int PD>
+__device__ __forceinline__ F tri_solve(int n, const F* __restrict__ Ur, const F* __restrict__ Ub,
+                                       const F* __restrict__ Ud, const F* __restrict__ Lc,
+                                       const signed char* __restrict__ piv, F* __restrict__ Y, F sin) {
+    F ycur = Y[0] * sin;
+    for (int k = 0; k < n - 1; k++) {
+        if (k + PD < n - 1) {
+            pf_l1(Lc + (size_t)(k + PD) * RS);
+            pf_l1(piv + (size_t)(k + PD) * RS);
+            pf_l1(Y + (size_t)(k + 1 + PD) * RS);
+        }
+        const F mult = Lc[(size_t)k * RS];
+        const F ynext = Y[(size_t)(k + 1) * RS] * sin;
+        F out;
+        if (piv[(size_t)k * RS] == 0) {
+            out = ycur;
+            ycur = ynext - mult * ycur;
+        } else {
+            out = ynext;
+            ycur = ycur - mult * ynext;
+        }
+        Y[(size_t)k * RS] = out;
+    }
+    F x1 = 0, x2 = 0, mx = 0;
+    {
+        const F x = ycur * Ur[(size_t)(n - 1) * RS];
+        Y[(size_t)(n - 1) * RS] = x;
+        x1 = x;
+        mx = fabs(x);
+    }
+    for (int k = n - 2; k >= 0; k--) {
+        if (k - PD >= 0) {
+            pf_l1(Ur + (size_t)(k - PD) * RS);
+            pf_l1(Ub + (size_t)(k - PD) * RS);
+            pf_l1(Ud + (size_t)(k - PD) * RS);
+            pf_l1(Y + (size_t)(k - PD) * RS);
+        }
+        const F x = (Y[(size_t)k * RS] - Ub[(size_t)k * RS] * x1 - Ud[(size_t)k * RS] * x2) * Ur[(size_t)k * RS];
+        Y[(size_t)k * RS] = x;
+        x2 = x1;
+        x1 = x;
+        mx = fmax(mx, fabs(x));
+    }
+    return mx;
+}
+
+// FP64 Rayleigh quotient z^T T z / z^T z of X (scaled by sx), with the squared norm.
+template <int RS, int PD>
+__device__ __forceinline__ double tri_rq(int n, const double* __restrict__ d, const double* __restrict__ e,
+                                         const double* __restrict__ X, double sx, double* den_out) {
+    double num = 0, den = 0, xprev = 0, x = X[0] * sx;
+    for (int k = 0; k < n; k++) {
+        if (k + PD < n) {
+            pf_l1(X + (size_t)(k + PD) * RS);
+            pf_l1(d + k + PD);
+        }
+        const double xn = (k + 1 < n) ? X[(size_t)(k + 1) * RS] * sx : 0.0;
+        num += x * (d[k] * x + (k > 0 ? e[k - 1] * xprev : 0.0) + (k + 1 < n ? e[k] * xn : 0.0));
+        den += x * x;
+        xprev = x;
+        x = xn;
+    }
+    *den_out = den;
+    return num / den;
+}
+
+// Eigenpair (w_i, z_i) of T for an eigenvalue FP32 bisection separates from its neighbours:
+// three FP32 inverse iterations from the FP32 estimate, then two FP64 Rayleigh-quotient
+// iterations.  Writes w[i], f_i = sum_k conj(y_k) z_k, and z_i for i < n_store.  Cluster
+// members (cl[i] != 0) are left to cluster_kernel.
+template <typename TZ>
+__global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restrict__ d, const double* __restrict__ e,
+                                                   const float* __restrict__ df, const float* __restrict__ ef,
+                                                   double* __restrict__ w, const signed char* __restrict__ cl,
+                                                   int i0, int count, double tnorm, const double2* __restrict__ y,
+                                                   double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz,
+                                                   int n_store, double* __restrict__ scr, float* __restrict__ scr32,
+                                                   signed char* __restrict__ piv) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int i = i0 + t;
+    if (cl[i]) return;
+    // this warp's scratch: [array][k][32 lanes], one 128-byte line per row in FP32
+    const size_t W32 = (size_t)n * 32;
+    const size_t lane = threadIdx.x & 31;
+    const double lam0 = w[i];
+    float* Ur = scr32 + (size_t)blockIdx.x * 5 * W32 + lane;
+    float* Ub = Ur + W32;
+    float* Ud = Ub + W32;
+    float* Lc = Ud + W32;
+    float* Y = Lc + W32;
+    signed char* pv = piv + (size_t)blockIdx.x * W32 + lane;
+    tri_factor<float, 32, 32>(n, df, ef, (float)lam0, 1.1920929e-7f * (float)fmax(tnorm, 1e-30), Ur, Ub, Ud, Lc, pv);
+    for (int k = 0; k < n; k++) Y[(size_t)k * 32] = (float)start_value(i, k);
+    float sc = 1.0f;
+    for (int it = 0; it < 3; it++) {
+        const float mx = tri_solve<float, 32, 32>(n, Ur, Ub, Ud, Lc, pv, Y, sc);
+        sc = mx > 0 ? 1.0f / mx : 1.0f;
+    }
+    double* Vr = scr + (size_t)blockIdx.x * 5 * W32 + lane;
+    double* Vb = Vr + W32;
+    double* Vd = Vb + W32;
+    double* Vc = Vd + W32;
+    double* X = Vc + W32;
+    for (int k = 0; k < n; k++) X[(size_t)k * 32] = (double)Y[(size_t)k * 32] * (double)sc;
+    const double pert = 2.220446049250313e-16 * fmax(tnorm, 1e-300);
+    double den = 1, sx = 1.0;
+    for (int it = 0; it < 2; it++) {
+        const double shift = tri_rq<32, 16>(n, d, e, X, sx, &den);
+        tri_factor<double, 32, 16>(n, d, e, shift, pert, Vr, Vb, Vd, Vc, pv);
+        const double mx = tri_solve<double, 32, 16>(n, Vr, Vb, Vd, Vc, pv, X, sx);
+        sx = mx > 0 ? 1.0 / mx : 1.0;
+    }
+    const double lam = tri_rq<32, 16>(n, d, e, X, sx, &den);
+    const double inv = sx / sqrt(den);
+    w[i] = lam;
+    double fx = 0, fy = 0;
+    const bool keep = i < n_store;
+    for (int k = 0; k < n; k++) {
+        if (k + 16 < n) pf_l1(X + (size_t)(k + 16) * 32);
+        const double x = X[(size_t)k * 32] * inv;
+        if (f) {
+            const double2 yy = y[k];
+            fx += yy.x * x;
+            fy -= yy.y * x;
+        }
+        if (keep) z[(size_t)k + (size_t)i * ldz] = (TZ)x;
+    }
+    if (f) f[i] = make_double2(fx, fy);
+}
+
+// Eigenpairs of a run of eigenvalues FP32 bisection cannot separate (dstein-style): one warp
+// per cluster.  Member j gets FP64 inverse iteration with its own shift (lane 0 runs the
+// tridiagonal factor and solves) and Gram-Schmidt against the cluster's earlier members (all
+// lanes); then a Rayleigh-Ritz step inside the cluster (Jacobi on the c x c projected matrix)
+// gives FP64 eigenpairs.  Member vectors stay in Zc (column-major n x c per cluster).
+__device__ __forceinline__ double warp_dsum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename TZ>
+__global__ void __launch_bounds__(32) cluster_kernel(int n, const double* __restrict__ d, const double* __restrict__ e,
+                                                     double* __restrict__ w, const int* __restrict__ cstart,
+                                                     const int* __restrict__ csize, const int64_t* __restrict__ coff,
+                                                     int ncl, double tnorm, const double2* __restrict__ y,
+                                                     double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz, int n_store,
+                                                     double* __restrict__ scr, signed char* __restrict__ piv,
+                                                     double* __restrict__ Zall) {
+    const int t = blockIdx.x, lane = threadIdx.x;
+    if (t >= ncl) return;
+    const int s0 = cstart[t], c = csize[t];
+    // this cluster's scratch: 5 contiguous arrays of n doubles (lane 0 only) and n pivots
+    double* Vr = scr + (size_t)t * 5 * n;
+    double* Vb = Vr + n;
+    double* Vd = Vb + n;
+    double* Vc = Vd + n;
+    double* X = Vc + n;
+    signed char* pv = piv + (size_t)t * n;
+    double* Zc = Zall + coff[t];                       // n x c
+    const double pert = 2.220446049250313e-16 * fmax(tnorm, 1e-300);
+    double sprev = -1e300;
+    for (int j = 0; j < c; j++) {
+        const double shift = fmax(w[s0 + j], sprev + 10.0 * pert);
+        sprev = shift;
+        if (lane == 0) tri_factor<double, 1, 64>(n, d, e, shift, pert, Vr, Vb, Vd, Vc, pv);
+        for (int k = lane; k < n; k += 32) X[k] = start_value(s0 + j, k) - 1.0;
+        __syncwarp();
+        for (int it = 0; it < 5; it++) {
+            if (lane == 0) tri_solve<double, 1, 64>(n, Vr, Vb, Vd, Vc, pv, X, 1.0);
+            __syncwarp();
+            for (int q = 0; q < j; q++) {               // Gram-Schmidt against earlier members
+                const double* zq = Zc + (size_t)q * n;
+                double dot = 0;
+                for (int k = lane; k < n; k += 32) dot += zq[k] * X[k];
+                dot = warp_dsum(dot);
+                for (int k = lane; k < n; k += 32) X[k] -= dot * zq[k];
+                __syncwarp();
+            }
+            double nrm = 0;
+            for (int k = lane; k < n; k += 32) nrm += X[k] * X[k];
+            nrm = warp_dsum(nrm);
+            const double inv = nrm > 0 ? 1.0 / sqrt(nrm) : 0.0;
+            for (int k = lane; k < n; k += 32) X[k] *= inv;
+            __syncwarp();
+        }
+        for (int k = lane; k < n; k += 32) Zc[k + (size_t)j * n] = X[k];
+        __syncwarp();
+    }
+    // Rayleigh-Ritz inside the cluster: M = Zc^T T Zc (lanes over k), Jacobi on lane 0
+    constexpr int CMAX = 32;
+    __shared__ double M[CMAX * CMAX], Q[CMAX * CMAX];
+    for (int a = 0; a < c; a++)
+        for (int b = 0; b <= a; b++) {
+            const double* za = Zc + (size_t)a * n;
+            const double* zb = Zc + (size_t)b * n;
+            double acc = 0;
+            for (int k = lane; k < n; k += 32) {
+                const double tz = d[k] * zb[k] + (k > 0 ? e[k - 1] * zb[k - 1] : 0.0) + (k + 1 < n ? e[k] * zb[k + 1] : 0.0);
+                acc += za[k] * tz;
+            }
+            acc = warp_dsum(acc);
+            if (lane == 0) M[a + b * CMAX] = M[b + a * CMAX] = acc;
+        }
+    __syncwarp();
+    if (lane == 0) {
+        for (int a = 0; a < c; a++)
+            for (int b = 0; b < c; b++) Q[a + b * CMAX] = a == b ? 1.0 : 0.0;
+        for (int sweep = 0; sweep < 30; sweep++) {
+            double off = 0;
+            for (int a = 0; a < c; a++)
+                for (int b = a + 1; b < c; b++) off += M[a + b * CMAX] * M[a + b * CMAX];
+            if (off < 1e-60) break;
+            for (int p = 0; p < c; p++)
+                for (int q = p + 1; q < c; q++) {
+                    const double apq = M[p + q * CMAX];
+                    if (apq == 0.0) continue;
+                    const double tau = (M[q + q * CMAX] - M[p + p * CMAX]) / (2.0 * apq);
+                    const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                    const double cs = 1.0 / sqrt(1.0 + tt * tt), sn = tt * cs;
+                    for (int k = 0; k < c; k++) {
+                        const double mkp = M[k + p * CMAX], mkq = M[k + q * CMAX];
+                        M[k + p * CMAX] = cs * mkp - sn * mkq;
+                        M[k + q * CMAX] = sn * mkp + cs * mkq;
+                    }
+                    for (int k = 0; k < c; k++) {
+                        const double mpk = M[p + k * CMAX], mqk = M[q + k * CMAX];
+                        M[p + k * CMAX] = cs * mpk - sn * mqk;
+                        M[q + k * CMAX] = sn * mpk + cs * mqk;
+                    }
+                    for (int k = 0; k < c; k++) {
+                        const double qkp = Q[k + p * CMAX], qkq = Q[k + q * CMAX];
+                        Q[k + p * CMAX] = cs * qkp - sn * qkq;
+                        Q[k + q * CMAX] = sn * qkp + cs * qkq;
+                    }
                 }
         }
+    }
+    __syncwarp();
+    __shared__ int ord[CMAX];
+    if (lane == 0) {
+        for (int a = 0; a < c; a++) ord[a] = a;
+        for (int a = 1; a < c; a++) {
+            const int x = ord[a];
+            int b = a - 1;
+            while (b >= 0 && M[ord[b] * (CMAX + 1)] > M[x * (CMAX + 1)]) { ord[b + 1] = ord[b]; b--; }
+            ord[b + 1] = x;
+        }
+    }
+    __syncwarp();
+    for (int a = 0; a < c; a++) {
+        const int i = s0 + a, col = ord[a];
+        double fx = 0, fy = 0;
+        for (int k = lane; k < n; k += 32) {
+            double v = 0;
+            for (int b = 0; b < c; b++) v += Zc[k + (size_t)b * n] * Q[b + col * CMAX];
+            if (y) {
+                fx += y[k].x * v;
+                fy -= y[k].y * v;
+            }
+            if (i < n_store) z[(size_t)k + (size_t)i * ldz] = (TZ)v;
+        }
+        fx = warp_dsum(fx);
+        fy = warp_dsum(fy);
+        if (lane == 0) {
+            w[i] = M[col * (CMAX + 1)];
+            if (f) f[i] = make_double2(fx, fy);
+        }
+    }
+}
+
+// Compact-WY factors of the reflector panels: panel p holds reflectors k0 = 32p .. k0+nb-1 and
+// Q_p = H_k0 ... H_{k0+nb-1} = I - V T V^H with T upper triangular (forward zlarft).
+// V[r][i] = 0 above row k0+i+1, 1 at row k0+i+1, A[r, k0+i] below.  One block per panel.
+template <typename T2>
+__device__ __forceinline__ T2 vpanel(const T2* __restrict__ A, int64_t lda, int k0, int i, int r) {
+    const int top = k0 + i + 1;
+    if (r < top) return C2<T2>(0, 0);
+    if (r == top) return C2<T2>(1, 0);
+    return A[r + (int64_t)(k0 + i) * lda];
+}
+
+template <typename T2>
+__global__ void __launch_bounds__(256) larft_kernel(int n, const T2* __restrict__ A, int64_t lda,
+                                                    const T2* __restrict__ tau, T2* __restrict__ Tout) {
+    typedef typename Real<T2>::t R;
+    constexpr int NB = 32;
+    __shared__ T2 G[NB][NB + 1];
+    __shared__ T2 Tm[NB][NB + 1];
+    const int p = blockIdx.x, k0 = p * NB, nref = n - 1;
+    const int nb = min(NB, nref - k0);
+    const int tid = threadIdx.x;
+    // Gram matrix G[j][i] = sum_r conj(V[r][j]) V[r][i], j < i (pairs spread over threads)
+    for (int pr = tid; pr < NB * NB; pr += blockDim.x) {
+        const int j = pr / NB, i = pr % NB;
+        if (!(j < i && i < nb)) continue;
+        R sx = 0, sy = 0;
+        for (int r = k0 + i + 1; r < n; r++) {
+            const T2 q = cconjmul(vpanel(A, lda, k0, j, r), vpanel(A, lda, k0, i, r));
+            sx += q.x;
+            sy += q.y;
+        }
+        G[j][i] = C2<T2>(sx, sy);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int i = 0; i < nb; i++) {
+            const T2 ti = tau[k0 + i];
+            // w = -tau_i * G[0:i, i];  T[0:i, i] = T[0:i, 0:i] w
+            for (int j = 0; j < i; j++) Tm[j][i] = cmul(C2<T2>(-ti.x, -ti.y), G[j][i]);
+            for (int j = 0; j < i; j++) {
+                T2 acc = C2<T2>(0, 0);
+                for (int l = j; l < i; l++) acc = cadd(acc, cmul(Tm[j][l], Tm[l][i]));
+                G[j][0] = acc;   // G column 0 is free now (rows j < i only)
+            }
+            for (int j = 0; j < i; j++) Tm[j][i] = G[j][0];
+            Tm[i][i] = ti;
+            for (int j = i + 1; j < NB; j++) Tm[j][i] = C2<T2>(0, 0);
+        }
+    }
+    __syncthreads();
+    for (int pr = tid; pr < NB * NB; pr += blockDim.x) {
+        const int j = pr / NB, i = pr % NB;
+        Tout[(size_t)p * NB * NB + pr] = (j <= i && i < nb) ? Tm[j][i] : C2<T2>(0, 0);
+    }
+}
+
+// X[:, cols of this block] <- Q X, panels from last to first: X -= V (T (V^H X)).
+// Warp w accumulates the dots of reflectors w, w+8, w+16, w+24 for the block's CB columns.
+template <typename T2, int CB>
+__global__ void __launch_bounds__(256) apply_wy_kernel(int n, const T2* __restrict__ A, int64_t lda,
+                                                       const T2* __restrict__ Tf, T2* __restrict__ X, int64_t ldx,
+                                                       int ncols) {
+    typedef typename Real<T2>::t R;
+    constexpr int NB = 32;
+    __shared__ T2 W[NB][CB];
+    __shared__ T2 W2[NB][CB];
+    __shared__ T2 Ts[NB][NB + 1];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int c0 = blockIdx.x * CB;
+    const int npanel = (n - 1 + NB - 1) / NB;
+    for (int p = npanel - 1; p >= 0; p--) {
+        const int k0 = p * NB;
+        const int nb = min(NB, n - 1 - k0);
+        for (int pr = tid; pr < NB * NB; pr += blockDim.x) Ts[pr / NB][pr % NB] = Tf[(size_t)p * NB * NB + pr];
+        // W = V^H X
+        R ax[4][CB], ay[4][CB];
 #pragma unroll
-        for (int j = 0; j < CB; j++) {
-            px[j] = warp_sum(px[j]);
-            py[j] = warp_sum(py[j]);
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int j = 0; j < CB; j++) ax[q][j] = ay[q][j] = 0;
+        for (int r = k0 + 1 + lane; r < n; r += 32) {
+            T2 xv[CB];
+#pragma unroll
+            for (int j = 0; j < CB; j++) xv[j] = (c0 + j < ncols) ? X[r + (int64_t)(c0 + j) * ldx] : C2<T2>(0, 0);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int i = warp + 8 * q;
+                if (i >= nb) continue;
+                const T2 v = vpanel(A, lda, k0, i, r);
+#pragma unroll
+                for (int j = 0; j < CB; j++) {
+                    const T2 t = cconjmul(v, xv[j]);
+                    ax[q][j] += t.x;
+                    ay[q][j] += t.y;
+                }
+            }
         }
-        if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
             for (int j = 0; j < CB; j++) {
-                red[2 * j][warp] = px[j];
-                red[2 * j + 1][warp] = py[j];
+                const R sx = warp_sum(ax[q][j]), sy = warp_sum(ay[q][j]);
+                if (lane == 0) W[warp + 8 * q][j] = C2<T2>(sx, sy);
             }
         __syncthreads();
-        if (tid < CB) {
-            R sx = 0, sy = 0;
-            for (int w = 0; w < nwarp; w++) {
-                sx += red[2 * tid][w];
-                sy += red[2 * tid + 1][w];
-            }
-            const T2 tt = adjoint ? C2<T2>(tk.x, -tk.y) : tk;
-            coef[tid] = cmul(tt, C2<T2>(sx, sy));
+        // W2 = T W (T upper triangular)
+        for (int pr = tid; pr < NB * CB; pr += blockDim.x) {
+            const int i = pr / CB, j = pr % CB;
+            T2 acc = C2<T2>(0, 0);
+            if (i < nb)
+                for (int l = i; l < nb; l++) acc = cadd(acc, cmul(Ts[i][l], W[l][j]));
+            W2[i][j] = acc;
         }
         __syncthreads();
-        for (int r = k + 1 + tid; r < n; r += blockDim.x) {
-            const T2 v = (r == k + 1) ? C2<T2>(1, 0) : A[r + (int64_t)k * lda];
+        // X -= V W2
+        for (int r = k0 + 1 + tid; r < n; r += blockDim.x) {
+            T2 acc[CB];
+#pragma unroll
+            for (int j = 0; j < CB; j++) acc[j] = C2<T2>(0, 0);
+            for (int i = 0; i < nb; i++) {
+                const T2 v = vpanel(A, lda, k0, i, r);
+#pragma unroll
+                for (int j = 0; j < CB; j++) acc[j] = cadd(acc[j], cmul(v, W2[i][j]));
+            }
 #pragma unroll
             for (int j = 0; j < CB; j++)
                 if (c0 + j < ncols) {
                     T2* xp = X + r + (int64_t)(c0 + j) * ldx;
-                    *xp = csub(*xp, cmul(coef[j], v));
+                    *xp = csub(*xp, acc[j]);
                 }
         }
         __syncthreads();
@@ -490,7 +859,7 @@ __global__ void real_to_complex_kernel(int64_t n, const typename Real<T2>::t* __
 template <typename R>
 __global__ void tri_prepare_kernel(int n, const R* __restrict__ d, const R* __restrict__ e, double* __restrict__ dd,
                                    double* __restrict__ ee, double* __restrict__ e2, float* __restrict__ df,
-                                   float* __restrict__ e2f) {
+                                   float* __restrict__ e2f, float* __restrict__ ef) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) {
         dd[t] = (double)d[t];
@@ -501,6 +870,7 @@ __global__ void tri_prepare_kernel(int n, const R* __restrict__ d, const R* __re
         ee[t] = x;
         e2[t] = x * x;
         e2f[t] = (float)(x * x);
+        ef[t] = (float)x;
     }
 }
 
@@ -525,24 +895,36 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int threads = 512;
     const int TR = 1024;
-    const size_t smem = 3 * (size_t)TR * sizeof(T2) + 64 * sizeof(R);
+    const size_t smem = 3 * (size_t)TR * sizeof(T2) + 4 * 32 * sizeof(R);
     int per_sm = 0;
     if ((st = cuda_check(c, cudaFuncSetAttribute(tridiag_kernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "tridiag smem"))) return st;
     if ((st = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_kernel<T2>, threads, smem), "occupancy"))) return st;
     if (per_sm < 1) return fail(c, BSE_ERR_CUDA, "tridiagonal kernel does not fit on an SM");
     const int B = nsm;   // one block per SM: cheapest barrier, 16 warps of loads in flight per SM
     const int nt_max = (n + TR - 1) / TR;
-    const int count_max = std::min(n, 8192);
+    // inverse-iteration batch: 61 bytes of scratch per (eigenvalue, row); one batch fills the GPU
+    const int count_max = std::min(n, std::max(32 * nsm, (int)std::min<int64_t>(8192, (int64_t)(12e9 / (61.0 * n)))));
     // workspace
     size_t off = 0;
     auto carve = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
     const size_t o_d = carve(n * sizeof(R)), o_e = carve(n * sizeof(R)), o_tau = carve(n * sizeof(T2));
-    const size_t o_v = carve(2 * (size_t)n * sizeof(T2)), o_p = carve(2 * (size_t)n * sizeof(T2));
+    // one barrier per reflector while every block can afford to finish all column sums itself;
+    // BSE_TRIDIAG_MODE=shared|redundant overrides (tests run the large-n path at small n)
+    bool redundant = n <= 8192;
+    if (const char* mode = std::getenv("BSE_TRIDIAG_MODE")) {
+        if (std::string(mode) == "shared") redundant = false;
+        else if (std::string(mode) == "redundant") redundant = true;
+    }
+    const size_t nbuf = redundant ? (size_t)B : 2;
+    const size_t o_v = carve(nbuf * n * sizeof(T2)), o_p = carve(nbuf * n * sizeof(T2));
     const size_t o_pp = carve((size_t)nt_max * n * sizeof(T2)), o_dp = carve(2 * (size_t)B * sizeof(T2));
-    const size_t o_y = carve(n * sizeof(T2)), o_bar = carve(64);
+    const size_t o_y = carve((redundant ? (size_t)B : 1) * n * sizeof(T2)), o_bar = carve(64);
     const size_t o_dd = carve(n * 8), o_ee = carve(n * 8), o_e2 = carve(n * 8), o_df = carve(n * 4), o_e2f = carve(n * 4);
+    const size_t o_ef = carve(n * 4), o_cl = carve(n);
     const size_t o_y64 = carve(n * sizeof(double2));
-    const size_t o_scr = carve(5 * (size_t)n * count_max * 8), o_piv = carve((size_t)n * count_max);
+    const size_t cpad = (size_t)(count_max + 31) / 32 * 32;   // whole warps of scratch
+    const size_t o_scr = carve(5 * (size_t)n * cpad * 8), o_scr32 = carve(5 * (size_t)n * cpad * 4);
+    const size_t o_piv = carve((size_t)n * cpad);
     const size_t o_z = carve((size_t)n * std::max(n_vec, 1) * sizeof(R));
     if ((st = ensure_work(c, off))) return st;
     char* w = (char*)c->d_work;
@@ -553,28 +935,33 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     unsigned* bar = (unsigned*)(w + o_bar);
     int* err = (int*)(w + o_bar + 16);
     if ((st = cuda_check(c, cudaMemsetAsync(bar, 0, 64, c->stream), "barrier reset"))) return st;
-    if ((st = cuda_check(c, cudaMemsetAsync(w + o_v, 0, 2 * (size_t)n * sizeof(T2), c->stream), "v reset"))) return st;
-    if ((st = cuda_check(c, cudaMemsetAsync(w + o_p, 0, 2 * (size_t)n * sizeof(T2), c->stream), "p reset"))) return st;
+    if ((st = cuda_check(c, cudaMemsetAsync(w + o_v, 0, nbuf * n * sizeof(T2), c->stream), "v reset"))) return st;
+    if ((st = cuda_check(c, cudaMemsetAsync(w + o_p, 0, nbuf * n * sizeof(T2), c->stream), "p reset"))) return st;
     if ((st = cuda_check(c, cudaMemsetAsync(tau, 0, n * sizeof(T2), c->stream), "tau reset"))) return st;
     if (y) {
-        rho_to_y_kernel<T2><<<(n + 255) / 256, 256, 0, c->stream>>>(n, rho0, y);
-        c->launches++;
+        // redundant mode: one copy per block (identical updates), block 0's copy is read back
+        for (int bb = 0; bb < (redundant ? B : 1); bb++)
+            rho_to_y_kernel<T2><<<(n + 255) / 256, 256, 0, c->stream>>>(n, rho0, y + (size_t)bb * n);
+        c->launches += redundant ? B : 1;
     }
     TriArgs<T2> ta;
     ta.n = n; ta.A = A; ta.lda = lda; ta.d = d; ta.e = e; ta.tau = tau;
     ta.vbuf = (T2*)(w + o_v); ta.pbuf = (T2*)(w + o_p); ta.ppart = (T2*)(w + o_pp); ta.dpart = (T2*)(w + o_dp);
-    ta.y = y; ta.bar = bar; ta.err = err; ta.TR = TR;
+    ta.y = y; ta.bar = bar; ta.err = err; ta.TR = TR; ta.redundant = redundant ? 1 : 0;
     void* kargs[] = {&ta};
+    stage_begin(c, 8);
     if ((st = cuda_check(c, cudaLaunchCooperativeKernel((void*)tridiag_kernel<T2>, dim3(B), dim3(threads), kargs, smem, c->stream),
                          "tridiagonal kernel launch"))) return st;
     c->launches++;
+    stage_end(c, 8);
     // T in FP64 / FP32 copies for the bisection and inverse iteration
     double* dd = (double*)(w + o_dd);
     double* ee = (double*)(w + o_ee);
     double* e2 = (double*)(w + o_e2);
     float* df = (float*)(w + o_df);
     float* e2f = (float*)(w + o_e2f);
-    tri_prepare_kernel<R><<<(n + 255) / 256, 256, 0, c->stream>>>(n, d, e, dd, ee, e2, df, e2f);
+    float* ef = (float*)(w + o_ef);
+    tri_prepare_kernel<R><<<(n + 255) / 256, 256, 0, c->stream>>>(n, d, e, dd, ee, e2, df, e2f, ef);
     c->launches++;
     int herr = 0;
     std::vector<double> hd(n), he(n > 1 ? n - 1 : 1);
@@ -597,8 +984,35 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     ghi += 2.220446049250313e-16 * tnorm * n + 1e-300;
     const double pivmin = 2.2250738585072014e-308 * std::max(1.0, emax2);
     const float pivminf = 1.17549435e-38f * (float)std::max(1.0, emax2);
-    bisect_kernel<<<(n + 127) / 128, 128, 0, c->stream>>>(n, dd, e2, df, e2f, glo, ghi, pivmin, pivminf, dW);
+    signed char* cl = (signed char*)(w + o_cl);
+    stage_begin(c, 9);
+    bisect32_kernel<<<(n + 31) / 32, 32, 0, c->stream>>>(n, df, e2f, (float)glo, (float)ghi, pivminf, dW);
     c->launches++;
+    // clusters: runs of eigenvalues closer than FP32 bisection can resolve
+    std::vector<double> hw(n);
+    if ((st = cuda_check(c, cudaMemcpyAsync(hw.data(), dW, n * 8, cudaMemcpyDeviceToHost, c->stream), "w32"))) return st;
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "bisection"))) return st;
+    stage_end(c, 9);
+    const double ctol = 16.0 * 1.1920929e-7 * tnorm;
+    std::vector<signed char> hcl(n, 0);
+    std::vector<int> cs, cz;
+    std::vector<int64_t> co;
+    int64_t ctot = 0;
+    for (int i = 0; i < n;) {
+        int j = i;
+        while (j + 1 < n && hw[j + 1] - hw[j] <= ctol && j + 1 - i < 32) j++;
+        if (j > i) {
+            cs.push_back(i);
+            cz.push_back(j - i + 1);
+            co.push_back(ctot);
+            ctot += (int64_t)(j - i + 1) * n;
+            for (int q = i; q <= j; q++) hcl[q] = 1;
+        }
+        i = j + 1;
+    }
+    const int ncl = (int)cs.size();
+    if ((st = cuda_check(c, cudaMemcpyAsync(cl, hcl.data(), n, cudaMemcpyHostToDevice, c->stream), "cluster flags"))) return st;
+    stage_begin(c, 10);
     double2* y64 = nullptr;
     if (y) {
         y64 = (double2*)(w + o_y64);
@@ -608,11 +1022,39 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     R* z = (R*)(w + o_z);
     for (int i0 = 0; i0 < n; i0 += count_max) {
         const int cnt = std::min(count_max, n - i0);
-        if (i0 >= n_vec && !f_out) break;
-        invit_kernel<R><<<(cnt + 127) / 128, 128, 0, c->stream>>>(n, dd, ee, dW, i0, cnt, tnorm, y64, f_out, z, n, n_vec,
-                                                                   (double*)(w + o_scr), (signed char*)(w + o_piv));
+        invit_kernel<R><<<(cnt + 31) / 32, 32, 0, c->stream>>>(n, dd, ee, df, ef, dW, cl, i0, cnt, tnorm, y64, f_out, z, n,
+                                                                 n_vec, (double*)(w + o_scr), (float*)(w + o_scr32),
+                                                                 (signed char*)(w + o_piv));
         c->launches++;
     }
+    stage_end(c, 10);
+    if (ncl > 0) {
+        // the batch scratch is free again once the batches above are done (same stream)
+        int* dcs = nullptr;
+        int* dcz = nullptr;
+        int64_t* dco = nullptr;
+        double* Zall = nullptr;
+        double* cscr = nullptr;
+        signed char* cpiv = nullptr;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&dcs, ncl * sizeof(int), c->stream), "clusters"))) return st;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&dcz, ncl * sizeof(int), c->stream), "clusters"))) return st;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&dco, ncl * sizeof(int64_t), c->stream), "clusters"))) return st;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&Zall, (size_t)ctot * 8, c->stream), "cluster vectors"))) return st;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&cscr, 5 * (size_t)n * ncl * 8, c->stream), "cluster scratch"))) return st;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&cpiv, (size_t)n * ncl, c->stream), "cluster pivots"))) return st;
+        cudaMemcpyAsync(dcs, cs.data(), ncl * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(dcz, cz.data(), ncl * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(dco, co.data(), ncl * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream);
+        stage_begin(c, 12);
+        cluster_kernel<R><<<ncl, 32, 0, c->stream>>>(n, dd, ee, dW, dcs, dcz, dco, ncl, tnorm, y64, f_out, z, n, n_vec, cscr,
+                                                      cpiv, Zall);
+        stage_end(c, 12);
+        c->launches++;
+        for (void* p : {(void*)dcs, (void*)dcz, (void*)dco, (void*)Zall, (void*)cscr, (void*)cpiv}) cudaFreeAsync(p, c->stream);
+        // cluster vectors must be in the host-visible count for the caller's stats
+        c->last_clusters = ncl;
+    }
+    stage_begin(c, 11);
     if ((st = cuda_check(c, cudaGetLastError(), "bisection / inverse iteration"))) return st;
     if (n_vec > 0) {
         // X = Q Z for the first n_vec eigenvectors; X is built in a separate buffer because A holds Q
@@ -621,14 +1063,22 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         const int64_t nz = (int64_t)n * n_vec;
         real_to_complex_kernel<T2><<<(unsigned)((nz + 255) / 256), 256, 0, c->stream>>>(nz, z, X);
         c->launches++;
-        constexpr int CB = 8;
-        apply_q_kernel<T2, CB><<<(n_vec + CB - 1) / CB, 256, 0, c->stream>>>(n, A, lda, tau, X, n, n_vec, false);
-        c->launches++;
+        if (n > 1) {
+            constexpr int CB = 4;
+            const int npanel = (n - 1 + 31) / 32;
+            T2* Tf = nullptr;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&Tf, (size_t)npanel * 32 * 32 * sizeof(T2), c->stream), "WY factors"))) return st;
+            larft_kernel<T2><<<npanel, 256, 0, c->stream>>>(n, A, lda, tau, Tf);
+            apply_wy_kernel<T2, CB><<<(n_vec + CB - 1) / CB, 256, 0, c->stream>>>(n, A, lda, Tf, X, n, n_vec);
+            c->launches += 2;
+            cudaFreeAsync(Tf, c->stream);
+        }
         st = cuda_check(c, cudaMemcpy2DAsync(A, lda * sizeof(T2), X, n * sizeof(T2), n * sizeof(T2), n_vec,
                                              cudaMemcpyDeviceToDevice, c->stream), "eigenvectors");
         cudaFreeAsync(X, c->stream);
         if (st) return st;
     }
+    stage_end(c, 11);
     return cuda_check(c, cudaGetLastError(), "own eigensolver");
 }
 

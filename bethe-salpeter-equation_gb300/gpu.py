@@ -76,7 +76,8 @@ def load(build_if_missing: bool = True):
     return L
 
 
-STAGES = ("bands", "tables", "build", "eig", "refine", "oscillators", "eps", "solve")
+STAGES = ("bands", "tables", "build", "eig", "refine", "oscillators", "eps", "solve",
+          "eig_tridiag", "eig_bisect", "eig_invit", "eig_backtransform", "eig_clusters")
 
 
 class BSEContext:

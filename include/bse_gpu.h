@@ -161,7 +161,9 @@ int bse_solve(bse_ctx* ctx, const double* omega, int32_t n_omega, double gamma,
 
 /* Device time (ms, CUDA events on the context stream) of the stages of the last calls:
  * [0] bands, [1] tables, [2] build, [3] eigensolve, [4] refinement, [5] oscillators, [6] eps,
- * [7] the whole of the last bse_solve. */
+ * [7] the whole of the last bse_solve; with BSE_EIG_OWN, the eigensolve's parts: [8] tridiagonal
+ * reduction, [9] eigenvalues, [10] inverse iteration, [11] back-transformation, [12] clusters
+ * resolved in FP64 (bse_stage_times resets unrecorded stages to 0). */
 int bse_stage_times(const bse_ctx* ctx, double* ms, int32_t n);
 
 /* Allocation-free dielectric function (no counterpart in the reference).  For callers that

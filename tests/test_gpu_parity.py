@@ -143,3 +143,38 @@ def test_stage_api_sequence(synth, oracle, gpu, solver):
     H = ref["H"]
     assert np.abs(A.conj().T @ H @ A - np.diag(E)).max() < 1e-8 * np.abs(E).max()
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
+
+
+@pytest.mark.parametrize("solver", ["own", "cusolver"])
+def test_degenerate_spectrum_weights(synth, oracle, gpu, solver):
+    """hBN in the independent-particle limit has exactly degenerate transitions (grid symmetry):
+    the eigenvectors inside each degenerate group must stay orthogonal, or the eps2 weights of
+    the group are wrong."""
+    prob = synth.hbn_problem(grid=12)
+    prob.params = prob.params.replace(ipa=1)
+    ref = oracle.solve(prob, OMEGA, GAMMA)
+    with gpu.BSEContext(prob, eig_solver=SOLVERS[solver]) as ctx:
+        E, e2, _ = ctx.solve(OMEGA, GAMMA)
+        f = ctx.oscillators()
+    assert np.abs(E - ref["E"]).max() < 1e-10
+    assert abs(np.sum(np.abs(f) ** 2) - np.sum(np.abs(ref["f"]) ** 2)) < 1e-9 * np.sum(np.abs(ref["f"]) ** 2)
+    assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
+
+
+@pytest.mark.parametrize("mode", ["shared", "redundant"])
+def test_tridiagonal_barrier_modes(synth, oracle, gpu, monkeypatch, mode):
+    """Both variants of the cooperative tridiagonal reduction (one grid barrier per reflector
+    with per-block copies, or two barriers with shared vectors -- the large-N path) give the
+    oracle's spectrum."""
+    monkeypatch.setenv("BSE_TRIDIAG_MODE", mode)
+    prob = synth.orb8_problem(grid=4)
+    ref = oracle.solve(prob, OMEGA, GAMMA)
+    for precision, tol in ((0, 1e-8), (1, None)):
+        with gpu.BSEContext(prob, precision=precision, eig_solver=0, n_refine=64) as ctx:
+            E, e2, _ = ctx.solve(OMEGA, GAMMA)
+        if tol is None:
+            assert np.abs(E[:64] - ref["E"][:64]).max() < 1e-6
+            assert np.linalg.norm(e2 - ref["eps2"]) < 1e-4 * np.linalg.norm(ref["eps2"])
+        else:
+            assert np.abs(E - ref["E"]).max() < tol
+            assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
