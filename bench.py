@@ -316,6 +316,40 @@ def run_gpu(args):
     return 0
 
 
+def run_batch(args):
+    """64 seeded 2- to 4-band models, grids 12x12 .. 30x30 (N_BSE 144 .. 3600): aggregate time of
+    one batched solve (bse_solve_many, 8 host workers) against the same solves one after another."""
+    import torch
+    entry.load_package()
+    from importlib import import_module
+    synth = import_module("bse_gb300.synth")
+    gpu = import_module("bse_gb300.gpu")
+    probs = synth.random_batch_problems(n_models=64, seed=77)
+    ctxs = [gpu.BSEContext(p, precision=1, n_refine=64, eig_solver=0) for p in probs]
+    gpu.solve_many(ctxs, OMEGA, GAMMA, n_workers=8)          # warm-up (workspaces, library modules)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        gpu.solve_many(ctxs, OMEGA, GAMMA, n_workers=8)
+        torch.cuda.synchronize()
+        ts.append((time.perf_counter() - t0) * 1e3)
+    t0 = time.perf_counter()
+    for c in ctxs:
+        c.solve(OMEGA, GAMMA)
+    seq = (time.perf_counter() - t0) * 1e3
+    ns = [p.n_bse for p in probs]
+    for c in ctxs:
+        c.close()
+    print(json.dumps({"metric": "batched BSE build+diag+eps2 wall time (64 models)", "value": float(np.median(ts)),
+                      "unit": "ms", "steps": args.steps, "higher_is_better": False, "n_gpus": 1,
+                      "config": {"workload": "batch64_rand_2to4band_12to30grid", "n_models": len(probs),
+                                 "n_bse_min": min(ns), "n_bse_max": max(ns), "n_bse_sum": sum(ns),
+                                 "precision": "mixed", "n_refine": 64, "workers": 8},
+                      "sequential_ms": seq, "models_per_s": len(probs) / (float(np.median(ts)) / 1e3)}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -325,7 +359,10 @@ def main():
     ap.add_argument("--solver", default="own", choices=["own", "cusolver"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
+    ap.add_argument("--workload", default="magnetic4", choices=["magnetic4", "batch"])
     args = ap.parse_args()
+    if args.workload == "batch":
+        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -8,8 +8,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <map>
 #include <new>
+#include <thread>
 
 #include "bse_internal.h"
 
@@ -466,6 +468,32 @@ int bse_solve(bse_ctx* c, const double* omega, int32_t n_omega, double gamma, do
     stage_end(c, 7);
     if (e_out && (st = cuda_check(c, cudaMemcpyAsync(e_out, c->d_E, c->n_exc * 8, cudaMemcpyDeviceToHost, c->stream), "E copy"))) return st;
     return cuda_check(c, cudaStreamSynchronize(c->stream), "solve");
+}
+
+int bse_solve_many(bse_ctx** ctxs, int32_t n_ctx, const double* omega, int32_t n_omega, double gamma, double* eps2,
+                   double* eps1, int32_t n_workers) {
+    if (!ctxs || n_ctx < 0 || (n_omega > 0 && !omega)) return fail(nullptr, BSE_ERR_BAD_INPUT, "bse_solve_many: arguments");
+    for (int i = 0; i < n_ctx; i++)
+        if (!ctxs[i]) return fail(nullptr, BSE_ERR_BAD_INPUT, "bse_solve_many: null context");
+    const int nw = std::max(1, std::min<int>(n_workers > 0 ? n_workers : 4, n_ctx));
+    std::atomic<int> next(0), first_err(0), first_idx(-1);
+    auto work = [&]() {
+        for (int i = next.fetch_add(1); i < n_ctx; i = next.fetch_add(1)) {
+            int st = bse_solve(ctxs[i], omega, n_omega, gamma, nullptr, eps2 ? eps2 + (size_t)i * n_omega : nullptr,
+                               eps1 ? eps1 + (size_t)i * n_omega : nullptr);
+            if (st) {
+                int expected = 0;
+                if (first_err.compare_exchange_strong(expected, st)) first_idx.store(i);
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nw; t++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    if (first_err.load())
+        g_create_err = "context " + std::to_string(first_idx.load()) + ": " + ctxs[first_idx.load()]->err;
+    return first_err.load();
 }
 
 int bse_stage_times(const bse_ctx* cc, double* ms, int32_t n) {

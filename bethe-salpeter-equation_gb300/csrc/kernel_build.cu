@@ -17,6 +17,8 @@
 // (2n-1)^d of them); the build kernel then writes each element of H exactly once, k1
 // fastest so that a warp stores 32 consecutive elements of one column: the kernel is
 // bound by the N^2 store of H, not by arithmetic (inner dimension nw <= 16).
+#include <mutex>
+
 #include "bse_internal.h"
 
 namespace bse {
@@ -431,10 +433,14 @@ int launch_build_nw(bse_ctx* c, void* H, int64_t ld, bool lower, const void* phi
     const int KW = 8;
     dim3 block(32, KW), grid((c->nk + 31) / 32, (c->nk + KW - 1) / KW, 1);
     size_t smem = (size_t)KW * (c->nc + c->nv) * c->nb * sizeof(typename cplx<T>::t);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(build_kernel<NW, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return cuda_check(c, e, "build smem attribute");
-    }
+    // process-wide attribute: set once to the largest size (nc, nv <= 8, nb <= 32)
+    static std::once_flag smem_once;
+    static cudaError_t smem_err = cudaSuccess;
+    std::call_once(smem_once, [] {
+        const int smax = 8 * (8 + 8) * 32 * (int)sizeof(typename cplx<T>::t);
+        smem_err = cudaFuncSetAttribute(build_kernel<NW, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    });
+    if (smem_err != cudaSuccess) return cuda_check(c, smem_err, "build smem attribute");
     build_kernel<NW, T><<<grid, block, smem, c->stream>>>(
         a, (const typename cplx<T>::t*)phi, (const typename cplx<T>::t*)qx, (typename cplx<T>::t*)H);
     c->launches++;

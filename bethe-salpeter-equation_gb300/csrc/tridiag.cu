@@ -25,6 +25,7 @@
 #include <cooperative_groups.h>
 
 #include <cstdlib>
+#include <mutex>
 #include <string>
 
 #include "bse_internal.h"
@@ -225,12 +226,12 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
                 T2* col = A + (int64_t)c * lda;
                 R accx = 0, accy = 0;
                 int r = r0 + lane;
-                for (; r + 96 < r1; r += 128) {          // four independent loads in flight per lane
-                    T2 x[4];
+                for (; r + 224 < r1; r += 256) {         // eight independent loads in flight per lane
+                    T2 x[8];
 #pragma unroll
-                    for (int u = 0; u < 4; u++) x[u] = col[r + 32 * u];
+                    for (int u = 0; u < 8; u++) x[u] = col[r + 32 * u];
 #pragma unroll
-                    for (int u = 0; u < 4; u++) {
+                    for (int u = 0; u < 8; u++) {
                         const int i = r + 32 * u - r0;
                         if (have_prev) {
                             x[u] = csub(csub(x[u], cmulc(sv[i], wc)), cmulc(sw[i], vc));
@@ -894,13 +895,26 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     int dev = c->device, nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int threads = 512;
-    const int TR = 1024;
+    // tuning overrides (sweeps): BSE_TRIDIAG_BLOCKS (grid size) and BSE_TRIDIAG_TR (tile rows)
+    int TR = std::min(4096, std::max(256, (n + 255) / 256 * 256));   // one tile for n <= 4096
+    if (const char* v = std::getenv("BSE_TRIDIAG_TR")) TR = std::max(64, std::min(4096, std::atoi(v)));
     const size_t smem = 3 * (size_t)TR * sizeof(T2) + 4 * 32 * sizeof(R);
     int per_sm = 0;
-    if ((st = cuda_check(c, cudaFuncSetAttribute(tridiag_kernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "tridiag smem"))) return st;
+    // the attribute is process-wide: set it once, to the largest tile any call uses (TR <= 4096),
+    // so concurrent contexts with different sizes never shrink it under each other
+    static std::once_flag smem_once;
+    static cudaError_t smem_err = cudaSuccess;
+    std::call_once(smem_once, [] {
+        const int smax = 3 * 4096 * (int)sizeof(T2) + 4 * 32 * (int)sizeof(R);
+        smem_err = cudaFuncSetAttribute(tridiag_kernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    });
+    if ((st = cuda_check(c, smem_err, "tridiag smem"))) return st;
     if ((st = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_kernel<T2>, threads, smem), "occupancy"))) return st;
     if (per_sm < 1) return fail(c, BSE_ERR_CUDA, "tridiagonal kernel does not fit on an SM");
-    const int B = nsm;   // one block per SM: cheapest barrier, 16 warps of loads in flight per SM
+    // one block per SM (16 warps of loads in flight each) once the matrix is large enough; small
+    // matrices (batched runs) use ~n/16 blocks so several models' reductions can share the GPU
+    int B = std::max(4, std::min(nsm, n / 16));
+    if (const char* v = std::getenv("BSE_TRIDIAG_BLOCKS")) B = std::max(1, std::min(nsm * per_sm, std::atoi(v)));
     const int nt_max = (n + TR - 1) / TR;
     // inverse-iteration batch: 61 bytes of scratch per (eigenvalue, row); one batch fills the GPU
     const int count_max = std::min(n, std::max(32 * nsm, (int)std::min<int64_t>(8192, (int64_t)(12e9 / (61.0 * n)))));

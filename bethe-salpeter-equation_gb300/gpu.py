@@ -25,6 +25,7 @@ EXPORTS = [
     "bse_create", "bse_destroy", "bse_compute_bands", "bse_get_bands", "bse_set_bands",
     "bse_build_kernel", "bse_diagonalize", "bse_oscillators", "bse_eps", "bse_solve",
     "bse_stage_times", "bse_kernel_launches", "bse_reset_kernel_launches", "bse_eps_noalloc",
+    "bse_solve_many",
 ]
 
 
@@ -72,6 +73,7 @@ def load(build_if_missing: bool = True):
     L.bse_reset_kernel_launches.argtypes = [C.c_void_p]
     L.bse_reset_kernel_launches.restype = None
     L.bse_eps_noalloc.argtypes = [C.c_int64, _dp, _dp, C.c_double, _dp, C.c_int32, C.c_double, _dp, _dp, C.c_void_p]
+    L.bse_solve_many.argtypes = [C.POINTER(C.c_void_p), C.c_int32, _dp, C.c_int32, C.c_double, _dp, _dp, C.c_int32]
     _LIB = L
     return L
 
@@ -171,3 +173,16 @@ class BSEContext:
 
     def reset_kernel_launches(self):
         self.lib.bse_reset_kernel_launches(self.h)
+
+
+def solve_many(contexts, omega, gamma, n_workers=8):
+    """bse_solve_many over BSEContext objects: returns eps2, eps1 (n_ctx x n_omega)."""
+    lib = load()
+    om = np.ascontiguousarray(omega, dtype=np.float64)
+    arr = (C.c_void_p * len(contexts))(*[c.h.value for c in contexts])
+    e2 = np.zeros((len(contexts), len(om)))
+    e1 = np.zeros((len(contexts), len(om)))
+    st = lib.bse_solve_many(arr, len(contexts), ptr(om), len(om), float(gamma), ptr(e2), ptr(e1), int(n_workers))
+    if st != 0:
+        raise BSEError(st, lib.bse_last_error(None).decode())
+    return e2, e1

@@ -159,6 +159,13 @@ int bse_eps(bse_ctx* ctx, const double* omega, int32_t n_omega, double gamma,
 int bse_solve(bse_ctx* ctx, const double* omega, int32_t n_omega, double gamma,
               double* e_out, double* eps2, double* eps1);
 
+/* Batched solves: runs bse_solve on n_ctx existing contexts (each on its own stream) from
+ * n_workers host threads, so one model's host-side steps overlap the others' device work.
+ * eps2 / eps1 (nullable) are n_ctx x n_omega row-major (model slowest).  Returns the first
+ * failing status (every context is still attempted).  No counterpart in the reference. */
+int bse_solve_many(bse_ctx** ctxs, int32_t n_ctx, const double* omega, int32_t n_omega, double gamma,
+                   double* eps2, double* eps1, int32_t n_workers);
+
 /* Device time (ms, CUDA events on the context stream) of the stages of the last calls:
  * [0] bands, [1] tables, [2] build, [3] eigensolve, [4] refinement, [5] oscillators, [6] eps,
  * [7] the whole of the last bse_solve; with BSE_EIG_OWN, the eigensolve's parts: [8] tridiagonal
