@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -350,6 +351,58 @@ def run_batch(args):
     return 0
 
 
+def run_large(args):
+    """8-orbital model, 4v x 4c, complex64 BSE matrix, FP64 refinement of the lowest 256:
+    a mixed solve at 48x48 (N_BSE = 36864) with its FP64 residual bound, and FP64 (cuSOLVER
+    zheevd) vs mixed solves at 12x12 and 24x24 (N_BSE = 2304, 9216) for the same-size eigenvalue
+    errors and the N^3 extrapolation of the plain FP64 GPU time to N_BSE = 36864."""
+    import torch
+    entry.load_package()
+    from importlib import import_module
+    synth = import_module("bse_gb300.synth")
+    gpu = import_module("bse_gb300.gpu")
+    out = {"metric": "BSE build+diag wall time at N_BSE=36864 (mixed) vs plain FP64 GPU path", "unit": "ms",
+           "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+           "config": {"workload": "orb8_48x48_4v4c", "precision": "mixed", "n_refine": 256, "eig_solver": "own"}}
+    small = {}
+    for grid in (12, 24):
+        prob = synth.orb8_problem(grid=grid)
+        with gpu.BSEContext(prob, precision=0, eig_solver=1) as c64:
+            c64.solve(OMEGA, GAMMA)
+            E64, e2_64, _ = c64.solve(OMEGA, GAMMA)
+            t64 = c64.stage_times()["solve"]
+        with gpu.BSEContext(prob, precision=1, n_refine=256, eig_solver=0) as cm:
+            cm.solve(OMEGA, GAMMA)
+            Em, e2m, _ = cm.solve(OMEGA, GAMMA)
+            tm = cm.stage_times()
+            dg = cm.diagnostics()
+        small[prob.n_bse] = {"fp64_cusolver_ms": t64, "mixed_own_ms": tm["solve"], "mixed_stages_ms": tm,
+                             "max_err_refined_256_ev": float(np.abs(Em[:256] - E64[:256]).max()),
+                             "max_err_all_ev": float(np.abs(Em - E64).max()),
+                             "eps2_rel_l2": float(np.linalg.norm(e2m - e2_64) / np.linalg.norm(e2_64)),
+                             "max_refined_residual_ev": dg["max_refined_residual"], "clusters": dg["clusters"]}
+        print(json.dumps({"n_bse": prob.n_bse, **small[prob.n_bse]}), file=sys.stderr, flush=True)
+    prob = synth.orb8_problem(grid=48)
+    with gpu.BSEContext(prob, precision=1, n_refine=256, eig_solver=0) as cm:
+        t0 = time.perf_counter()
+        cm.solve(OMEGA, GAMMA)
+        first = (time.perf_counter() - t0) * 1e3
+        if args.steps > 1:
+            cm.solve(OMEGA, GAMMA)
+        st = cm.stage_times()
+        dg = cm.diagnostics()
+    n1, n2 = 2304, 9216
+    expo = math.log(small[n2]["fp64_cusolver_ms"] / small[n1]["fp64_cusolver_ms"]) / math.log(n2 / n1)
+    fp64_est = small[n2]["fp64_cusolver_ms"] * (36864 / n2) ** 3
+    out.update({"value": st["solve"], "ms_per_step": st["solve"], "first_solve_wall_ms": first, "stages_ms": st,
+                "n_bse": prob.n_bse, "max_refined_residual_ev": dg["max_refined_residual"],
+                "clusters": dg["clusters"], "fp64_cusolver_ms_extrapolated_n3": fp64_est,
+                "fp64_growth_exponent_2304_9216": expo, "speedup_vs_fp64_gpu_extrapolated": fp64_est / st["solve"],
+                "smaller_sizes": small})
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -359,10 +412,12 @@ def main():
     ap.add_argument("--solver", default="own", choices=["own", "cusolver"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
-    ap.add_argument("--workload", default="magnetic4", choices=["magnetic4", "batch"])
+    ap.add_argument("--workload", default="magnetic4", choices=["magnetic4", "batch", "large"])
     args = ap.parse_args()
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "large":
+        return run_large(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -105,6 +105,7 @@ struct bse_ctx {
     bool f_from_eig = false;     // the own solver produced f for every exciton
     int64_t n_refined = 0;       // leading columns replaced by the FP64 refinement
     int last_clusters = 0;       // clusters the own eigensolver resolved in FP64 in its last call
+    double max_residual = 0;     // max ||H x - theta x||_2 (FP64) over the refined eigenpairs
     // workspaces
     void* d_work = nullptr;
     size_t work_bytes = 0;

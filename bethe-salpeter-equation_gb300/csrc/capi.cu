@@ -509,6 +509,13 @@ int bse_stage_times(const bse_ctx* cc, double* ms, int32_t n) {
     return BSE_OK;
 }
 
+int bse_diagnostics(const bse_ctx* c, double* out, int32_t n) {
+    if (!c || !out) return BSE_ERR_BAD_INPUT;
+    const double v[4] = {c->max_residual, (double)c->last_clusters, (double)c->n_refined, (double)c->n_vec_valid};
+    for (int i = 0; i < n && i < 4; i++) out[i] = v[i];
+    return BSE_OK;
+}
+
 int64_t bse_kernel_launches(const bse_ctx* c) { return c ? c->launches : 0; }
 void bse_reset_kernel_launches(bse_ctx* c) {
     if (c) c->launches = 0;

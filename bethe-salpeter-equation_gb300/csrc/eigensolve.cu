@@ -30,6 +30,28 @@ __global__ void f2d_kernel(int64_t n, const float* __restrict__ a, double* __res
     if (t < n) b[t] = a[t];
 }
 
+// ||HX_j - theta_j X_j||_2 for column j (one block per column)
+__global__ void residual_kernel(int64_t n, const double2* __restrict__ HX, const double2* __restrict__ X,
+                                const double* __restrict__ theta, double* __restrict__ out) {
+    const int64_t j = blockIdx.x;
+    const double t = theta[j];
+    double s = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 h = HX[i + j * n], x = X[i + j * n];
+        const double rx = h.x - t * x.x, ry = h.y - t * x.y;
+        s += rx * rx + ry * ry;
+    }
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) out[j] = sqrt(s);
+    }
+}
+
 int cusolver_check(bse_ctx* c, cusolverStatus_t s, const char* what) {
     if (s == CUSOLVER_STATUS_SUCCESS) return BSE_OK;
     if (s == CUSOLVER_STATUS_ALLOC_FAILED) return fail(c, BSE_ERR_OOM, std::string(what) + ": cuSOLVER allocation failed");
@@ -143,6 +165,7 @@ int run_refine(bse_ctx* c) {
     size_t off = 0;
     auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
     const size_t oX = carve(n * m * sizeof(double2)), oY = carve(n * m * sizeof(double2));
+    const size_t oZ = carve(n * m * sizeof(double2)), oN = carve(m * sizeof(double));
     const size_t oG = carve(m * m * sizeof(double2)), oT = carve(m * sizeof(double));
     const size_t oB = c->S ? carve((size_t)n * n * sizeof(double2)) : 0;
     // potrf / heevd workspaces on top
@@ -200,15 +223,27 @@ int run_refine(bse_ctx* c) {
     if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m,
                                                  CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo), "heevd m"))) return st;
     cusolverDnDestroyParams(prm);
-    // Y = X Z  (refined Ritz vectors)
+    // XZ = X Z (refined Ritz vectors) and HXZ = (H X) Z; residuals r_j = HXZ_j - theta_j XZ_j
+    double2* XZ = (double2*)(base + oZ);
     if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, (cuDoubleComplex*)X, n,
-                                          (cuDoubleComplex*)G, m, &zero, (cuDoubleComplex*)Y, n), "gemm XZ"))) return st;
+                                          (cuDoubleComplex*)G, m, &zero, (cuDoubleComplex*)XZ, n), "gemm XZ"))) return st;
+    if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, (cuDoubleComplex*)Y, n,
+                                          (cuDoubleComplex*)G, m, &zero, (cuDoubleComplex*)X, n), "gemm HXZ"))) return st;
+    double* rn = (double*)(base + oN);
+    residual_kernel<<<(unsigned)nref, 256, 0, c->stream>>>(n, X, XZ, theta, rn);
+    c->launches++;
+    Y = XZ;
     // write back the lowest nref pairs
     double* E = c->S ? c->d_E + 2 * c->N : c->d_E;
     if ((st = cuda_check(c, cudaMemcpyAsync(E, theta, nref * sizeof(double), cudaMemcpyDeviceToDevice, c->stream), "theta"))) return st;
     narrow_kernel<<<(unsigned)((n * nref + 255) / 256), 256, 0, c->stream>>>(n * nref, Y, (float2*)c->d_A);
     c->launches++;
     c->n_refined = nref;
+    std::vector<double> hrn(nref);
+    if ((st = cuda_check(c, cudaMemcpyAsync(hrn.data(), rn, nref * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "residuals"))) return st;
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "residuals"))) return st;
+    c->max_residual = 0;
+    for (double v : hrn) c->max_residual = std::max(c->max_residual, v);
     stage_end(c, 4);
     return cuda_check(c, cudaGetLastError(), "refine");
 }

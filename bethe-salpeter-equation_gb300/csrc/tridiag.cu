@@ -1025,6 +1025,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         i = j + 1;
     }
     const int ncl = (int)cs.size();
+    c->last_clusters = ncl;
     if ((st = cuda_check(c, cudaMemcpyAsync(cl, hcl.data(), n, cudaMemcpyHostToDevice, c->stream), "cluster flags"))) return st;
     stage_begin(c, 10);
     double2* y64 = nullptr;
@@ -1065,8 +1066,6 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         stage_end(c, 12);
         c->launches++;
         for (void* p : {(void*)dcs, (void*)dcz, (void*)dco, (void*)Zall, (void*)cscr, (void*)cpiv}) cudaFreeAsync(p, c->stream);
-        // cluster vectors must be in the host-visible count for the caller's stats
-        c->last_clusters = ncl;
     }
     stage_begin(c, 11);
     if ((st = cuda_check(c, cudaGetLastError(), "bisection / inverse iteration"))) return st;

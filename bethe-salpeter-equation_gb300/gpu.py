@@ -25,7 +25,7 @@ EXPORTS = [
     "bse_create", "bse_destroy", "bse_compute_bands", "bse_get_bands", "bse_set_bands",
     "bse_build_kernel", "bse_diagonalize", "bse_oscillators", "bse_eps", "bse_solve",
     "bse_stage_times", "bse_kernel_launches", "bse_reset_kernel_launches", "bse_eps_noalloc",
-    "bse_solve_many",
+    "bse_solve_many", "bse_diagnostics",
 ]
 
 
@@ -73,6 +73,7 @@ def load(build_if_missing: bool = True):
     L.bse_reset_kernel_launches.argtypes = [C.c_void_p]
     L.bse_reset_kernel_launches.restype = None
     L.bse_eps_noalloc.argtypes = [C.c_int64, _dp, _dp, C.c_double, _dp, C.c_int32, C.c_double, _dp, _dp, C.c_void_p]
+    L.bse_diagnostics.argtypes = [C.c_void_p, _dp, C.c_int32]
     L.bse_solve_many.argtypes = [C.POINTER(C.c_void_p), C.c_int32, _dp, C.c_int32, C.c_double, _dp, _dp, C.c_int32]
     _LIB = L
     return L
@@ -167,6 +168,12 @@ class BSEContext:
         ms = np.zeros(len(STAGES))
         self._check(self.lib.bse_stage_times(self.h, ptr(ms), len(STAGES)))
         return dict(zip(STAGES, ms.tolist()))
+
+    def diagnostics(self):
+        out = np.zeros(4)
+        self._check(self.lib.bse_diagnostics(self.h, ptr(out), 4))
+        return {"max_refined_residual": out[0], "clusters": int(out[1]), "n_refined": int(out[2]),
+                "n_vectors": int(out[3])}
 
     def kernel_launches(self) -> int:
         return int(self.lib.bse_kernel_launches(self.h))

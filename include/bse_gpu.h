@@ -189,6 +189,11 @@ int bse_eps_noalloc(int64_t n_exc, const double* e, const double* f, double pref
                     const double* omega, int32_t n_omega, double gamma,
                     double* eps2, double* eps1, void* stream);
 
+/* Diagnostics of the last solve: [0] max FP64 residual ||H x - theta x||_2 (eV) over the refined
+ * eigenpairs (an eigenvalue error bound), [1] eigenvalue clusters the own solver resolved in FP64,
+ * [2] refined eigenpairs, [3] eigenvector columns formed. */
+int bse_diagnostics(const bse_ctx* ctx, double* out, int32_t n);
+
 /* Launch/kernel statistics of the context: number of this library's kernel launches since
  * creation or the last reset. */
 int64_t bse_kernel_launches(const bse_ctx* ctx);
