@@ -135,4 +135,12 @@ int run_eps(bse_ctx* c, const double* omega, int n_omega, double gamma, double* 
 int own_heevd(bse_ctx* c, int n, void* dA, int lda, bool fp64, double* dW, int n_vec, const double2* rho0,
               double2* f_out);
 
+// two-stage reduction (band.cu): dense -> band -> real tridiagonal (d, e), y <- Q^H y; with keep_q the
+// reflectors stay in ws for band_backtransform (X = Q Z, Z real n x n_vec).  bar/err: barrier words.
+size_t band_workspace(int n, bool fp64, bool keep_q, int n_vec, int nsm);
+int band_tridiag(bse_ctx* c, int n, void* A, int64_t lda, bool fp64, void* d, void* e, void* y, bool keep_q, char* ws,
+                 unsigned* bar, int* err, int n_vec);
+int band_backtransform(bse_ctx* c, int n, bool fp64, const void* z, int n_vec, void* X, char* ws, unsigned* bar,
+                       int* err);
+
 }  // namespace bse

@@ -1,0 +1,101 @@
+// Device helpers shared by the eigensolver kernels: complex arithmetic on float2 / double2,
+// warp and block reductions, and the bounded grid-wide barrier of the cooperative kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace bse {
+namespace dev {
+
+template <typename T2> struct Real;
+template <> struct Real<float2> { typedef float t; };
+template <> struct Real<double2> { typedef double t; };
+
+template <typename T2> __device__ __forceinline__ T2 C2(typename Real<T2>::t x, typename Real<T2>::t y) {
+    T2 r; r.x = x; r.y = y; return r;
+}
+template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { return C2<T2>(a.x + b.x, a.y + b.y); }
+template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { return C2<T2>(a.x - b.x, a.y - b.y); }
+template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+    return C2<T2>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename T2> __device__ __forceinline__ T2 cmulc(T2 a, T2 b) {
+    return C2<T2>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+// conj(a) * b
+template <typename T2> __device__ __forceinline__ T2 cconjmul(T2 a, T2 b) {
+    return C2<T2>(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+template <typename T2> __device__ __forceinline__ T2 cinv(T2 a) {
+    typedef typename Real<T2>::t R;
+    R s = a.x * a.x + a.y * a.y;
+    return C2<T2>(a.x / s, -a.y / s);
+}
+
+constexpr unsigned kSpinLimit = 1u << 26;   // ~seconds of polling before a barrier gives up
+
+// Grid-wide barrier for a cooperative launch.  bar[0] arrivals, bar[1] generation.
+// Returns false (after setting *err) if a block did not arrive in time or another block failed.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = bar + 1;
+        volatile int* verr = err;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned it = 0;
+            while (*vgen == gen) {
+                if (*verr != 0) break;
+                if (++it > kSpinLimit) { atomicExch(err, 1); break; }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)err == 0;
+}
+
+template <typename R>
+__device__ __forceinline__ R warp_sum(R v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of a real value; every thread gets the result.  `red` holds >= 32 R.
+template <typename R>
+__device__ __forceinline__ R block_sum(R v, R* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    R t = lane < nw ? red[lane] : R(0);
+    t = warp_sum(t);
+    return t;
+}
+
+// Block-wide sums of NV real values at once (one reduction round); every thread gets them.
+template <typename R, int NV>
+__device__ __forceinline__ void block_sums(R (&v)[NV], R* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; j++) v[j] = warp_sum(v[j]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NV; j++) red[j * 32 + wid] = v[j];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NV; j++) v[j] = warp_sum(lane < nw ? red[j * 32 + lane] : R(0));
+}
+
+}  // namespace dev
+}  // namespace bse

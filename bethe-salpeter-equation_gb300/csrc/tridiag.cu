@@ -29,99 +29,12 @@
 #include <string>
 
 #include "bse_internal.h"
+#include "dev_util.h"
 
 namespace bse {
 namespace {
 
-template <typename T2> struct Real;
-template <> struct Real<float2> { typedef float t; };
-template <> struct Real<double2> { typedef double t; };
-
-template <typename T2> __device__ __forceinline__ T2 C2(typename Real<T2>::t x, typename Real<T2>::t y) {
-    T2 r; r.x = x; r.y = y; return r;
-}
-template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { return C2<T2>(a.x + b.x, a.y + b.y); }
-template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { return C2<T2>(a.x - b.x, a.y - b.y); }
-template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
-    return C2<T2>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-// a * conj(b)
-template <typename T2> __device__ __forceinline__ T2 cmulc(T2 a, T2 b) {
-    return C2<T2>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
-}
-// conj(a) * b
-template <typename T2> __device__ __forceinline__ T2 cconjmul(T2 a, T2 b) {
-    return C2<T2>(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
-}
-template <typename T2> __device__ __forceinline__ T2 cinv(T2 a) {
-    typedef typename Real<T2>::t R;
-    R s = a.x * a.x + a.y * a.y;
-    return C2<T2>(a.x / s, -a.y / s);
-}
-
-constexpr unsigned kSpinLimit = 1u << 26;   // ~seconds of polling before a barrier gives up
-
-// Grid-wide barrier for a cooperative launch.  bar[0] arrivals, bar[1] generation.
-// Returns false (after setting *err) if a block did not arrive in time or another block failed.
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = bar + 1;
-        volatile int* verr = err;
-        const unsigned gen = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            unsigned it = 0;
-            while (*vgen == gen) {
-                if (*verr != 0) break;
-                if (++it > kSpinLimit) { atomicExch(err, 1); break; }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return *(volatile int*)err == 0;
-}
-
-template <typename R>
-__device__ __forceinline__ R warp_sum(R v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Block-wide sum of a real value; every thread gets the result.  `red` holds >= 32 R.
-template <typename R>
-__device__ __forceinline__ R block_sum(R v, R* red) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_sum(v);
-    __syncthreads();
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    R t = lane < nw ? red[lane] : R(0);
-    t = warp_sum(t);
-    return t;
-}
-
-// Block-wide sums of NV real values at once (one reduction round); every thread gets them.
-template <typename R, int NV>
-__device__ __forceinline__ void block_sums(R (&v)[NV], R* red) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int j = 0; j < NV; j++) v[j] = warp_sum(v[j]);
-    __syncthreads();
-    if (lane == 0)
-#pragma unroll
-        for (int j = 0; j < NV; j++) red[j * 32 + wid] = v[j];
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < NV; j++) v[j] = warp_sum(lane < nw ? red[j * 32 + lane] : R(0));
-}
+using namespace dev;
 
 template <typename T2>
 struct TriArgs {
@@ -888,6 +801,9 @@ __global__ void y_to_double_kernel(int n, const T2* __restrict__ y, double2* __r
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
+// above this order the two-stage reduction (band.cu) replaces the one-stage tridiag_kernel
+constexpr int kTwoStageMin = 8192;
+
 template <typename T2>
 int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, const double2* rho0, double2* f_out) {
     typedef typename Real<T2>::t R;
@@ -924,15 +840,22 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const size_t o_d = carve(n * sizeof(R)), o_e = carve(n * sizeof(R)), o_tau = carve(n * sizeof(T2));
     // one barrier per reflector while every block can afford to finish all column sums itself;
     // BSE_TRIDIAG_MODE=shared|redundant overrides (tests run the large-n path at small n)
+    // BSE_TRIDIAG_MODE=shared|redundant|twostage overrides (tests run every path at small n)
     bool redundant = n <= 8192;
+    bool two_stage = n > kTwoStageMin;
     if (const char* mode = std::getenv("BSE_TRIDIAG_MODE")) {
-        if (std::string(mode) == "shared") redundant = false;
-        else if (std::string(mode) == "redundant") redundant = true;
+        const std::string md(mode);
+        if (md == "shared") redundant = two_stage = false;
+        else if (md == "redundant") { redundant = true; two_stage = false; }
+        else if (md == "twostage") { redundant = false; two_stage = n >= 3; }
     }
-    const size_t nbuf = redundant ? (size_t)B : 2;
+    if (two_stage) redundant = false;
+    const size_t nbuf = two_stage ? 0 : (redundant ? (size_t)B : 2);
     const size_t o_v = carve(nbuf * n * sizeof(T2)), o_p = carve(nbuf * n * sizeof(T2));
-    const size_t o_pp = carve((size_t)nt_max * n * sizeof(T2)), o_dp = carve(2 * (size_t)B * sizeof(T2));
+    const size_t o_pp = carve(two_stage ? 0 : (size_t)nt_max * n * sizeof(T2)), o_dp = carve(2 * (size_t)B * sizeof(T2));
     const size_t o_y = carve((redundant ? (size_t)B : 1) * n * sizeof(T2)), o_bar = carve(64);
+    const bool fp64 = sizeof(T2) == sizeof(double2);
+    const size_t o_band = carve(two_stage ? band_workspace(n, fp64, n_vec > 0, n_vec, nsm) : 0);
     const size_t o_dd = carve(n * 8), o_ee = carve(n * 8), o_e2 = carve(n * 8), o_df = carve(n * 4), o_e2f = carve(n * 4);
     const size_t o_ef = carve(n * 4), o_cl = carve(n);
     const size_t o_y64 = carve(n * sizeof(double2));
@@ -964,9 +887,13 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     ta.y = y; ta.bar = bar; ta.err = err; ta.TR = TR; ta.redundant = redundant ? 1 : 0;
     void* kargs[] = {&ta};
     stage_begin(c, 8);
-    if ((st = cuda_check(c, cudaLaunchCooperativeKernel((void*)tridiag_kernel<T2>, dim3(B), dim3(threads), kargs, smem, c->stream),
-                         "tridiagonal kernel launch"))) return st;
-    c->launches++;
+    if (two_stage) {
+        if ((st = band_tridiag(c, n, A, lda, fp64, d, e, y, n_vec > 0, w + o_band, bar, err, n_vec))) return st;
+    } else {
+        if ((st = cuda_check(c, cudaLaunchCooperativeKernel((void*)tridiag_kernel<T2>, dim3(B), dim3(threads), kargs, smem,
+                                                            c->stream), "tridiagonal kernel launch"))) return st;
+        c->launches++;
+    }
     stage_end(c, 8);
     // T in FP64 / FP32 copies for the bisection and inverse iteration
     double* dd = (double*)(w + o_dd);
@@ -1074,9 +1001,16 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         T2* X = nullptr;
         if ((st = cuda_check(c, cudaMallocAsync((void**)&X, (size_t)n * n_vec * sizeof(T2), c->stream), "eigenvector buffer"))) return st;
         const int64_t nz = (int64_t)n * n_vec;
-        real_to_complex_kernel<T2><<<(unsigned)((nz + 255) / 256), 256, 0, c->stream>>>(nz, z, X);
-        c->launches++;
-        if (n > 1) {
+        if (two_stage) {
+            if ((st = band_backtransform(c, n, fp64, z, n_vec, X, w + o_band, bar, err))) {
+                cudaFreeAsync(X, c->stream);
+                return st;
+            }
+        } else {
+            real_to_complex_kernel<T2><<<(unsigned)((nz + 255) / 256), 256, 0, c->stream>>>(nz, z, X);
+            c->launches++;
+        }
+        if (n > 1 && !two_stage) {
             constexpr int CB = 4;
             const int npanel = (n - 1 + 31) / 32;
             T2* Tf = nullptr;
@@ -1090,6 +1024,11 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
                                              cudaMemcpyDeviceToDevice, c->stream), "eigenvectors");
         cudaFreeAsync(X, c->stream);
         if (st) return st;
+        if (two_stage) {
+            if ((st = cuda_check(c, cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "barrier status"))) return st;
+            if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "back-transformation"))) return st;
+            if (herr) return fail(c, BSE_ERR_NOT_CONVERGED, "back-transformation: a grid barrier timed out");
+        }
     }
     stage_end(c, 11);
     return cuda_check(c, cudaGetLastError(), "own eigensolver");

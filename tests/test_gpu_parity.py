@@ -161,11 +161,11 @@ def test_degenerate_spectrum_weights(synth, oracle, gpu, solver):
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
 
 
-@pytest.mark.parametrize("mode", ["shared", "redundant"])
+@pytest.mark.parametrize("mode", ["shared", "redundant", "twostage"])
 def test_tridiagonal_barrier_modes(synth, oracle, gpu, monkeypatch, mode):
-    """Both variants of the cooperative tridiagonal reduction (one grid barrier per reflector
-    with per-block copies, or two barriers with shared vectors -- the large-N path) give the
-    oracle's spectrum."""
+    """Every variant of the tridiagonal reduction (one-stage with one grid barrier per reflector
+    and per-block copies, or two barriers with shared vectors; the two-stage dense -> band ->
+    tridiagonal path of the largest matrices) gives the oracle's spectrum."""
     monkeypatch.setenv("BSE_TRIDIAG_MODE", mode)
     prob = synth.orb8_problem(grid=4)
     ref = oracle.solve(prob, OMEGA, GAMMA)
@@ -178,3 +178,67 @@ def test_tridiagonal_barrier_modes(synth, oracle, gpu, monkeypatch, mode):
         else:
             assert np.abs(E - ref["E"]).max() < tol
             assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
+
+
+@pytest.mark.parametrize("grid", [13, 7])
+def test_two_stage_vectors_ragged(synth, oracle, gpu, monkeypatch, grid):
+    """Two-stage reduction at orders that are not multiples of the band width (169, 49), FP64:
+    all eigenvalues, all back-transformed eigenvectors (orthonormal, A^H H A = diag(E)), eps2."""
+    monkeypatch.setenv("BSE_TRIDIAG_MODE", "twostage")
+    prob = synth.hbn_problem(grid=grid)
+    ref = oracle.solve(prob, OMEGA, GAMMA)
+    with gpu.BSEContext(prob, eig_solver=0) as ctx:
+        ctx.build_kernel()
+        E, A = ctx.diagonalize(want_vectors=True)
+        f = ctx.oscillators()
+        e2, _ = ctx.eps(OMEGA, GAMMA)
+    assert np.abs(E - ref["E"]).max() < 1e-8
+    assert np.abs(A.conj().T @ A - np.eye(A.shape[0])).max() < 1e-9
+    H = ref["H"]
+    assert np.abs(A.conj().T @ H @ A - np.diag(E)).max() < 1e-8 * np.abs(E).max()
+    assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
+
+
+def test_two_stage_degenerate_and_collinear(synth, oracle, gpu, monkeypatch):
+    """Two-stage reduction on exactly degenerate spectra (hBN IPA limit) and on the collinear
+    spin-block layout, FP64 and mixed precision with refinement."""
+    monkeypatch.setenv("BSE_TRIDIAG_MODE", "twostage")
+    prob = synth.hbn_problem(grid=12)
+    prob.params = prob.params.replace(ipa=1)
+    ref = oracle.solve(prob, OMEGA, GAMMA)
+    with gpu.BSEContext(prob, eig_solver=0) as ctx:
+        E, e2, _ = ctx.solve(OMEGA, GAMMA)
+    assert np.abs(E - ref["E"]).max() < 1e-10
+    assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
+    prob = synth.collinear_problem(grid=6)
+    ref = oracle.solve(prob, OMEGA, GAMMA)
+    for precision in (0, 1):
+        with gpu.BSEContext(prob, precision=precision, eig_solver=0, n_refine=64) as ctx:
+            E, e2, _ = ctx.solve(OMEGA, GAMMA)
+        if precision == 0:
+            assert np.abs(E - ref["E"]).max() < 1e-8
+            assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
+        else:
+            # the refinement covers the optically active block, the last n_opt eigenvalues
+            n_opt = len(ref["E_opt"])
+            assert np.abs(E[-n_opt:][:64] - ref["E_opt"][:64]).max() < 1e-6
+            assert np.abs(E - ref["E"]).max() < max(1e-5, 1e-6 * np.abs(ref["E"]).max())
+            assert np.linalg.norm(e2 - ref["eps2"]) < 1e-4 * np.linalg.norm(ref["eps2"])
+
+
+def test_two_stage_repeatable_mixed(synth, gpu, monkeypatch):
+    """The concurrent bulge chase gives bit-identical tridiagonals run after run and agrees with
+    the one-stage reduction to FP32 accuracy (N=2304: sweeps of 72 steps, ~24 running at once)."""
+    prob = synth.orb8_problem(grid=12)
+    monkeypatch.setenv("BSE_TRIDIAG_MODE", "shared")
+    with gpu.BSEContext(prob, precision=1, eig_solver=0, n_refine=0) as ctx:
+        E1, _, _ = ctx.solve(OMEGA, GAMMA)
+    monkeypatch.setenv("BSE_TRIDIAG_MODE", "twostage")
+    runs = []
+    for _ in range(3):
+        with gpu.BSEContext(prob, precision=1, eig_solver=0, n_refine=0) as ctx:
+            E, _, _ = ctx.solve(OMEGA, GAMMA)
+        runs.append(E)
+    for E in runs[1:]:
+        assert np.array_equal(E, runs[0])
+    assert np.abs(runs[0] - E1).max() < max(1e-5, 1e-6 * np.abs(E1).max())
