@@ -11,8 +11,10 @@ value  = device time per solve (CUDA events on the library's stream), inputs res
 e2e    = the same solve through the C ABI with host buffers: context creation (model
          upload), solve, copy-back of eigenvalues and eps, destroy -- wall clock
 Other keys: the plain FP64 GPU path (cuSOLVER zheevd) on the same problem, the max
-eigenvalue error of the mixed path against it, the roofline of the build kernel, the
-CPU oracle baseline and the SM clocks sampled during the timed region.
+eigenvalue error of the mixed path against it, the roofline of the dominant kernel (the
+tridiagonal reduction of the own eigensolver; the kernel build as a second figure), the
+eigensolve rate in the 14.7 N^3 flop unit, the CPU oracle baseline and the SM clocks
+sampled during the timed region.
 """
 from __future__ import annotations
 
@@ -192,7 +194,7 @@ def run_gpu(args):
     for _ in range(args.warmup):
         ctx.solve(OMEGA, GAMMA)
     ctx.reset_kernel_launches()
-    step_ms, build_ms, eig_ms = [], [], []
+    step_ms, build_ms, eig_ms, tri_ms = [], [], [], []
     _barrier(ws)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
@@ -205,6 +207,7 @@ def run_gpu(args):
         step_ms.append(st["solve"])
         build_ms.append(st["build"])
         eig_ms.append(st["eig"])
+        tri_ms.append(st["eig_tridiag"])
     torch.cuda.synchronize()
     host_s = time.perf_counter() - t_host0
     clk = clocks.stop()
@@ -244,12 +247,18 @@ def run_gpu(args):
     err_all = float(np.abs(E_mixed - E64).max())
     eps2_err = float(np.linalg.norm(e2_mixed - e2_64) / np.linalg.norm(e2_64))
 
-    # --- roofline of the build kernel (lower triangle, complex64 store) ---
+    # --- rooflines.  Dominant kernel (own solver): the one-stage tridiagonal reduction, which reads
+    # and rewrites the trailing (n-k-1)^2 block of full complex64 storage for every reflector k:
+    # 2 * 8 B * sum_m m^2 per launch.  The 42 MB matrix stays in L2 (ncu: 0.34 MB of DRAM traffic
+    # per launch), so the HBM denominator overstates what bounds it; the figure shows how far the
+    # latency-bound sweep is from streaming.  Second figure: the build kernel (HBM store of H). ---
     N = prob.n_bse
     nb = prob.model.nw * prob.model.n_spin
-    alg_bytes = N * (N + 1) // 2 * 8 + 16 * prob.nk * nb * (prob.params.nv + prob.params.nc)
+    build_bytes = N * N * 8 + 16 * prob.nk * nb * (prob.params.nv + prob.params.nc)   # full c64 store (own solver)
     build_avg_ms = float(np.mean(build_ms))
-    achieved = alg_bytes / (build_avg_ms * 1e-3) / 1e9
+    tri_bytes = 16 * (N - 1) * N * (2 * N - 1) // 6
+    tri_avg_ms = float(np.mean(tri_ms))
+    eig_avg_ms = float(np.mean(eig_ms))
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -283,6 +292,19 @@ def run_gpu(args):
                "sample": f"one full CPU solve of {WORKLOAD} (N_BSE={N}): C++ OpenMP restatement of the "
                          "reference loops + LAPACK zheevd (scipy)"}
 
+    build_gbs = build_bytes / (build_avg_ms * 1e-3) / 1e9
+    if args.solver == "own" and N <= 8192:
+        tri_gbs = tri_bytes / (tri_avg_ms * 1e-3) / 1e9
+        roof = {"kernel": "tridiag_kernel<float2>", "bound": "hbm", "achieved": tri_gbs, "peak": peak,
+                "peak_source": peak_src, "unit": "GB/s", "frac": tri_gbs / peak,
+                "traffic": 336491 if N == 2304 else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at N_BSE=2304 "
+                                  "(profiles/tridiag_kernel_magnetic4_24x24.md): the matrix is L2-resident",
+                "alg_bytes_per_launch": int(tri_bytes), "avg_launch_ms": tri_avg_ms}
+    else:
+        roof = {"kernel": "build_kernel<4,float>", "bound": "hbm", "achieved": build_gbs, "peak": peak,
+                "peak_source": peak_src, "unit": "GB/s", "frac": build_gbs / peak, "traffic": None,
+                "alg_bytes_per_launch": int(build_bytes), "avg_launch_ms": build_avg_ms}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "ms", "n_gpus": ws, "steps": args.steps,
@@ -295,9 +317,13 @@ def run_gpu(args):
                        "l2": "flushed between steps (256 MB write); H is 42 MB"},
             "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
-            "roofline": {"kernel": "build_kernel<8,float>", "bound": "hbm", "achieved": achieved, "peak": peak,
-                         "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "alg_bytes_per_launch": int(alg_bytes), "avg_launch_ms": build_avg_ms},
+            "roofline": roof,
+            "roofline_build": {"kernel": "build_kernel<4,float>", "bound": "hbm", "achieved": build_gbs, "peak": peak,
+                               "peak_source": peak_src, "unit": "GB/s", "frac": build_gbs / peak, "traffic": None,
+                               "alg_bytes_per_launch": int(build_bytes), "avg_launch_ms": build_avg_ms},
+            "eig_rate": {"unit": "TFLOP/s", "flop_per_solve": 14.7 * N ** 3, "eig_ms": eig_avg_ms,
+                         "value": 14.7 * N ** 3 / (eig_avg_ms * 1e-3) / 1e12,
+                         "note": "14.7 N^3 = zhetrd 16/3 + D&C 4/3 + zunmtr 8 (N^3 real flops), the LAPACK-equivalent count"},
             "stages_ms": stage,
             "eps2_grad_ms": grad_ms,
             "eps2_grad_config": "d(sum_s w_s eps2(w_s))/d(12 hopping/onsite, r0), FP64 forward + hand-written adjoint, N_BSE=2304",

@@ -404,17 +404,18 @@ __device__ __forceinline__ F tri_solve(int n, const F* __restrict__ Ur, const F*
     return mx;
 }
 
-// FP64 Rayleigh quotient z^T T z / z^T z of X (scaled by sx), with the squared norm.
-template <int RS, int PD>
+// FP64 Rayleigh quotient z^T T z / z^T z of X (FP32 or FP64 elements, scaled by sx), with the
+// squared norm.
+template <int RS, int PD, typename V>
 __device__ __forceinline__ double tri_rq(int n, const double* __restrict__ d, const double* __restrict__ e,
-                                         const double* __restrict__ X, double sx, double* den_out) {
-    double num = 0, den = 0, xprev = 0, x = X[0] * sx;
+                                         const V* __restrict__ X, double sx, double* den_out) {
+    double num = 0, den = 0, xprev = 0, x = (double)X[0] * sx;
     for (int k = 0; k < n; k++) {
         if (k + PD < n) {
             pf_l1(X + (size_t)(k + PD) * RS);
             pf_l1(d + k + PD);
         }
-        const double xn = (k + 1 < n) ? X[(size_t)(k + 1) * RS] * sx : 0.0;
+        const double xn = (k + 1 < n) ? (double)X[(size_t)(k + 1) * RS] * sx : 0.0;
         num += x * (d[k] * x + (k > 0 ? e[k - 1] * xprev : 0.0) + (k + 1 < n ? e[k] * xn : 0.0));
         den += x * x;
         xprev = x;
@@ -425,9 +426,11 @@ __device__ __forceinline__ double tri_rq(int n, const double* __restrict__ d, co
 }
 
 // Eigenpair (w_i, z_i) of T for an eigenvalue FP32 bisection separates from its neighbours:
-// three FP32 inverse iterations from the FP32 estimate, then two FP64 Rayleigh-quotient
-// iterations.  Writes w[i], f_i = sum_k conj(y_k) z_k, and z_i for i < n_store.  Cluster
-// members (cl[i] != 0) are left to cluster_kernel.
+// three FP32 inverse iterations from the FP32 estimate; with `fp64` two FP64 Rayleigh-quotient
+// iterations follow (the FP64 path), otherwise the eigenvalue is the FP64 Rayleigh quotient of
+// the FP32 vector (T itself carries FP32 rounding in the mixed path, so FP64 iterations on it
+// would not make the pair more accurate).  Writes w[i], f_i = sum_k conj(y_k) z_k, and z_i for
+// i < n_store.  Cluster members (cl[i] != 0) are left to the cluster kernels.
 template <typename TZ>
 __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restrict__ d, const double* __restrict__ e,
                                                    const float* __restrict__ df, const float* __restrict__ ef,
@@ -435,7 +438,7 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
                                                    int i0, int count, double tnorm, const double2* __restrict__ y,
                                                    double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz,
                                                    int n_store, double* __restrict__ scr, float* __restrict__ scr32,
-                                                   signed char* __restrict__ piv) {
+                                                   signed char* __restrict__ piv, int fp64) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
     const int i = i0 + t;
@@ -457,6 +460,26 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
         const float mx = tri_solve<float, 32, 32>(n, Ur, Ub, Ud, Lc, pv, Y, sc);
         sc = mx > 0 ? 1.0f / mx : 1.0f;
     }
+    const bool keep = i < n_store;
+    if (!fp64) {
+        double den = 1;
+        const double lam = tri_rq<32, 32>(n, d, e, Y, (double)sc, &den);
+        const double inv = (double)sc / sqrt(den);
+        w[i] = lam;
+        double fx = 0, fy = 0;
+        for (int k = 0; k < n; k++) {
+            if (k + 32 < n) pf_l1(Y + (size_t)(k + 32) * 32);
+            const double x = (double)Y[(size_t)k * 32] * inv;
+            if (f) {
+                const double2 yy = y[k];
+                fx += yy.x * x;
+                fy -= yy.y * x;
+            }
+            if (keep) z[(size_t)k + (size_t)i * ldz] = (TZ)x;
+        }
+        if (f) f[i] = make_double2(fx, fy);
+        return;
+    }
     double* Vr = scr + (size_t)blockIdx.x * 5 * W32 + lane;
     double* Vb = Vr + W32;
     double* Vd = Vb + W32;
@@ -475,7 +498,6 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
     const double inv = sx / sqrt(den);
     w[i] = lam;
     double fx = 0, fy = 0;
-    const bool keep = i < n_store;
     for (int k = 0; k < n; k++) {
         if (k + 16 < n) pf_l1(X + (size_t)(k + 16) * 32);
         const double x = X[(size_t)k * 32] * inv;
@@ -489,21 +511,23 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
     if (f) f[i] = make_double2(fx, fy);
 }
 
-// Eigenpairs of a run of eigenvalues FP32 bisection cannot separate (dstein-style): one warp
+// FP64 path: eigenpairs of a cluster (dstein-style), one warp
 // per cluster.  Member j gets FP64 inverse iteration with its own shift (lane 0 runs the
 // tridiagonal factor and solves) and Gram-Schmidt against the cluster's earlier members (all
 // lanes); then a Rayleigh-Ritz step inside the cluster (Jacobi on the c x c projected matrix)
-// gives FP64 eigenpairs.  Member vectors stay in Zc (column-major n x c per cluster).
+// gives FP64 eigenpairs.  Member vectors stay in Zc (column-major n x c per cluster).  Members
+// outside [cout[2t], cout[2t+1]) are guards: solved with the cluster, not written.
 __device__ __forceinline__ double warp_dsum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
 template <typename TZ>
-__global__ void __launch_bounds__(32) cluster_kernel(int n, const double* __restrict__ d, const double* __restrict__ e,
-                                                     double* __restrict__ w, const int* __restrict__ cstart,
-                                                     const int* __restrict__ csize, const int64_t* __restrict__ coff,
-                                                     int ncl, double tnorm, const double2* __restrict__ y,
+__global__ void __launch_bounds__(32) cluster64_kernel(int n, const double* __restrict__ d, const double* __restrict__ e,
+                                                       const double* __restrict__ w0, double* __restrict__ w,
+                                                       const int* __restrict__ cstart, const int* __restrict__ csize,
+                                                       const int* __restrict__ cout, const int64_t* __restrict__ coff,
+                                                       int ncl, double tnorm, const double2* __restrict__ y,
                                                      double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz, int n_store,
                                                      double* __restrict__ scr, signed char* __restrict__ piv,
                                                      double* __restrict__ Zall) {
@@ -521,7 +545,7 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const double* __rest
     const double pert = 2.220446049250313e-16 * fmax(tnorm, 1e-300);
     double sprev = -1e300;
     for (int j = 0; j < c; j++) {
-        const double shift = fmax(w[s0 + j], sprev + 10.0 * pert);
+        const double shift = fmax(w0[s0 + j], sprev + 10.0 * pert);
         sprev = shift;
         if (lane == 0) tri_factor<double, 1, 64>(n, d, e, shift, pert, Vr, Vb, Vd, Vc, pv);
         for (int k = lane; k < n; k += 32) X[k] = start_value(s0 + j, k) - 1.0;
@@ -610,6 +634,7 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const double* __rest
     __syncwarp();
     for (int a = 0; a < c; a++) {
         const int i = s0 + a, col = ord[a];
+        if (i < cout[2 * t] || i >= cout[2 * t + 1]) continue;   // guard member
         double fx = 0, fy = 0;
         for (int k = lane; k < n; k += 32) {
             double v = 0;
@@ -626,6 +651,283 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const double* __rest
             w[i] = M[col * (CMAX + 1)];
             if (f) f[i] = make_double2(fx, fy);
         }
+    }
+}
+
+// Mixed path: eigenpairs of runs of eigenvalues FP32 bisection cannot separate.  Several
+// clusters sit side by side on the lanes of one warp (a warp holds clusters of total size <= 32,
+// most runs are pairs); lane j of a cluster's segment runs inverse iteration for member j with its
+// own shift, the segment orthonormalises its member vectors after every iteration (Cholesky QR,
+// Gram matrix accumulated in FP64) so they cannot collapse onto the member nearest to a shift, and
+// a generalised Rayleigh-Ritz step inside the cluster (Jacobi on the c x c projected matrix, FP64)
+// gives the eigenpairs.  The iterations run in FP32, as the tridiagonal of the mixed path carries
+// FP32 rounding itself.  Members outside [cout[2t], cout[2t+1]) are guards, solved but not written.
+// Scratch: interleaved [k][32] arrays per warp.
+constexpr int CMAX = 32;
+
+// out[b][a] = sum_k u_b(k) z_a(k) over the columns z_a = X[k * 32 + a] of lane b's segment
+// [slo, slo + sc); lane b accumulates row b; u = z (Gram matrix) or u = T z (projected T).
+// FP32 partial sums over 16 rows go into FP64.
+template <typename F, bool APPLY_T>
+__device__ void cluster_gram(int n, int slo, int sc, const F* __restrict__ X, const F* __restrict__ d,
+                             const F* __restrict__ e, double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    double acc[CMAX];
+#pragma unroll
+    for (int a = 0; a < CMAX; a++) acc[a] = 0;
+    F zprev = 0;
+    for (int k0 = 0; k0 < n; k0 += 16) {
+        // the chunk's rows (and one row ahead for T z) are loaded before any is used, so the
+        // loads are in flight together instead of one dependent load per row
+        F zb[17], db[16], eb[17];
+#pragma unroll
+        for (int q = 0; q < 17; q++) {
+            const int k = k0 + q;
+            zb[q] = k < n ? X[(size_t)k * 32] : F(0);
+            if (APPLY_T) {
+                if (q < 16) db[q] = k < n ? d[k] : F(0);
+                eb[q] = k < n - 1 ? e[k] : F(0);
+            }
+        }
+        const F eprev = (APPLY_T && k0 > 0) ? e[k0 - 1] : F(0);
+        F part[CMAX];
+#pragma unroll
+        for (int a = 0; a < CMAX; a++) part[a] = 0;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const F zc = zb[q];
+            F u = zc;
+            if (APPLY_T) u = db[q] * zc + (q > 0 ? eb[q - 1] : eprev) * zprev + eb[q] * zb[q + 1];
+#pragma unroll
+            for (int a = 0; a < CMAX; a++) part[a] += u * __shfl_sync(0xffffffffu, zc, a);
+            zprev = zc;
+        }
+#pragma unroll
+        for (int a = 0; a < CMAX; a++) acc[a] += (double)part[a];
+    }
+#pragma unroll
+    for (int a = 0; a < CMAX; a++)
+        if (sc > 0 && a >= slo && a < slo + sc) out[lane * CMAX + a] = acc[a];
+    __syncwarp();
+}
+
+// Cholesky G = R^T R in place (R upper, row-major, row stride CMAX); a pivot below 1e-10 of its
+// diagonal entry (a column numerically inside the span of the earlier ones) is raised to that
+// level, so the column comes out short instead of blowing up and the next iteration refills it.
+__device__ void chol_upper(int c, double* G) {
+    for (int j = 0; j < c; j++) {
+        const double g0 = G[j * CMAX + j];
+        double djj = g0;
+        for (int q = 0; q < j; q++) djj -= G[q * CMAX + j] * G[q * CMAX + j];
+        djj = sqrt(fmax(djj, 1e-10 * fmax(g0, 1e-300)));
+        G[j * CMAX + j] = djj;
+        for (int b = j + 1; b < c; b++) {
+            double v = G[j * CMAX + b];
+            for (int q = 0; q < j; q++) v -= G[q * CMAX + j] * G[q * CMAX + b];
+            G[j * CMAX + b] = v / djj;
+        }
+    }
+}
+
+// Rinv = R^{-1} (upper), row-major.
+__device__ void inv_upper(int c, const double* R, double* Rinv) {
+    for (int jc = 0; jc < c; jc++) {
+        for (int r = jc; r >= 0; r--) {
+            double v = r == jc ? 1.0 : 0.0;
+            for (int q = r + 1; q <= jc; q++) v -= R[r * CMAX + q] * Rinv[q * CMAX + jc];
+            Rinv[r * CMAX + jc] = v / R[r * CMAX + r];
+        }
+        for (int r = jc + 1; r < c; r++) Rinv[r * CMAX + jc] = 0;
+    }
+}
+
+// Orthonormalise each segment's columns X[k * 32 + lane]: X <- X R^{-1} with G = R^T R, the
+// segment's first lane factoring its diagonal block.
+template <typename F>
+__device__ void cluster_cholqr(int n, int slo, int sc, F* __restrict__ X, double* __restrict__ Gs,
+                               double* __restrict__ Rinv) {
+    const int lane = threadIdx.x & 31;
+    cluster_gram<F, false>(n, slo, sc, X, (const F*)nullptr, (const F*)nullptr, Gs);
+    if (sc > 0 && lane == slo) {
+        chol_upper(sc, Gs + slo * (CMAX + 1));
+        inv_upper(sc, Gs + slo * (CMAX + 1), Rinv + slo * (CMAX + 1));
+    }
+    __syncwarp();
+    F rcol[CMAX];
+#pragma unroll
+    for (int a = 0; a < CMAX; a++) rcol[a] = (sc > 0 && a >= slo && a <= lane) ? (F)Rinv[a * CMAX + lane] : F(0);
+    for (int k0 = 0; k0 < n; k0 += 16) {
+        F xb[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) xb[q] = k0 + q < n ? X[(size_t)(k0 + q) * 32] : F(0);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            F v = 0;
+#pragma unroll
+            for (int a = 0; a < CMAX; a++) v += __shfl_sync(0xffffffffu, xb[q], a) * rcol[a];
+            if (sc > 0 && k0 + q < n) X[(size_t)(k0 + q) * 32] = v;
+        }
+    }
+    __syncwarp();
+}
+
+// Rayleigh-Ritz inside a cluster (one lane): M q = theta S q with S = Gs = Z^T Z = R^T R, Jacobi
+// on R^{-T} M R^{-1}; on return M's diagonal holds theta, Q (column-major) the coefficient vectors
+// R^{-1} q', ord the ascending order.  Gs and Rinv are overwritten.  All arrays relative to the
+// block's top-left corner, row stride CMAX.
+__device__ void cluster_rr(int c, double* Gs, double* Rinv, double* M, double* Q, int* ord) {
+    for (int a = 0; a < c; a++)
+        for (int b = 0; b < a; b++) M[a * CMAX + b] = M[b * CMAX + a] = 0.5 * (M[a * CMAX + b] + M[b * CMAX + a]);
+    chol_upper(c, Gs);
+    inv_upper(c, Gs, Rinv);
+    for (int a = 0; a < c; a++)            // Q = M Rinv (row-major scratch)
+        for (int b = 0; b < c; b++) {
+            double v = 0;
+            for (int q = 0; q <= b; q++) v += M[a * CMAX + q] * Rinv[q * CMAX + b];
+            Q[a * CMAX + b] = v;
+        }
+    for (int a = 0; a < c; a++)            // M = Rinv^T Q (column-major from here on)
+        for (int b = 0; b < c; b++) {
+            double v = 0;
+            for (int q = 0; q <= a; q++) v += Rinv[q * CMAX + a] * Q[q * CMAX + b];
+            M[a + b * CMAX] = v;
+        }
+    for (int a = 0; a < c; a++)
+        for (int b = 0; b < a; b++) M[a + b * CMAX] = M[b + a * CMAX] = 0.5 * (M[a + b * CMAX] + M[b + a * CMAX]);
+    for (int a = 0; a < c; a++)
+        for (int b = 0; b < c; b++) Q[a + b * CMAX] = a == b ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 30; sweep++) {
+        double off = 0;
+        for (int a = 0; a < c; a++)
+            for (int b = a + 1; b < c; b++) off += M[a + b * CMAX] * M[a + b * CMAX];
+        if (off < 1e-60) break;
+        for (int p = 0; p < c; p++)
+            for (int q = p + 1; q < c; q++) {
+                const double apq = M[p + q * CMAX];
+                if (apq == 0.0) continue;
+                const double tau = (M[q + q * CMAX] - M[p + p * CMAX]) / (2.0 * apq);
+                const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                const double cs = 1.0 / sqrt(1.0 + tt * tt), sn = tt * cs;
+                for (int k = 0; k < c; k++) {
+                    const double mkp = M[k + p * CMAX], mkq = M[k + q * CMAX];
+                    M[k + p * CMAX] = cs * mkp - sn * mkq;
+                    M[k + q * CMAX] = sn * mkp + cs * mkq;
+                }
+                for (int k = 0; k < c; k++) {
+                    const double mpk = M[p + k * CMAX], mqk = M[q + k * CMAX];
+                    M[p + k * CMAX] = cs * mpk - sn * mqk;
+                    M[q + k * CMAX] = sn * mpk + cs * mqk;
+                }
+                for (int k = 0; k < c; k++) {
+                    const double qkp = Q[k + p * CMAX], qkq = Q[k + q * CMAX];
+                    Q[k + p * CMAX] = cs * qkp - sn * qkq;
+                    Q[k + q * CMAX] = sn * qkp + cs * qkq;
+                }
+            }
+    }
+    for (int a = 0; a < c; a++)            // Q <- Rinv Q
+        for (int b = 0; b < c; b++) {
+            double v = 0;
+            for (int q = a; q < c; q++) v += Rinv[a * CMAX + q] * Q[q + b * CMAX];
+            Gs[a + b * CMAX] = v;
+        }
+    for (int a = 0; a < c; a++)
+        for (int b = 0; b < c; b++) Q[a + b * CMAX] = Gs[a + b * CMAX];
+    for (int a = 0; a < c; a++) ord[a] = a;
+    for (int a = 1; a < c; a++) {
+        const int x = ord[a];
+        int b = a - 1;
+        while (b >= 0 && M[ord[b] * (CMAX + 1)] > M[x * (CMAX + 1)]) { ord[b + 1] = ord[b]; b--; }
+        ord[b + 1] = x;
+    }
+}
+
+template <typename TZ>
+__global__ void __launch_bounds__(32) cluster_kernel(int n, const float* __restrict__ df, const float* __restrict__ ef,
+                                                     const double* __restrict__ w0, double* __restrict__ w,
+                                                     const int* __restrict__ cstart, const int* __restrict__ csize,
+                                                     const int* __restrict__ cout, const int* __restrict__ wfirst,
+                                                     int wbase, double tnorm, const double2* __restrict__ y,
+                                                     double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz,
+                                                     int n_store, float* __restrict__ scr32, signed char* __restrict__ piv) {
+    __shared__ double Gs[CMAX * CMAX], Rinv[CMAX * CMAX], M[CMAX * CMAX], Q[CMAX * CMAX];
+    __shared__ int ord[CMAX];
+    const int lane = threadIdx.x;
+    // this warp's clusters sit side by side on the lanes; find this lane's cluster and segment
+    const int t_end = wfirst[wbase + blockIdx.x + 1];
+    int t = -1, slo = 0, sc = 0;
+    for (int q = wfirst[wbase + blockIdx.x], off = 0; q < t_end; q++) {
+        const int cq = csize[q];
+        if (lane >= off && lane < off + cq) {
+            t = q;
+            slo = off;
+            sc = cq;
+        }
+        off += cq;
+    }
+    const bool act = t >= 0;
+    const int s0 = act ? cstart[t] : 0, m = lane - slo;
+    const size_t W32 = (size_t)n * 32;
+    float* Ur = scr32 + (size_t)blockIdx.x * 5 * W32 + lane;
+    float* Ub = Ur + W32;
+    float* Ud = Ub + W32;
+    float* Lc = Ud + W32;
+    float* Y = Lc + W32;
+    signed char* pv = piv + (size_t)blockIdx.x * W32 + lane;
+    const float pert32 = 1.1920929e-7f * (float)fmax(tnorm, 1e-30);
+    const double pert = 2.220446049250313e-16 * fmax(tnorm, 1e-300);
+    // shifts: the FP32 estimates in increasing order within each cluster (distinct start vectors
+    // and the orthonormalisation keep the members apart, so the shifts may coincide)
+    double sh = act ? w0[s0 + m] : 0.0;
+    for (int j = 1; j < 32; j++) {
+        const double prev = __shfl_sync(0xffffffffu, sh, j - 1);
+        if (lane == j && act && m > 0) sh = fmax(sh, prev + 10.0 * pert);
+    }
+    if (act) tri_factor<float, 32, 32>(n, df, ef, (float)sh, pert32, Ur, Ub, Ud, Lc, pv);
+    for (int k = 0; k < n; k++) Y[(size_t)k * 32] = act ? (float)start_value(s0 + m, k) - 1.0f : 0.0f;
+    __syncwarp();
+    for (int it = 0; it < 3; it++) {
+        if (act) tri_solve<float, 32, 32>(n, Ur, Ub, Ud, Lc, pv, Y, 1.0f);
+        __syncwarp();
+        cluster_cholqr<float>(n, slo, sc, Y, Gs, Rinv);
+    }
+    cluster_gram<float, false>(n, slo, sc, Y, df, ef, Gs);
+    cluster_gram<float, true>(n, slo, sc, Y, df, ef, M);
+    const int blk = slo * (CMAX + 1);
+    if (act && lane == slo) cluster_rr(sc, Gs + blk, Rinv + blk, M + blk, Q + blk, ord + slo);
+    __syncwarp();
+    // member m (lane slo + m) = Z Q[:, ord[m]] of its segment; f = y^H z
+    double qcol[CMAX];
+    const int col = act ? slo + ord[slo + m] : 0;
+#pragma unroll
+    for (int b = 0; b < CMAX; b++) qcol[b] = (act && b >= slo && b < slo + sc) ? Q[b + col * CMAX] : 0.0;
+    const int i = s0 + m;
+    const bool outp = act && i >= cout[2 * t] && i < cout[2 * t + 1];
+    const bool keep = outp && i < n_store;
+    double fx = 0, fy = 0;
+    for (int k0 = 0; k0 < n; k0 += 16) {
+        float yb[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) yb[q] = k0 + q < n ? Y[(size_t)(k0 + q) * 32] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int k = k0 + q;
+            double v = 0;
+#pragma unroll
+            for (int b = 0; b < CMAX; b++) v += (double)__shfl_sync(0xffffffffu, yb[q], b) * qcol[b];
+            if (k < n) {
+                if (y && outp) {
+                    const double2 yy = y[k];
+                    fx += yy.x * v;
+                    fy -= yy.y * v;
+                }
+                if (keep) z[(size_t)k + (size_t)i * ldz] = (TZ)v;
+            }
+        }
+    }
+    if (outp) {
+        w[i] = M[col * (CMAX + 1)];
+        if (f) f[i] = make_double2(fx, fy);
     }
 }
 
@@ -936,20 +1238,36 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     stage_end(c, 9);
     const double ctol = 16.0 * 1.1920929e-7 * tnorm;
     std::vector<signed char> hcl(n, 0);
-    std::vector<int> cs, cz;
-    std::vector<int64_t> co;
-    int64_t ctot = 0;
+    std::vector<int> cs, cz, co;
+    // runs of eigenvalues closer than ctol, cut into chunks of at most kChunk outputs at the widest
+    // gap (never inside a degenerate group); each chunk is solved together with up to kGuardMembers
+    // neighbours per side (within 10 ctol), so that a cut through a run, or a close neighbour
+    // outside it, cannot pull a member's Ritz pair over
+    constexpr int kChunk = 24, kGuardMembers = 4;
     for (int i = 0; i < n;) {
-        int j = i;
-        while (j + 1 < n && hw[j + 1] - hw[j] <= ctol && j + 1 - i < 32) j++;
-        if (j > i) {
-            cs.push_back(i);
-            cz.push_back(j - i + 1);
-            co.push_back(ctot);
-            ctot += (int64_t)(j - i + 1) * n;
-            for (int q = i; q <= j; q++) hcl[q] = 1;
+        int g1 = i;
+        while (g1 + 1 < n && hw[g1 + 1] - hw[g1] <= ctol) g1++;
+        if (g1 == i) {
+            i++;
+            continue;
         }
-        i = j + 1;
+        for (int a = i, b = i; a <= g1; a = b + 1) {
+            b = g1;
+            if (g1 - a + 1 > kChunk) {
+                b = a + kChunk / 2 - 1;
+                for (int q = b + 1; q <= a + kChunk - 1; q++)
+                    if (hw[q + 1] - hw[q] > hw[b + 1] - hw[b]) b = q;
+            }
+            int lo = a, hi = b;
+            while (lo > 0 && a - lo < kGuardMembers && hw[a] - hw[lo - 1] <= 10.0 * ctol) lo--;
+            while (hi + 1 < n && hi - b < kGuardMembers && hw[hi + 1] - hw[b] <= 10.0 * ctol) hi++;
+            cs.push_back(lo);
+            cz.push_back(hi - lo + 1);
+            co.push_back(a);
+            co.push_back(b + 1);
+            for (int q = a; q <= b; q++) hcl[q] = 1;
+        }
+        i = g1 + 1;
     }
     const int ncl = (int)cs.size();
     c->last_clusters = ncl;
@@ -966,33 +1284,76 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         const int cnt = std::min(count_max, n - i0);
         invit_kernel<R><<<(cnt + 31) / 32, 32, 0, c->stream>>>(n, dd, ee, df, ef, dW, cl, i0, cnt, tnorm, y64, f_out, z, n,
                                                                  n_vec, (double*)(w + o_scr), (float*)(w + o_scr32),
-                                                                 (signed char*)(w + o_piv));
+                                                                 (signed char*)(w + o_piv), fp64 ? 1 : 0);
         c->launches++;
     }
     stage_end(c, 10);
     if (ncl > 0) {
-        // the batch scratch is free again once the batches above are done (same stream)
+        // the inverse-iteration scratch is free again (same stream)
         int* dcs = nullptr;
         int* dcz = nullptr;
-        int64_t* dco = nullptr;
-        double* Zall = nullptr;
-        double* cscr = nullptr;
-        signed char* cpiv = nullptr;
+        int* dco = nullptr;
+        double* w0 = nullptr;
         if ((st = cuda_check(c, cudaMallocAsync((void**)&dcs, ncl * sizeof(int), c->stream), "clusters"))) return st;
         if ((st = cuda_check(c, cudaMallocAsync((void**)&dcz, ncl * sizeof(int), c->stream), "clusters"))) return st;
-        if ((st = cuda_check(c, cudaMallocAsync((void**)&dco, ncl * sizeof(int64_t), c->stream), "clusters"))) return st;
-        if ((st = cuda_check(c, cudaMallocAsync((void**)&Zall, (size_t)ctot * 8, c->stream), "cluster vectors"))) return st;
-        if ((st = cuda_check(c, cudaMallocAsync((void**)&cscr, 5 * (size_t)n * ncl * 8, c->stream), "cluster scratch"))) return st;
-        if ((st = cuda_check(c, cudaMallocAsync((void**)&cpiv, (size_t)n * ncl, c->stream), "cluster pivots"))) return st;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&dco, 2 * ncl * sizeof(int), c->stream), "clusters"))) return st;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&w0, n * sizeof(double), c->stream), "cluster shifts"))) return st;
         cudaMemcpyAsync(dcs, cs.data(), ncl * sizeof(int), cudaMemcpyHostToDevice, c->stream);
         cudaMemcpyAsync(dcz, cz.data(), ncl * sizeof(int), cudaMemcpyHostToDevice, c->stream);
-        cudaMemcpyAsync(dco, co.data(), ncl * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(dco, co.data(), 2 * ncl * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+        // shifts come from a snapshot: clusters overwrite the eigenvalues of their outputs, which
+        // other clusters read as guards
+        cudaMemcpyAsync(w0, dW, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
         stage_begin(c, 12);
-        cluster_kernel<R><<<ncl, 32, 0, c->stream>>>(n, dd, ee, dW, dcs, dcz, dco, ncl, tnorm, y64, f_out, z, n, n_vec, cscr,
-                                                      cpiv, Zall);
+        if (fp64) {
+            // FP64 path: per-member FP64 inverse iteration with Gram-Schmidt, then Rayleigh-Ritz;
+            // member vectors in Zc (n x c per cluster)
+            std::vector<int64_t> hco(ncl);
+            int64_t ctot = 0;
+            for (int q = 0; q < ncl; q++) {
+                hco[q] = ctot;
+                ctot += (int64_t)cz[q] * n;
+            }
+            int64_t* dcoff = nullptr;
+            double* Zall = nullptr;
+            double* cscr = nullptr;
+            signed char* cpiv = nullptr;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&dcoff, ncl * sizeof(int64_t), c->stream), "clusters"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&Zall, (size_t)ctot * 8, c->stream), "cluster vectors"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&cscr, 5 * (size_t)n * ncl * 8, c->stream), "cluster scratch"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&cpiv, (size_t)n * ncl, c->stream), "cluster pivots"))) return st;
+            cudaMemcpyAsync(dcoff, hco.data(), ncl * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream);
+            cluster64_kernel<R><<<ncl, 32, 0, c->stream>>>(n, dd, ee, w0, dW, dcs, dcz, dco, dcoff, ncl, tnorm, y64, f_out, z, n,
+                                                             n_vec, cscr, cpiv, Zall);
+            c->launches++;
+            for (void* p : {(void*)dcoff, (void*)Zall, (void*)cscr, (void*)cpiv}) cudaFreeAsync(p, c->stream);
+        } else {
+            // mixed path: clusters packed side by side into warps of 32 lanes, in batches of as
+            // many warps as the interleaved scratch holds
+            std::vector<int> wfirst(1, 0);
+            for (int q = 0, used = 0; q < ncl; q++) {
+                if (used + cz[q] > 32) {
+                    wfirst.push_back(q);
+                    used = 0;
+                }
+                used += cz[q];
+            }
+            wfirst.push_back(ncl);
+            const int nwarps = (int)wfirst.size() - 1;
+            const int wmax = (int)(cpad / 32);
+            int* dwf = nullptr;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&dwf, wfirst.size() * sizeof(int), c->stream), "cluster warps"))) return st;
+            cudaMemcpyAsync(dwf, wfirst.data(), wfirst.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+            for (int wb = 0; wb < nwarps; wb += wmax) {
+                const int nb = std::min(wmax, nwarps - wb);
+                cluster_kernel<R><<<nb, 32, 0, c->stream>>>(n, df, ef, w0, dW, dcs, dcz, dco, dwf, wb, tnorm, y64, f_out, z, n,
+                                                            n_vec, (float*)(w + o_scr32), (signed char*)(w + o_piv));
+                c->launches++;
+            }
+            cudaFreeAsync(dwf, c->stream);
+        }
         stage_end(c, 12);
-        c->launches++;
-        for (void* p : {(void*)dcs, (void*)dcz, (void*)dco, (void*)Zall, (void*)cscr, (void*)cpiv}) cudaFreeAsync(p, c->stream);
+        for (void* p : {(void*)dcs, (void*)dcz, (void*)dco, (void*)w0}) cudaFreeAsync(p, c->stream);
     }
     stage_begin(c, 11);
     if ((st = cuda_check(c, cudaGetLastError(), "bisection / inverse iteration"))) return st;
