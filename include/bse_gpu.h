@@ -170,7 +170,8 @@ int bse_solve_many(bse_ctx** ctxs, int32_t n_ctx, const double* omega, int32_t n
  * [0] bands, [1] tables, [2] build, [3] eigensolve, [4] refinement, [5] oscillators, [6] eps,
  * [7] the whole of the last bse_solve; with BSE_EIG_OWN, the eigensolve's parts: [8] tridiagonal
  * reduction, [9] eigenvalues, [10] inverse iteration, [11] back-transformation, [12] clusters
- * resolved in FP64 (bse_stage_times resets unrecorded stages to 0). */
+ * (runs of eigenvalues FP32 bisection cannot separate, solved together) (bse_stage_times resets
+ * unrecorded stages to 0). */
 int bse_stage_times(const bse_ctx* ctx, double* ms, int32_t n);
 
 /* Allocation-free dielectric function (no counterpart in the reference).  For callers that
@@ -190,7 +191,7 @@ int bse_eps_noalloc(int64_t n_exc, const double* e, const double* f, double pref
                     double* eps2, double* eps1, void* stream);
 
 /* Diagnostics of the last solve: [0] max FP64 residual ||H x - theta x||_2 (eV) over the refined
- * eigenpairs (an eigenvalue error bound), [1] eigenvalue clusters the own solver resolved in FP64,
+ * eigenpairs (an eigenvalue error bound), [1] eigenvalue clusters the own solver solved together,
  * [2] refined eigenpairs, [3] eigenvector columns formed. */
 int bse_diagnostics(const bse_ctx* ctx, double* out, int32_t n);
 
