@@ -404,6 +404,195 @@ __device__ __forceinline__ F tri_solve(int n, const F* __restrict__ Ur, const F*
     return mx;
 }
 
+
+// Staged FP32 sweeps for the inverse iterations.  The dependent row recurrences of the LU factor
+// and the two triangular solves run one warp per SM (one lane per eigenvalue); with operands read
+// from global memory row by row each step waits for a load (long-scoreboard stalls dominated).  Here
+// the warp copies chunks of SCH rows of its interleaved [k][32] arrays into shared memory with
+// cp.async, SNS chunks ahead, so every step reads shared memory.  All 32 lanes must call these.
+constexpr int SCH = 32;                                  // rows per staged chunk
+constexpr int SNS = 4;                                   // chunks in flight
+constexpr int SRW = SCH * 32;                            // elements of one array in one chunk
+constexpr size_t kStageSmem = (size_t)SNS * 4 * SRW * sizeof(float) + (size_t)SNS * SRW;   // 68 KB
+
+__device__ __forceinline__ void cp16(void* sdst, const void* gsrc) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// rows [r0, r1) of an interleaved array (32 elements of esz bytes per row) -> dst
+__device__ __forceinline__ void stage_rows(void* dst, const void* base, int r0, int r1, int esz) {
+    const int lane = threadIdx.x & 31;
+    const int bytes = (r1 - r0) * 32 * esz;
+    const char* src = (const char*)base + (size_t)r0 * 32 * esz;
+    for (int q = lane * 16; q < bytes; q += 32 * 16) cp16((char*)dst + q, src + q);
+}
+// rows [r0, r1) of a plain array of floats (one value per row, shared by the lanes) -> dst
+__device__ __forceinline__ void stage_vec(float* dst, const float* base, int r0, int r1) {
+    const int lane = threadIdx.x & 31;
+    // 16-byte pieces covering [r0, r1) rounded out to multiples of 4 floats (the arrays are
+    // allocated with 8 floats of padding)
+    const int a0 = r0 & ~3, a1 = (r1 + 3) & ~3;
+    for (int q = a0 + lane * 4; q < a1; q += 32 * 4) cp16(dst + (q - a0), base + q);
+}
+
+// LU of T - s I (as tri_factor), d/e staged; U/L written to the warp's interleaved arrays
+// (warp base pointers: element k of lane l at p[k * 32 + l]).
+__device__ void tri_factor_staged(int n, const float* __restrict__ d, const float* __restrict__ e, float s, float pert,
+                                  float* __restrict__ Urw, float* __restrict__ Ubw, float* __restrict__ Udw,
+                                  float* __restrict__ Lcw, signed char* __restrict__ pvw, float* sm) {
+    const int lane = threadIdx.x & 31;
+    // stage ch: d and e rows [ch*SCH, ch*SCH + SCH] (one row of lookahead), 16-byte pieces
+    constexpr int VW = SCH + 8;
+    const int nch = (n + SCH - 1) / SCH;
+    auto issue = [&](int ch) {
+        if (ch < nch) {
+            // rows k in [r0, rk1) read d[k + 1], e[k] and e[k + 1]
+            const int st = ch % SNS, r0 = ch * SCH, rk1 = min(n - 1, r0 + SCH);
+            stage_vec(sm + (st * 2) * VW, d, r0, min(n, rk1 + 1));
+            stage_vec(sm + (st * 2 + 1) * VW, e, r0, min(n - 1, rk1 + 1));
+        }
+        cp_commit();
+    };
+    for (int ch = 0; ch < SNS - 1; ch++) issue(ch);
+    float ak = 0, bk = 0;
+    for (int ch = 0; ch < nch; ch++) {
+        issue(ch + SNS - 1);
+        cp_wait<SNS - 1>();
+        __syncwarp();
+        const int st = ch % SNS, r0 = ch * SCH, r1 = min(n - 1, r0 + SCH);
+        const float* sd = sm + (st * 2) * VW;
+        const float* se = sm + (st * 2 + 1) * VW;
+        const int off = r0 & 3;                  // stage_vec starts at r0 rounded down to 4
+        if (ch == 0) {
+            ak = sd[off] - s;
+            bk = n > 1 ? se[off] : 0.0f;
+        }
+        for (int k = r0; k < r1; k++) {
+            const int q = k - r0 + off;
+            const float ck = se[q];
+            const float anext = sd[q + 1] - s;
+            const float bnext = (k + 1 < n - 1) ? se[q + 1] : 0.0f;
+            if (fabsf(ck) <= fabsf(ak)) {
+                const float u = fabsf(ak) < pert ? (ak < 0 ? -pert : pert) : ak;
+                const float r = 1.0f / u;
+                const float mult = ck * r;
+                Urw[(size_t)k * 32 + lane] = r;
+                Ubw[(size_t)k * 32 + lane] = bk;
+                Udw[(size_t)k * 32 + lane] = 0.0f;
+                Lcw[(size_t)k * 32 + lane] = mult;
+                pvw[(size_t)k * 32 + lane] = 0;
+                ak = anext - mult * bk;
+                bk = bnext;
+            } else {
+                const float r = 1.0f / ck;
+                const float mult = ak * r;
+                Urw[(size_t)k * 32 + lane] = r;
+                Ubw[(size_t)k * 32 + lane] = anext;
+                Udw[(size_t)k * 32 + lane] = bnext;
+                Lcw[(size_t)k * 32 + lane] = mult;
+                pvw[(size_t)k * 32 + lane] = 1;
+                ak = bk - mult * anext;
+                bk = -mult * bnext;
+            }
+        }
+        __syncwarp();
+    }
+    cp_wait<0>();
+    const float u = fabsf(ak) < pert ? (ak < 0 ? -pert : pert) : ak;
+    Urw[(size_t)(n - 1) * 32 + lane] = 1.0f / u;
+    __threadfence();
+    __syncwarp();
+}
+
+// (T - s I) x = y in place on the warp's Y (input scaled by sin); returns max |x| of this lane.
+__device__ float tri_solve_staged(int n, const float* __restrict__ Urw, const float* __restrict__ Ubw,
+                                  const float* __restrict__ Udw, const float* __restrict__ Lcw,
+                                  const signed char* __restrict__ pvw, float* __restrict__ Yw, float sin, float* sm) {
+    const int lane = threadIdx.x & 31;
+    signed char* smp = reinterpret_cast<signed char*>(sm + SNS * 4 * SRW);
+    float ycur = Yw[lane] * sin;
+    // forward elimination, rows k = 0 .. n-2: Lc[k], piv[k], Y[k+1]
+    const int nf = n - 1, nchf = (nf + SCH - 1) / SCH;
+    auto issue_f = [&](int ch) {
+        if (ch < nchf) {
+            const int st = ch % SNS, r0 = ch * SCH, r1 = min(nf, r0 + SCH);
+            stage_rows(sm + (st * 4 + 0) * SRW, Lcw, r0, r1, 4);
+            stage_rows(sm + (st * 4 + 1) * SRW, Yw + 32, r0, r1, 4);
+            stage_rows(smp + st * SRW, pvw, r0, r1, 1);
+        }
+        cp_commit();
+    };
+    for (int ch = 0; ch < SNS - 1; ch++) issue_f(ch);
+    for (int ch = 0; ch < nchf; ch++) {
+        issue_f(ch + SNS - 1);
+        cp_wait<SNS - 1>();
+        __syncwarp();
+        const int st = ch % SNS, r0 = ch * SCH, r1 = min(nf, r0 + SCH);
+        const float* sL = sm + (st * 4 + 0) * SRW;
+        const float* sY = sm + (st * 4 + 1) * SRW;
+        const signed char* sP = smp + st * SRW;
+        for (int k = r0; k < r1; k++) {
+            const int q = (k - r0) * 32 + lane;
+            const float mult = sL[q];
+            const float ynext = sY[q] * sin;
+            float out;
+            if (sP[q] == 0) {
+                out = ycur;
+                ycur = ynext - mult * ycur;
+            } else {
+                out = ynext;
+                ycur = ycur - mult * ynext;
+            }
+            Yw[(size_t)k * 32 + lane] = out;
+        }
+        __syncwarp();
+    }
+    cp_wait<0>();
+    __threadfence();
+    __syncwarp();
+    // back substitution: x_{n-1} = ycur Ur[n-1]; rows k = n-2 .. 0: Y[k], Ub[k], Ud[k], Ur[k]
+    float x1 = ycur * Urw[(size_t)(n - 1) * 32 + lane], x2 = 0.0f, mx = fabsf(x1);
+    Yw[(size_t)(n - 1) * 32 + lane] = x1;
+    const int nb = n - 1, nchb = (nb + SCH - 1) / SCH;
+    auto issue_b = [&](int ch) {
+        if (ch < nchb) {
+            const int st = ch % SNS, r1 = nb - ch * SCH, r0 = max(0, r1 - SCH);
+            stage_rows(sm + (st * 4 + 0) * SRW, Urw, r0, r1, 4);
+            stage_rows(sm + (st * 4 + 1) * SRW, Ubw, r0, r1, 4);
+            stage_rows(sm + (st * 4 + 2) * SRW, Udw, r0, r1, 4);
+            stage_rows(sm + (st * 4 + 3) * SRW, Yw, r0, r1, 4);
+        }
+        cp_commit();
+    };
+    for (int ch = 0; ch < SNS - 1; ch++) issue_b(ch);
+    for (int ch = 0; ch < nchb; ch++) {
+        issue_b(ch + SNS - 1);
+        cp_wait<SNS - 1>();
+        __syncwarp();
+        const int st = ch % SNS, r1 = nb - ch * SCH, r0 = max(0, r1 - SCH);
+        const float* sR = sm + (st * 4 + 0) * SRW;
+        const float* sB = sm + (st * 4 + 1) * SRW;
+        const float* sD = sm + (st * 4 + 2) * SRW;
+        const float* sY = sm + (st * 4 + 3) * SRW;
+        for (int k = r1 - 1; k >= r0; k--) {
+            const int q = (k - r0) * 32 + lane;
+            const float x = (sY[q] - sB[q] * x1 - sD[q] * x2) * sR[q];
+            Yw[(size_t)k * 32 + lane] = x;
+            x2 = x1;
+            x1 = x;
+            mx = fmaxf(mx, fabsf(x));
+        }
+        __syncwarp();
+    }
+    cp_wait<0>();
+    __threadfence();
+    __syncwarp();
+    return mx;
+}
+
 // FP64 Rayleigh quotient z^T T z / z^T z of X (FP32 or FP64 elements, scaled by sx), with the
 // squared norm.
 template <int RS, int PD, typename V>
@@ -439,27 +628,34 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
                                                    double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz,
                                                    int n_store, double* __restrict__ scr, float* __restrict__ scr32,
                                                    signed char* __restrict__ piv, int fp64) {
+    extern __shared__ float stage_sm[];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= count) return;
     const int i = i0 + t;
-    if (cl[i]) return;
+    // lanes past the batch or on cluster members run the sweeps on a dummy right-hand side (the
+    // staged sweeps need the whole warp) and write nothing
+    const bool act = t < count && !cl[i];
     // this warp's scratch: [array][k][32 lanes], one 128-byte line per row in FP32
     const size_t W32 = (size_t)n * 32;
     const size_t lane = threadIdx.x & 31;
-    const double lam0 = w[i];
-    float* Ur = scr32 + (size_t)blockIdx.x * 5 * W32 + lane;
-    float* Ub = Ur + W32;
-    float* Ud = Ub + W32;
-    float* Lc = Ud + W32;
-    float* Y = Lc + W32;
-    signed char* pv = piv + (size_t)blockIdx.x * W32 + lane;
-    tri_factor<float, 32, 32>(n, df, ef, (float)lam0, 1.1920929e-7f * (float)fmax(tnorm, 1e-30), Ur, Ub, Ud, Lc, pv);
-    for (int k = 0; k < n; k++) Y[(size_t)k * 32] = (float)start_value(i, k);
+    const double lam0 = act ? w[i] : 0.0;
+    float* Urw = scr32 + (size_t)blockIdx.x * 5 * W32;
+    float* Ubw = Urw + W32;
+    float* Udw = Ubw + W32;
+    float* Lcw = Udw + W32;
+    float* Yw = Lcw + W32;
+    signed char* pvw = piv + (size_t)blockIdx.x * W32;
+    float* Y = Yw + lane;
+    signed char* pv = pvw + lane;
+    tri_factor_staged(n, df, ef, (float)lam0, 1.1920929e-7f * (float)fmax(tnorm, 1e-30), Urw, Ubw, Udw, Lcw, pvw, stage_sm);
+    for (int k = 0; k < n; k++) Y[(size_t)k * 32] = act ? (float)start_value(i, k) : 0.0f;
+    __threadfence();
+    __syncwarp();
     float sc = 1.0f;
     for (int it = 0; it < 3; it++) {
-        const float mx = tri_solve<float, 32, 32>(n, Ur, Ub, Ud, Lc, pv, Y, sc);
+        const float mx = tri_solve_staged(n, Urw, Ubw, Udw, Lcw, pvw, Yw, sc, stage_sm);
         sc = mx > 0 ? 1.0f / mx : 1.0f;
     }
+    if (!act) return;
     const bool keep = i < n_store;
     if (!fp64) {
         double den = 1;
@@ -868,12 +1064,14 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const float* __restr
     const bool act = t >= 0;
     const int s0 = act ? cstart[t] : 0, m = lane - slo;
     const size_t W32 = (size_t)n * 32;
-    float* Ur = scr32 + (size_t)blockIdx.x * 5 * W32 + lane;
-    float* Ub = Ur + W32;
-    float* Ud = Ub + W32;
-    float* Lc = Ud + W32;
-    float* Y = Lc + W32;
-    signed char* pv = piv + (size_t)blockIdx.x * W32 + lane;
+    extern __shared__ float stage_sm[];
+    float* Urw = scr32 + (size_t)blockIdx.x * 5 * W32;
+    float* Ubw = Urw + W32;
+    float* Udw = Ubw + W32;
+    float* Lcw = Udw + W32;
+    float* Yw = Lcw + W32;
+    signed char* pvw = piv + (size_t)blockIdx.x * W32;
+    float* Y = Yw + lane;
     const float pert32 = 1.1920929e-7f * (float)fmax(tnorm, 1e-30);
     const double pert = 2.220446049250313e-16 * fmax(tnorm, 1e-300);
     // shifts: the FP32 estimates in increasing order within each cluster (distinct start vectors
@@ -883,11 +1081,13 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const float* __restr
         const double prev = __shfl_sync(0xffffffffu, sh, j - 1);
         if (lane == j && act && m > 0) sh = fmax(sh, prev + 10.0 * pert);
     }
-    if (act) tri_factor<float, 32, 32>(n, df, ef, (float)sh, pert32, Ur, Ub, Ud, Lc, pv);
+    // lanes without a member factor T itself and solve with a zero right-hand side
+    tri_factor_staged(n, df, ef, (float)sh, pert32, Urw, Ubw, Udw, Lcw, pvw, stage_sm);
     for (int k = 0; k < n; k++) Y[(size_t)k * 32] = act ? (float)start_value(s0 + m, k) - 1.0f : 0.0f;
+    __threadfence();
     __syncwarp();
     for (int it = 0; it < 3; it++) {
-        if (act) tri_solve<float, 32, 32>(n, Ur, Ub, Ud, Lc, pv, Y, 1.0f);
+        tri_solve_staged(n, Urw, Ubw, Udw, Lcw, pvw, Yw, 1.0f, stage_sm);
         __syncwarp();
         cluster_cholqr<float>(n, slo, sc, Y, Gs, Rinv);
     }
@@ -1127,6 +1327,14 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         smem_err = cudaFuncSetAttribute(tridiag_kernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     });
     if ((st = cuda_check(c, smem_err, "tridiag smem"))) return st;
+    static std::once_flag stage_once;
+    static cudaError_t stage_err = cudaSuccess;
+    std::call_once(stage_once, [] {
+        stage_err = cudaFuncSetAttribute(invit_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageSmem);
+        if (stage_err == cudaSuccess)
+            stage_err = cudaFuncSetAttribute(cluster_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageSmem);
+    });
+    if ((st = cuda_check(c, stage_err, "inverse-iteration smem"))) return st;
     if ((st = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_kernel<T2>, threads, smem), "occupancy"))) return st;
     if (per_sm < 1) return fail(c, BSE_ERR_CUDA, "tridiagonal kernel does not fit on an SM");
     // one block per SM (16 warps of loads in flight each) once the matrix is large enough; small
@@ -1158,8 +1366,10 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const size_t o_y = carve((redundant ? (size_t)B : 1) * n * sizeof(T2)), o_bar = carve(64);
     const bool fp64 = sizeof(T2) == sizeof(double2);
     const size_t o_band = carve(two_stage ? band_workspace(n, fp64, n_vec > 0, n_vec, nsm) : 0);
-    const size_t o_dd = carve(n * 8), o_ee = carve(n * 8), o_e2 = carve(n * 8), o_df = carve(n * 4), o_e2f = carve(n * 4);
-    const size_t o_ef = carve(n * 4), o_cl = carve(n);
+    // FP32 copies padded by 8 floats: the staged sweeps copy them in 16-byte pieces
+    const size_t o_dd = carve(n * 8), o_ee = carve(n * 8), o_e2 = carve(n * 8), o_df = carve((n + 8) * 4),
+                 o_e2f = carve(n * 4);
+    const size_t o_ef = carve((n + 8) * 4), o_cl = carve(n);
     const size_t o_y64 = carve(n * sizeof(double2));
     const size_t cpad = (size_t)(count_max + 31) / 32 * 32;   // whole warps of scratch
     const size_t o_scr = carve(5 * (size_t)n * cpad * 8), o_scr32 = carve(5 * (size_t)n * cpad * 4);
@@ -1282,7 +1492,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     R* z = (R*)(w + o_z);
     for (int i0 = 0; i0 < n; i0 += count_max) {
         const int cnt = std::min(count_max, n - i0);
-        invit_kernel<R><<<(cnt + 31) / 32, 32, 0, c->stream>>>(n, dd, ee, df, ef, dW, cl, i0, cnt, tnorm, y64, f_out, z, n,
+        invit_kernel<R><<<(cnt + 31) / 32, 32, kStageSmem, c->stream>>>(n, dd, ee, df, ef, dW, cl, i0, cnt, tnorm, y64, f_out, z, n,
                                                                  n_vec, (double*)(w + o_scr), (float*)(w + o_scr32),
                                                                  (signed char*)(w + o_piv), fp64 ? 1 : 0);
         c->launches++;
@@ -1346,7 +1556,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             cudaMemcpyAsync(dwf, wfirst.data(), wfirst.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream);
             for (int wb = 0; wb < nwarps; wb += wmax) {
                 const int nb = std::min(wmax, nwarps - wb);
-                cluster_kernel<R><<<nb, 32, 0, c->stream>>>(n, df, ef, w0, dW, dcs, dcz, dco, dwf, wb, tnorm, y64, f_out, z, n,
+                cluster_kernel<R><<<nb, 32, kStageSmem, c->stream>>>(n, df, ef, w0, dW, dcs, dcz, dco, dwf, wb, tnorm, y64, f_out, z, n,
                                                             n_vec, (float*)(w + o_scr32), (signed char*)(w + o_piv));
                 c->launches++;
             }
