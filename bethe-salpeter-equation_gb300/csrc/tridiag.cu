@@ -1342,8 +1342,12 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     int B = std::max(4, std::min(nsm, n / 16));
     if (const char* v = std::getenv("BSE_TRIDIAG_BLOCKS")) B = std::max(1, std::min(nsm * per_sm, std::atoi(v)));
     const int nt_max = (n + TR - 1) / TR;
-    // inverse-iteration batch: 61 bytes of scratch per (eigenvalue, row); one batch fills the GPU
-    const int count_max = std::min(n, std::max(32 * nsm, (int)std::min<int64_t>(8192, (int64_t)(12e9 / (61.0 * n)))));
+    // inverse-iteration batch: per (eigenvalue, row) 21 bytes of FP32 scratch, plus 40 bytes of FP64
+    // scratch in the FP64 path; the mixed path takes batches of up to 32768 eigenvalues (24 GB), so
+    // at large n every SM holds several warps of the latency-bound sweeps
+    const bool fp64 = sizeof(T2) == sizeof(double2);
+    const int count_max = fp64 ? std::min(n, std::max(32 * nsm, (int)std::min<int64_t>(8192, (int64_t)(12e9 / (61.0 * n)))))
+                               : std::min(n, std::max(32 * nsm, (int)std::min<int64_t>(32768, (int64_t)(24e9 / (21.0 * n)))));
     // workspace
     size_t off = 0;
     auto carve = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
@@ -1364,7 +1368,6 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const size_t o_v = carve(nbuf * n * sizeof(T2)), o_p = carve(nbuf * n * sizeof(T2));
     const size_t o_pp = carve(two_stage ? 0 : (size_t)nt_max * n * sizeof(T2)), o_dp = carve(2 * (size_t)B * sizeof(T2));
     const size_t o_y = carve((redundant ? (size_t)B : 1) * n * sizeof(T2)), o_bar = carve(64);
-    const bool fp64 = sizeof(T2) == sizeof(double2);
     const size_t o_band = carve(two_stage ? band_workspace(n, fp64, n_vec > 0, n_vec, nsm) : 0);
     // FP32 copies padded by 8 floats: the staged sweeps copy them in 16-byte pieces
     const size_t o_dd = carve(n * 8), o_ee = carve(n * 8), o_e2 = carve(n * 8), o_df = carve((n + 8) * 4),
@@ -1372,7 +1375,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const size_t o_ef = carve((n + 8) * 4), o_cl = carve(n);
     const size_t o_y64 = carve(n * sizeof(double2));
     const size_t cpad = (size_t)(count_max + 31) / 32 * 32;   // whole warps of scratch
-    const size_t o_scr = carve(5 * (size_t)n * cpad * 8), o_scr32 = carve(5 * (size_t)n * cpad * 4);
+    const size_t o_scr = carve(fp64 ? 5 * (size_t)n * cpad * 8 : 0), o_scr32 = carve(5 * (size_t)n * cpad * 4);
     const size_t o_piv = carve((size_t)n * cpad);
     const size_t o_z = carve((size_t)n * std::max(n_vec, 1) * sizeof(R));
     if ((st = ensure_work(c, off))) return st;
