@@ -31,6 +31,7 @@
 #include <string>
 #include <type_traits>
 
+#include "blas_ops.h"
 #include "bse_internal.h"
 #include "dev_util.h"
 
@@ -494,45 +495,6 @@ __global__ void transpose_kernel(int rows, int cols, const Tin* __restrict__ in,
         const int c = by + threadIdx.x, r = bx + j;
         if (r < rows && c < cols) out[c + (int64_t)r * ld_out] = tile[threadIdx.x][j];
     }
-}
-
-// ------------------------------------------------------------------------------------------
-// cuBLAS overloads (complex64 / complex128)
-// ------------------------------------------------------------------------------------------
-inline cublasStatus_t xhemm(cublasHandle_t h, int m, int n, const float2* al, const float2* A, int lda, const float2* B,
-                            int ldb, const float2* be, float2* C, int ldc) {
-    return cublasChemm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, m, n, al, A, lda, B, ldb, be, C, ldc);
-}
-inline cublasStatus_t xhemm(cublasHandle_t h, int m, int n, const double2* al, const double2* A, int lda,
-                            const double2* B, int ldb, const double2* be, double2* C, int ldc) {
-    return cublasZhemm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, m, n, al, A, lda, B, ldb, be, C, ldc);
-}
-inline cublasStatus_t xtrmm(cublasHandle_t h, cublasSideMode_t side, cublasOperation_t op, int m, int n,
-                            const float2* al, const float2* T, int ldt, const float2* B, int ldb, float2* C, int ldc) {
-    return cublasCtrmm(h, side, CUBLAS_FILL_MODE_UPPER, op, CUBLAS_DIAG_NON_UNIT, m, n, al, T, ldt, B, ldb, C, ldc);
-}
-inline cublasStatus_t xtrmm(cublasHandle_t h, cublasSideMode_t side, cublasOperation_t op, int m, int n,
-                            const double2* al, const double2* T, int ldt, const double2* B, int ldb, double2* C,
-                            int ldc) {
-    return cublasZtrmm(h, side, CUBLAS_FILL_MODE_UPPER, op, CUBLAS_DIAG_NON_UNIT, m, n, al, T, ldt, B, ldb, C, ldc);
-}
-inline cublasStatus_t xgemm(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
-                            const float2* al, const float2* A, int lda, const float2* B, int ldb, const float2* be,
-                            float2* C, int ldc) {
-    return cublasCgemm(h, ta, tb, m, n, k, al, A, lda, B, ldb, be, C, ldc);
-}
-inline cublasStatus_t xgemm(cublasHandle_t h, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
-                            const double2* al, const double2* A, int lda, const double2* B, int ldb,
-                            const double2* be, double2* C, int ldc) {
-    return cublasZgemm(h, ta, tb, m, n, k, al, A, lda, B, ldb, be, C, ldc);
-}
-inline cublasStatus_t xher2k(cublasHandle_t h, int n, int k, const float2* al, const float2* A, int lda,
-                             const float2* B, int ldb, const float* be, float2* C, int ldc) {
-    return cublasCher2k(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, k, al, A, lda, B, ldb, be, C, ldc);
-}
-inline cublasStatus_t xher2k(cublasHandle_t h, int n, int k, const double2* al, const double2* A, int lda,
-                             const double2* B, int ldb, const double* be, double2* C, int ldc) {
-    return cublasZher2k(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, k, al, A, lda, B, ldb, be, C, ldc);
 }
 
 int blas_check(bse_ctx* c, cublasStatus_t s, const char* what) {

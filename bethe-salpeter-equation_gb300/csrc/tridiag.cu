@@ -17,9 +17,9 @@
 //  3. invit_kernel: eigenvectors z_l of T by inverse iteration (LU with partial pivoting,
 //     dlagtf/dlagts style): three FP32 iterations, then one FP64 Rayleigh-quotient iteration
 //     that also gives the FP64 eigenvalue; one thread per eigenvalue, f_l on the fly.
-//  4. larft_kernel + apply_wy_kernel: X = Q Z, in compact-WY panels of 32 reflectors, only
-//     for the eigenvectors that are asked for (the FP64 refinement subspace, or all of them
-//     when the caller wants A).
+//  4. larft_kernel + build_vpanels_kernel: X = Q Z, in compact-WY panels of 32 reflectors applied
+//     by cuBLAS gemm / trmm, only for the eigenvectors that are asked for (the FP64 refinement
+//     subspace, or all of them when the caller wants A).
 // Every wait on another block is bounded: a barrier that times out sets an error word and
 // the kernel returns; the host reports BSE_ERR_NOT_CONVERGED.
 #include <cooperative_groups.h>
@@ -28,6 +28,7 @@
 #include <mutex>
 #include <string>
 
+#include "blas_ops.h"
 #include "bse_internal.h"
 #include "dev_util.h"
 
@@ -1183,87 +1184,21 @@ __global__ void __launch_bounds__(256) larft_kernel(int n, const T2* __restrict_
     __syncthreads();
     for (int pr = tid; pr < NB * NB; pr += blockDim.x) {
         const int j = pr / NB, i = pr % NB;
-        Tout[(size_t)p * NB * NB + pr] = (j <= i && i < nb) ? Tm[j][i] : C2<T2>(0, 0);
+        Tout[(size_t)p * NB * NB + j + (size_t)i * NB] = (j <= i && i < nb) ? Tm[j][i] : C2<T2>(0, 0);   // column-major
     }
 }
 
-// X[:, cols of this block] <- Q X, panels from last to first: X -= V (T (V^H X)).
-// Warp w accumulates the dots of reflectors w, w+8, w+16, w+24 for the block's CB columns.
-template <typename T2, int CB>
-__global__ void __launch_bounds__(256) apply_wy_kernel(int n, const T2* __restrict__ A, int64_t lda,
-                                                       const T2* __restrict__ Tf, T2* __restrict__ X, int64_t ldx,
-                                                       int ncols) {
-    typedef typename Real<T2>::t R;
-    constexpr int NB = 32;
-    __shared__ T2 W[NB][CB];
-    __shared__ T2 W2[NB][CB];
-    __shared__ T2 Ts[NB][NB + 1];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int c0 = blockIdx.x * CB;
-    const int npanel = (n - 1 + NB - 1) / NB;
-    for (int p = npanel - 1; p >= 0; p--) {
-        const int k0 = p * NB;
-        const int nb = min(NB, n - 1 - k0);
-        for (int pr = tid; pr < NB * NB; pr += blockDim.x) Ts[pr / NB][pr % NB] = Tf[(size_t)p * NB * NB + pr];
-        // W = V^H X
-        R ax[4][CB], ay[4][CB];
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-#pragma unroll
-            for (int j = 0; j < CB; j++) ax[q][j] = ay[q][j] = 0;
-        for (int r = k0 + 1 + lane; r < n; r += 32) {
-            T2 xv[CB];
-#pragma unroll
-            for (int j = 0; j < CB; j++) xv[j] = (c0 + j < ncols) ? X[r + (int64_t)(c0 + j) * ldx] : C2<T2>(0, 0);
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int i = warp + 8 * q;
-                if (i >= nb) continue;
-                const T2 v = vpanel(A, lda, k0, i, r);
-#pragma unroll
-                for (int j = 0; j < CB; j++) {
-                    const T2 t = cconjmul(v, xv[j]);
-                    ax[q][j] += t.x;
-                    ay[q][j] += t.y;
-                }
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-#pragma unroll
-            for (int j = 0; j < CB; j++) {
-                const R sx = warp_sum(ax[q][j]), sy = warp_sum(ay[q][j]);
-                if (lane == 0) W[warp + 8 * q][j] = C2<T2>(sx, sy);
-            }
-        __syncthreads();
-        // W2 = T W (T upper triangular)
-        for (int pr = tid; pr < NB * CB; pr += blockDim.x) {
-            const int i = pr / CB, j = pr % CB;
-            T2 acc = C2<T2>(0, 0);
-            if (i < nb)
-                for (int l = i; l < nb; l++) acc = cadd(acc, cmul(Ts[i][l], W[l][j]));
-            W2[i][j] = acc;
-        }
-        __syncthreads();
-        // X -= V W2
-        for (int r = k0 + 1 + tid; r < n; r += blockDim.x) {
-            T2 acc[CB];
-#pragma unroll
-            for (int j = 0; j < CB; j++) acc[j] = C2<T2>(0, 0);
-            for (int i = 0; i < nb; i++) {
-                const T2 v = vpanel(A, lda, k0, i, r);
-#pragma unroll
-                for (int j = 0; j < CB; j++) acc[j] = cadd(acc[j], cmul(v, W2[i][j]));
-            }
-#pragma unroll
-            for (int j = 0; j < CB; j++)
-                if (c0 + j < ncols) {
-                    T2* xp = X + r + (int64_t)(c0 + j) * ldx;
-                    *xp = csub(*xp, acc[j]);
-                }
-        }
-        __syncthreads();
-    }
+// Explicit reflector panels for the back-transformation: panel p (reflectors k0 = 32p ..
+// k0+nb-1, rows k0+1 .. n-1, m_p = n - k0 - 1 of them) at offset 32 * sum_{q<p} m_q, leading
+// dimension m_p; columns past nb are zero.
+template <typename T2>
+__global__ void build_vpanels_kernel(int n, const T2* __restrict__ A, int64_t lda, T2* __restrict__ V) {
+    const int p = blockIdx.y, k0 = 32 * p, m = n - k0 - 1, nb = min(32, n - 1 - k0);
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    const int64_t off = 32 * ((int64_t)p * (n - 1) - 32 * (int64_t)p * (p - 1) / 2);
+    for (int i = 0; i < 32; i++)
+        V[off + r + (int64_t)i * m] = i < nb ? vpanel(A, lda, k0, i, k0 + 1 + r) : C2<T2>(0, 0);
 }
 
 template <typename T2>
@@ -1585,14 +1520,36 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             c->launches++;
         }
         if (n > 1 && !two_stage) {
-            constexpr int CB = 4;
+            // X <- Q X in compact-WY panels of 32 reflectors, last to first: X[r0:] -= V (T (V^H X[r0:]))
             const int npanel = (n - 1 + 31) / 32;
-            T2* Tf = nullptr;
+            const int64_t vsize = 32 * ((int64_t)npanel * (n - 1) - 32 * (int64_t)npanel * (npanel - 1) / 2);
+            T2 *Tf = nullptr, *Vall = nullptr, *W1 = nullptr;
             if ((st = cuda_check(c, cudaMallocAsync((void**)&Tf, (size_t)npanel * 32 * 32 * sizeof(T2), c->stream), "WY factors"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&Vall, (size_t)vsize * sizeof(T2), c->stream), "WY panels"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&W1, 2 * (size_t)32 * n_vec * sizeof(T2), c->stream), "WY work"))) return st;
+            T2* W2 = W1 + (size_t)32 * n_vec;
             larft_kernel<T2><<<npanel, 256, 0, c->stream>>>(n, A, lda, tau, Tf);
-            apply_wy_kernel<T2, CB><<<(n_vec + CB - 1) / CB, 256, 0, c->stream>>>(n, A, lda, Tf, X, n, n_vec);
+            build_vpanels_kernel<T2><<<dim3((n + 255) / 256, npanel), 256, 0, c->stream>>>(n, A, lda, Vall);
             c->launches += 2;
-            cudaFreeAsync(Tf, c->stream);
+            cublasSetStream(c->cublas, c->stream);
+            T2 one, zero, mone;
+            one.x = 1; one.y = 0; zero.x = 0; zero.y = 0; mone.x = -1; mone.y = 0;
+            for (int p = npanel - 1; p >= 0 && !st; p--) {
+                const int k0 = 32 * p, m = n - k0 - 1, nb = std::min(32, n - 1 - k0);
+                const T2* Vp = Vall + 32 * ((int64_t)p * (n - 1) - 32 * (int64_t)p * (p - 1) / 2);
+                const T2* Tp = Tf + (size_t)p * 32 * 32;
+                cublasStatus_t bs = xgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nb, n_vec, m, &one, Vp, m, X + k0 + 1, n, &zero, W1, 32);
+                if (bs == CUBLAS_STATUS_SUCCESS)
+                    bs = xtrmm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, nb, n_vec, &one, Tp, 32, W1, 32, W2, 32);
+                if (bs == CUBLAS_STATUS_SUCCESS)
+                    bs = xgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m, n_vec, nb, &mone, Vp, m, W2, 32, &one, X + k0 + 1, n);
+                if (bs != CUBLAS_STATUS_SUCCESS) st = fail(c, BSE_ERR_CUDA, "cuBLAS failed in the back-transformation");
+            }
+            for (void* q : {(void*)Tf, (void*)Vall, (void*)W1}) cudaFreeAsync(q, c->stream);
+            if (st) {
+                cudaFreeAsync(X, c->stream);
+                return st;
+            }
         }
         st = cuda_check(c, cudaMemcpy2DAsync(A, lda * sizeof(T2), X, n * sizeof(T2), n * sizeof(T2), n_vec,
                                              cudaMemcpyDeviceToDevice, c->stream), "eigenvectors");
