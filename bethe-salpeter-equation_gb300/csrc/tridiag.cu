@@ -859,21 +859,35 @@ __global__ void __launch_bounds__(32) cluster64_kernel(int n, const double* __re
 // a generalised Rayleigh-Ritz step inside the cluster (Jacobi on the c x c projected matrix, FP64)
 // gives the eigenpairs.  The iterations run in FP32, as the tridiagonal of the mixed path carries
 // FP32 rounding itself.  Members outside [cout[2t], cout[2t+1]) are guards, solved but not written.
-// Scratch: interleaved [k][32] arrays per warp.
+// Scratch: interleaved [k][32] arrays per lane group.  A block of kClusterWarps warps serves one
+// lane group: warp 0 runs the (sequential) triangular solves, and all warps split the rows of the
+// Gram, orthonormalisation and output passes, which are row-parallel.
 constexpr int CMAX = 32;
+constexpr int kClusterWarps = 8;
+
+// this warp's share of rows [kb, ke) of the block's row-parallel passes (multiples of 16 rows)
+__device__ __forceinline__ void warp_rows(int n, int& kb, int& ke) {
+    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int per = ((n + nw - 1) / nw + 15) / 16 * 16;
+    kb = min(n, wid * per);
+    ke = min(n, kb + per);
+}
 
 // out[b][a] = sum_k u_b(k) z_a(k) over the columns z_a = X[k * 32 + a] of lane b's segment
 // [slo, slo + sc); lane b accumulates row b; u = z (Gram matrix) or u = T z (projected T).
-// FP32 partial sums over 16 rows go into FP64.
+// FP32 partial sums over 16 rows go into FP64.  The block's warps split the rows and add their
+// partial sums into out one warp after the other; every thread of the block calls this.
 template <typename F, bool APPLY_T>
 __device__ void cluster_gram(int n, int slo, int sc, const F* __restrict__ X, const F* __restrict__ d,
                              const F* __restrict__ e, double* __restrict__ out) {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int kb, ke;
+    warp_rows(n, kb, ke);
     double acc[CMAX];
 #pragma unroll
     for (int a = 0; a < CMAX; a++) acc[a] = 0;
-    F zprev = 0;
-    for (int k0 = 0; k0 < n; k0 += 16) {
+    F zprev = (APPLY_T && kb > 0 && kb < n) ? X[(size_t)(kb - 1) * 32] : F(0);
+    for (int k0 = kb; k0 < ke; k0 += 16) {
         // the chunk's rows (and one row ahead for T z) are loaded before any is used, so the
         // loads are in flight together instead of one dependent load per row
         F zb[17], db[16], eb[17];
@@ -892,20 +906,26 @@ __device__ void cluster_gram(int n, int slo, int sc, const F* __restrict__ X, co
         for (int a = 0; a < CMAX; a++) part[a] = 0;
 #pragma unroll
         for (int q = 0; q < 16; q++) {
-            const F zc = zb[q];
-            F u = zc;
-            if (APPLY_T) u = db[q] * zc + (q > 0 ? eb[q - 1] : eprev) * zprev + eb[q] * zb[q + 1];
+            if (k0 + q < ke) {
+                const F zc = zb[q];
+                F u = zc;
+                if (APPLY_T) u = db[q] * zc + (q > 0 ? eb[q - 1] : eprev) * zprev + eb[q] * zb[q + 1];
 #pragma unroll
-            for (int a = 0; a < CMAX; a++) part[a] += u * __shfl_sync(0xffffffffu, zc, a);
-            zprev = zc;
+                for (int a = 0; a < CMAX; a++) part[a] += u * __shfl_sync(0xffffffffu, zc, a);
+                zprev = zc;
+            }
         }
 #pragma unroll
         for (int a = 0; a < CMAX; a++) acc[a] += (double)part[a];
     }
+    for (int wq = 0; wq < nw; wq++) {
+        if (wid == wq)
 #pragma unroll
-    for (int a = 0; a < CMAX; a++)
-        if (sc > 0 && a >= slo && a < slo + sc) out[lane * CMAX + a] = acc[a];
-    __syncwarp();
+            for (int a = 0; a < CMAX; a++)
+                if (sc > 0 && a >= slo && a < slo + sc)
+                    out[lane * CMAX + a] = (wq == 0 ? 0.0 : out[lane * CMAX + a]) + acc[a];
+        __syncthreads();
+    }
 }
 
 // Cholesky G = R^T R in place (R upper, row-major, row stride CMAX); a pivot below 1e-10 of its
@@ -939,33 +959,38 @@ __device__ void inv_upper(int c, const double* R, double* Rinv) {
 }
 
 // Orthonormalise each segment's columns X[k * 32 + lane]: X <- X R^{-1} with G = R^T R, the
-// segment's first lane factoring its diagonal block.
+// segment's first lane in warp 0 factoring its diagonal block; rows split over the block's warps.
 template <typename F>
 __device__ void cluster_cholqr(int n, int slo, int sc, F* __restrict__ X, double* __restrict__ Gs,
                                double* __restrict__ Rinv) {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     cluster_gram<F, false>(n, slo, sc, X, (const F*)nullptr, (const F*)nullptr, Gs);
-    if (sc > 0 && lane == slo) {
+    if (wid == 0 && sc > 0 && lane == slo) {
         chol_upper(sc, Gs + slo * (CMAX + 1));
         inv_upper(sc, Gs + slo * (CMAX + 1), Rinv + slo * (CMAX + 1));
     }
-    __syncwarp();
+    __syncthreads();
     F rcol[CMAX];
 #pragma unroll
     for (int a = 0; a < CMAX; a++) rcol[a] = (sc > 0 && a >= slo && a <= lane) ? (F)Rinv[a * CMAX + lane] : F(0);
-    for (int k0 = 0; k0 < n; k0 += 16) {
+    int kb, ke;
+    warp_rows(n, kb, ke);
+    for (int k0 = kb; k0 < ke; k0 += 16) {
         F xb[16];
 #pragma unroll
-        for (int q = 0; q < 16; q++) xb[q] = k0 + q < n ? X[(size_t)(k0 + q) * 32] : F(0);
+        for (int q = 0; q < 16; q++) xb[q] = k0 + q < ke ? X[(size_t)(k0 + q) * 32] : F(0);
 #pragma unroll
         for (int q = 0; q < 16; q++) {
-            F v = 0;
+            if (k0 + q < ke) {
+                F v = 0;
 #pragma unroll
-            for (int a = 0; a < CMAX; a++) v += __shfl_sync(0xffffffffu, xb[q], a) * rcol[a];
-            if (sc > 0 && k0 + q < n) X[(size_t)(k0 + q) * 32] = v;
+                for (int a = 0; a < CMAX; a++) v += __shfl_sync(0xffffffffu, xb[q], a) * rcol[a];
+                if (sc > 0) X[(size_t)(k0 + q) * 32] = v;
+            }
         }
     }
-    __syncwarp();
+    __threadfence();
+    __syncthreads();
 }
 
 // Rayleigh-Ritz inside a cluster (one lane): M q = theta S q with S = Gs = Z^T Z = R^T R, Jacobi
@@ -1040,7 +1065,7 @@ __device__ void cluster_rr(int c, double* Gs, double* Rinv, double* M, double* Q
 }
 
 template <typename TZ>
-__global__ void __launch_bounds__(32) cluster_kernel(int n, const float* __restrict__ df, const float* __restrict__ ef,
+__global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, const float* __restrict__ df, const float* __restrict__ ef,
                                                      const double* __restrict__ w0, double* __restrict__ w,
                                                      const int* __restrict__ cstart, const int* __restrict__ csize,
                                                      const int* __restrict__ cout, const int* __restrict__ wfirst,
@@ -1048,9 +1073,10 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const float* __restr
                                                      double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz,
                                                      int n_store, float* __restrict__ scr32, signed char* __restrict__ piv) {
     __shared__ double Gs[CMAX * CMAX], Rinv[CMAX * CMAX], M[CMAX * CMAX], Q[CMAX * CMAX];
+    __shared__ double fred[kClusterWarps][32][2];
     __shared__ int ord[CMAX];
-    const int lane = threadIdx.x;
-    // this warp's clusters sit side by side on the lanes; find this lane's cluster and segment
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // this block's clusters sit side by side on the lanes; find this lane's cluster and segment
     const int t_end = wfirst[wbase + blockIdx.x + 1];
     int t = -1, slo = 0, sc = 0;
     for (int q = wfirst[wbase + blockIdx.x], off = 0; q < t_end; q++) {
@@ -1082,21 +1108,24 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const float* __restr
         const double prev = __shfl_sync(0xffffffffu, sh, j - 1);
         if (lane == j && act && m > 0) sh = fmax(sh, prev + 10.0 * pert);
     }
-    // lanes without a member factor T itself and solve with a zero right-hand side
-    tri_factor_staged(n, df, ef, (float)sh, pert32, Urw, Ubw, Udw, Lcw, pvw, stage_sm);
-    for (int k = 0; k < n; k++) Y[(size_t)k * 32] = act ? (float)start_value(s0 + m, k) - 1.0f : 0.0f;
+    // warp 0 runs the factor and the solves (lanes without a member factor T itself and solve
+    // with a zero right-hand side); the other warps help with the row-parallel passes
+    if (wid == 0) tri_factor_staged(n, df, ef, (float)sh, pert32, Urw, Ubw, Udw, Lcw, pvw, stage_sm);
+    int kb, ke;
+    warp_rows(n, kb, ke);
+    for (int k = kb; k < ke; k++) Y[(size_t)k * 32] = act ? (float)start_value(s0 + m, k) - 1.0f : 0.0f;
     __threadfence();
-    __syncwarp();
+    __syncthreads();
     for (int it = 0; it < 3; it++) {
-        tri_solve_staged(n, Urw, Ubw, Udw, Lcw, pvw, Yw, 1.0f, stage_sm);
-        __syncwarp();
+        if (wid == 0) tri_solve_staged(n, Urw, Ubw, Udw, Lcw, pvw, Yw, 1.0f, stage_sm);
+        __syncthreads();
         cluster_cholqr<float>(n, slo, sc, Y, Gs, Rinv);
     }
     cluster_gram<float, false>(n, slo, sc, Y, df, ef, Gs);
     cluster_gram<float, true>(n, slo, sc, Y, df, ef, M);
     const int blk = slo * (CMAX + 1);
-    if (act && lane == slo) cluster_rr(sc, Gs + blk, Rinv + blk, M + blk, Q + blk, ord + slo);
-    __syncwarp();
+    if (wid == 0 && act && lane == slo) cluster_rr(sc, Gs + blk, Rinv + blk, M + blk, Q + blk, ord + slo);
+    __syncthreads();
     // member m (lane slo + m) = Z Q[:, ord[m]] of its segment; f = y^H z
     double qcol[CMAX];
     const int col = act ? slo + ord[slo + m] : 0;
@@ -1106,17 +1135,17 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const float* __restr
     const bool outp = act && i >= cout[2 * t] && i < cout[2 * t + 1];
     const bool keep = outp && i < n_store;
     double fx = 0, fy = 0;
-    for (int k0 = 0; k0 < n; k0 += 16) {
+    for (int k0 = kb; k0 < ke; k0 += 16) {
         float yb[16];
 #pragma unroll
-        for (int q = 0; q < 16; q++) yb[q] = k0 + q < n ? Y[(size_t)(k0 + q) * 32] : 0.0f;
+        for (int q = 0; q < 16; q++) yb[q] = k0 + q < ke ? Y[(size_t)(k0 + q) * 32] : 0.0f;
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             const int k = k0 + q;
-            double v = 0;
+            if (k < ke) {
+                double v = 0;
 #pragma unroll
-            for (int b = 0; b < CMAX; b++) v += (double)__shfl_sync(0xffffffffu, yb[q], b) * qcol[b];
-            if (k < n) {
+                for (int b = 0; b < CMAX; b++) v += (double)__shfl_sync(0xffffffffu, yb[q], b) * qcol[b];
                 if (y && outp) {
                     const double2 yy = y[k];
                     fx += yy.x * v;
@@ -1126,9 +1155,17 @@ __global__ void __launch_bounds__(32) cluster_kernel(int n, const float* __restr
             }
         }
     }
-    if (outp) {
+    fred[wid][lane][0] = fx;
+    fred[wid][lane][1] = fy;
+    __syncthreads();
+    if (wid == 0 && outp) {
+        double sx = 0, sy = 0;
+        for (int q = 0; q < kClusterWarps; q++) {
+            sx += fred[q][lane][0];
+            sy += fred[q][lane][1];
+        }
         w[i] = M[col * (CMAX + 1)];
-        if (f) f[i] = make_double2(fx, fy);
+        if (f) f[i] = make_double2(sx, sy);
     }
 }
 
@@ -1494,7 +1531,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             cudaMemcpyAsync(dwf, wfirst.data(), wfirst.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream);
             for (int wb = 0; wb < nwarps; wb += wmax) {
                 const int nb = std::min(wmax, nwarps - wb);
-                cluster_kernel<R><<<nb, 32, kStageSmem, c->stream>>>(n, df, ef, w0, dW, dcs, dcz, dco, dwf, wb, tnorm, y64, f_out, z, n,
+                cluster_kernel<R><<<nb, 32 * kClusterWarps, kStageSmem, c->stream>>>(n, df, ef, w0, dW, dcs, dcz, dco, dwf, wb, tnorm, y64, f_out, z, n,
                                                             n_vec, (float*)(w + o_scr32), (signed char*)(w + o_piv));
                 c->launches++;
             }
