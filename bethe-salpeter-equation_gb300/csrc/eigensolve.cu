@@ -52,6 +52,96 @@ __global__ void residual_kernel(int64_t n, const double2* __restrict__ HX, const
     }
 }
 
+// Y = H X for Hermitian H (n x n FP64, lower triangle, leading dimension n) and X (n x m FP64),
+// in compensated FP32 ("double-float") arithmetic instead of FP64 (whose rate on this part is
+// ~1/64 of FP32): H and X are split into FP32 hi + lo parts as tiles are loaded, every hi*hi
+// product is formed exactly (TwoProd with an FMA) and added with TwoSum into an (s, t) pair, the
+// hi*lo cross terms go into t, lo*lo is dropped.  Relative error ~1e-12, FP64-class for the
+// Rayleigh-Ritz step.  Block tile 64 rows x 32 columns of Y; thread (lane c, warp w) owns rows
+// 8w .. 8w+7 of column c.
+constexpr int HM_TM = 64, HM_TN = 32, HM_TK = 16;
+
+__device__ __forceinline__ float4 split2(double2 v) {
+    const float rh = (float)v.x, ih = (float)v.y;
+    return make_float4(rh, ih, (float)(v.x - (double)rh), (float)(v.y - (double)ih));
+}
+// (s, t) += a * b with the product and the sum's rounding errors kept in t
+__device__ __forceinline__ void twoacc(float& s, float& t, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);
+    const float ns = __fadd_rn(s, p);
+    const float bv = __fsub_rn(ns, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(ns, bv)), __fsub_rn(p, bv));
+    s = ns;
+    t = __fadd_rn(t, __fadd_rn(e, pe));
+}
+
+__global__ void __launch_bounds__(256) hemm_df_kernel(int n, int m, const double2* __restrict__ H,
+                                                      const double2* __restrict__ X, double2* __restrict__ Y) {
+    __shared__ float4 Hs[HM_TK][HM_TM + 1];   // (re hi, im hi, re lo, im lo), [k][row]
+    __shared__ float4 Xs[HM_TK][HM_TN + 1];   // [k][column]
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int i0 = blockIdx.x * HM_TM, c0 = blockIdx.y * HM_TN;
+    float sr[8], tr[8], si[8], ti[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) sr[r] = tr[r] = si[r] = ti[r] = 0.0f;
+    for (int j0 = 0; j0 < n; j0 += HM_TK) {
+        if (i0 + HM_TM - 1 < j0) {
+            // tile strictly above the diagonal: conj of the stored lower tile, read along its columns
+            for (int e = tid; e < HM_TM * HM_TK; e += 256) {
+                const int jj = e % HM_TK, ii = e / HM_TK, i = i0 + ii, j = j0 + jj;
+                double2 h = make_double2(0.0, 0.0);
+                if (i < n && j < n) {
+                    h = H[j + (size_t)i * n];
+                    h.y = -h.y;
+                }
+                Hs[jj][ii] = split2(h);
+            }
+        } else {
+            for (int e = tid; e < HM_TM * HM_TK; e += 256) {
+                const int ii = e % HM_TM, jj = e / HM_TM, i = i0 + ii, j = j0 + jj;
+                double2 h = make_double2(0.0, 0.0);
+                if (i < n && j < n) {
+                    if (i >= j) {
+                        h = H[i + (size_t)j * n];
+                    } else {
+                        h = H[j + (size_t)i * n];
+                        h.y = -h.y;
+                    }
+                }
+                Hs[jj][ii] = split2(h);
+            }
+        }
+        for (int e = tid; e < HM_TK * HM_TN; e += 256) {
+            const int jj = e % HM_TK, cc = e / HM_TK, j = j0 + jj, col = c0 + cc;
+            Xs[jj][cc] = split2((j < n && col < m) ? X[j + (size_t)col * n] : make_double2(0.0, 0.0));
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int jj = 0; jj < HM_TK; jj++) {
+            const float4 x = Xs[jj][tx];
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const float4 h = Hs[jj][ty * 8 + r];
+                // real: hr xr - hi xi;  imag: hr xi + hi xr
+                twoacc(sr[r], tr[r], h.x, x.x);
+                twoacc(sr[r], tr[r], -h.y, x.y);
+                tr[r] = __fmaf_rn(h.x, x.z, __fmaf_rn(h.z, x.x, __fmaf_rn(-h.y, x.w, __fmaf_rn(-h.w, x.y, tr[r]))));
+                twoacc(si[r], ti[r], h.x, x.y);
+                twoacc(si[r], ti[r], h.y, x.x);
+                ti[r] = __fmaf_rn(h.x, x.w, __fmaf_rn(h.z, x.y, __fmaf_rn(h.y, x.z, __fmaf_rn(h.w, x.x, ti[r]))));
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const int row = i0 + ty * 8 + r, col = c0 + tx;
+        if (row < n && col < m)
+            Y[row + (size_t)col * n] = make_double2((double)sr[r] + (double)tr[r], (double)si[r] + (double)ti[r]);
+    }
+}
+
 int cusolver_check(bse_ctx* c, cusolverStatus_t s, const char* what) {
     if (s == CUSOLVER_STATUS_SUCCESS) return BSE_OK;
     if (s == CUSOLVER_STATUS_ALLOC_FAILED) return fail(c, BSE_ERR_OOM, std::string(what) + ": cuSOLVER allocation failed");
@@ -215,9 +305,11 @@ int run_refine(bse_ctx* c) {
         if ((st = cublas_check(c, cublasZtrsm(c->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
                                               n, m, &one, (cuDoubleComplex*)G, m, (cuDoubleComplex*)X, n), "trsm"))) return st;
     }
-    // Y = H X (Hermitian, lower triangle);  G = X^H Y
-    if ((st = cublas_check(c, cublasZhemm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, n, m, &one, (cuDoubleComplex*)H64, n,
-                                          (cuDoubleComplex*)X, n, &zero, (cuDoubleComplex*)Y, n), "hemm"))) return st;
+    // Y = H X (Hermitian, lower triangle; compensated FP32);  G = X^H Y
+    hemm_df_kernel<<<dim3((unsigned)((n + HM_TM - 1) / HM_TM), (unsigned)((m + HM_TN - 1) / HM_TN)), 256, 0, c->stream>>>(
+        (int)n, (int)m, H64, X, Y);
+    c->launches++;
+    if ((st = cuda_check(c, cudaGetLastError(), "refinement product"))) return st;
     if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, m, m, n, &one, (cuDoubleComplex*)X, n,
                                           (cuDoubleComplex*)Y, n, &zero, (cuDoubleComplex*)G, m), "gemm XhY"))) return st;
     if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m,
