@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <mutex>
+#include <utility>
 #include <string>
 #include <type_traits>
 
@@ -504,7 +505,7 @@ int blas_check(bse_ctx* c, cublasStatus_t s, const char* what) {
 
 // Workspace of the two-stage path; the same layout is used by the reduction and the back-transform.
 struct Layout {
-    size_t vall, tall, tau, ybuf, xbuf, small, pnorm, pw, pgram, bc, ab, prog, v2, zrm, total;
+    size_t vall, tall, tau, ybuf, xbuf, lr, small, pnorm, pw, pgram, bc, ab, prog, v2, zrm, total;
     int npanel, gmax;
     int64_t vsize;
 };
@@ -529,6 +530,7 @@ Layout layout(int n, size_t e, bool keep_q, int gmax, int n_vec) {
     L.tau = carve((size_t)std::max(L.npanel, 1) * NB * e);
     L.ybuf = carve((size_t)n * NB * e);
     L.xbuf = carve((size_t)n * NB * e);
+    L.lr = carve(4 * (size_t)n * NB * e);   // [V W] and [W V] for the full-storage update
     L.small = carve(4 * (size_t)NB * NB * e + (size_t)NB * std::max(n_vec, 1) * e * 2);
     L.pnorm = carve((size_t)gmax * e);
     L.pw = carve((size_t)gmax * NB * e);
@@ -587,7 +589,25 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
     T2* Nsm = Msm + NB * NB;
     const T2 one = C2h<T2>(1, 0), zero = C2h<T2>(0, 0), mone = C2h<T2>(-1, 0), mhalf = C2h<T2>(-0.5, 0);
     const R rone = 1;
+    // trailing update: Hermitian BLAS-3 on the lower triangle (hemm / her2k), or, for complex64,
+    // full-storage GEMMs (BSE_BAND_UPDATE=gemm, or =emul for the BF16x9 tensor-core emulation of
+    // FP32 GEMM; the own solver's matrix is built in full storage)
+    bool full_update = false;
+    cublasComputeType_t ctype = CUBLAS_COMPUTE_32F;
+    cublasEmulationStrategy_t emu_prev = CUBLAS_EMULATION_STRATEGY_DEFAULT;
+    cublasGetEmulationStrategy(c->cublas, &emu_prev);
+    if (const char* v = std::getenv("BSE_BAND_UPDATE")) {
+        const std::string mv(v);
+        if (sizeof(T2) == sizeof(float2) && (mv == "gemm" || mv == "emul")) {
+            full_update = true;
+            if (mv == "emul") {
+                ctype = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+                cublasSetEmulationStrategy(c->cublas, CUBLAS_EMULATION_STRATEGY_EAGER);
+            }
+        }
+    }
     int64_t voff = 0;
+    stage_begin(c, 13);
     for (int j = 0; j < Ly.npanel; j++) {
         const int c0 = j * NB, r0 = c0 + NB, m = n - r0, kk = std::min(NB, m);
         T2* Vj = keep_q ? Vall + voff : Vall;
@@ -612,15 +632,35 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
         // A22 <- Q^H A22 Q
         T2* A22 = A + r0 + (int64_t)r0 * lda;
         cublasHandle_t h = c->cublas;
-        if ((st = blas_check(c, xhemm(h, m, kk, &one, A22, (int)lda, Vj, m, &zero, Ybuf, m), "hemm"))) return st;
+        if (full_update) {
+            if ((st = blas_check(c, cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, kk, m, &one, A22, CUDA_C_32F, (int)lda, Vj, CUDA_C_32F, m,
+                                                 &zero, Ybuf, CUDA_C_32F, m, ctype, CUBLAS_GEMM_DEFAULT), "gemm AV"))) return st;
+        } else {
+            if ((st = blas_check(c, xhemm(h, m, kk, &one, A22, (int)lda, Vj, m, &zero, Ybuf, m), "hemm"))) return st;
+        }
         if ((st = blas_check(c, xtrmm(h, CUBLAS_SIDE_RIGHT, CUBLAS_OP_N, m, kk, &one, Tj, NB, Ybuf, m, Xbuf, m), "trmm"))) return st;
         if ((st = blas_check(c, xgemm(h, CUBLAS_OP_C, CUBLAS_OP_N, kk, kk, m, &one, Vj, m, Xbuf, m, &zero, Msm, NB), "gemm VX"))) return st;
         if ((st = blas_check(c, xtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_OP_C, kk, kk, &one, Tj, NB, Msm, NB, Nsm, NB), "trmm T^H"))) return st;
         if ((st = blas_check(c, xgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, kk, kk, &mhalf, Vj, m, Nsm, NB, &one, Xbuf, m), "gemm W"))) return st;
-        if ((st = blas_check(c, xher2k(h, m, kk, &mone, Vj, m, Xbuf, m, &rone, A22, (int)lda), "her2k"))) return st;
+        if (full_update) {
+            // A22 -= [V W] [W V]^H on full storage, one GEMM with k = 2 kk
+            T2* Lm = (T2*)(ws + Ly.lr);
+            T2* Rm = Lm + (size_t)2 * NB * n;
+            const size_t blk = (size_t)m * kk * sizeof(T2);
+            for (auto cp : {std::make_pair(Lm, (const T2*)Vj), std::make_pair(Lm + (size_t)m * kk, (const T2*)Xbuf),
+                            std::make_pair(Rm, (const T2*)Xbuf), std::make_pair(Rm + (size_t)m * kk, (const T2*)Vj)})
+                if ((st = cuda_check(c, cudaMemcpyAsync(cp.first, cp.second, blk, cudaMemcpyDeviceToDevice, c->stream), "update operands"))) return st;
+            if ((st = blas_check(c, cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_C, m, m, 2 * kk, &mone, Lm, CUDA_C_32F, m, Rm, CUDA_C_32F, m,
+                                                 &one, A22, CUDA_C_32F, (int)lda, ctype, CUBLAS_GEMM_DEFAULT), "update gemm"))) return st;
+        } else {
+            if ((st = blas_check(c, xher2k(h, m, kk, &mone, Vj, m, Xbuf, m, &rone, A22, (int)lda), "her2k"))) return st;
+        }
     }
     cublasSetMathMode(c->cublas, math_prev);
+    cublasSetEmulationStrategy(c->cublas, emu_prev);
+    stage_end(c, 13);
     // band -> tridiagonal
+    stage_begin(c, 14);
     T2* AB = (T2*)(ws + Ly.ab);
     int* prog = (int*)(ws + Ly.prog);
     band_extract_kernel<T2><<<(unsigned)(((int64_t)LDB * n + 255) / 256), 256, 0, c->stream>>>(n, A, lda, AB);
@@ -640,6 +680,7 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
     }
     band_diag_kernel<T2, R><<<(n + 255) / 256, 256, 0, c->stream>>>(n, AB, d, e);
     c->launches++;
+    stage_end(c, 14);
     return cuda_check(c, cudaGetLastError(), "two-stage reduction");
 }
 

@@ -18,8 +18,9 @@ constexpr double kMinval = 1.0e-5;                               // bse.version1
 constexpr double kPi = 3.1415926535897932384626433832;           // bse.version13.cpp:29
 constexpr double kConv = (1.602176634 * 1000) / (8.8541878176);  // bse.version13.cpp:32
 constexpr int kMaxNw = 16;        // orbitals per spin channel handled by the band kernel
-constexpr int kStages = 13;  // bands, tables, build, eig, refine, oscillators, eps, whole solve,
-                              // own solver: tridiagonal, eigenvalues, inverse iteration, back-transform, clusters
+constexpr int kStages = 15;  // bands, tables, build, eig, refine, oscillators, eps, whole solve,
+                              // own solver: tridiagonal, eigenvalues, inverse iteration, back-transform, clusters,
+                              // two-stage reduction: dense -> band, bulge chase
 
 // Geometry derived once from the lattice (Crystal_Lattice, bse.version13.cpp:85-124).
 struct Geometry {

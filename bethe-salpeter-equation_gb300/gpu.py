@@ -80,7 +80,8 @@ def load(build_if_missing: bool = True):
 
 
 STAGES = ("bands", "tables", "build", "eig", "refine", "oscillators", "eps", "solve",
-          "eig_tridiag", "eig_bisect", "eig_invit", "eig_backtransform", "eig_clusters")
+          "eig_tridiag", "eig_bisect", "eig_invit", "eig_backtransform", "eig_clusters",
+          "eig_band", "eig_chase")
 
 
 class BSEContext:

@@ -170,8 +170,9 @@ int bse_solve_many(bse_ctx** ctxs, int32_t n_ctx, const double* omega, int32_t n
  * [0] bands, [1] tables, [2] build, [3] eigensolve, [4] refinement, [5] oscillators, [6] eps,
  * [7] the whole of the last bse_solve; with BSE_EIG_OWN, the eigensolve's parts: [8] tridiagonal
  * reduction, [9] eigenvalues, [10] inverse iteration, [11] back-transformation, [12] clusters
- * (runs of eigenvalues FP32 bisection cannot separate, solved together) (bse_stage_times resets
- * unrecorded stages to 0). */
+ * (runs of eigenvalues FP32 bisection cannot separate, solved together); for the two-stage
+ * reduction (N > 8192) the parts of [8]: [13] dense -> band, [14] bulge chase.  A stage keeps the
+ * time of the last call that ran it. */
 int bse_stage_times(const bse_ctx* ctx, double* ms, int32_t n);
 
 /* Allocation-free dielectric function (no counterpart in the reference).  For callers that
