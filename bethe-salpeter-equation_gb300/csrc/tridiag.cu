@@ -11,12 +11,13 @@
 //     reflector; two grid barriers per reflector finish p and the scalar of w.  The same
 //     pass applies Q^H to the optical pair-density vector (y = Q^H rho), so oscillator
 //     strengths never need the eigenvectors of A: f_l = y^H z_l with z_l real.
-//  2. bisect32_kernel: eigenvalues of T by FP32 Sturm-count bisection, one thread per
-//     eigenvalue; cluster_bisect_kernel repeats it in FP64 only for eigenvalues that FP32
-//     cannot separate (FP64 division is slow on this part).
+//  2. bisect32_kernel: eigenvalues of T by FP32 Sturm-count multisection (several lanes per
+//     eigenvalue when the problem is small); runs of eigenvalues FP32 cannot separate form
+//     clusters (FP64 division is slow on this part, so no FP64 bisection).
 //  3. invit_kernel: eigenvectors z_l of T by inverse iteration (LU with partial pivoting,
-//     dlagtf/dlagts style): three FP32 iterations, then one FP64 Rayleigh-quotient iteration
-//     that also gives the FP64 eigenvalue; one thread per eigenvalue, f_l on the fly.
+//     dlagtf/dlagts style): three FP32 iterations (operands staged through shared memory), then
+//     in the FP64 path two FP64 Rayleigh-quotient iterations; one lane per eigenvalue, f_l on the
+//     fly.  cluster_kernel / cluster64_kernel: clusters by block inverse iteration + Rayleigh-Ritz.
 //  4. larft_kernel + build_vpanels_kernel: X = Q Z, in compact-WY panels of 32 reflectors applied
 //     by cuBLAS gemm / trmm, only for the eigenvectors that are asked for (the FP64 refinement
 //     subspace, or all of them when the caller wants A).
@@ -24,6 +25,7 @@
 // the kernel returns; the host reports BSE_ERR_NOT_CONVERGED.
 #include <cooperative_groups.h>
 
+#include <cmath>
 #include <cstdlib>
 #include <mutex>
 #include <string>
@@ -285,18 +287,41 @@ __device__ __forceinline__ int sturm(int n, const R* __restrict__ d, const R* __
 // eigenvalue whose FP32 estimate lies within `ctol` of a neighbour's (a cluster at FP32
 // resolution); those get FP64 bisection in cluster_bisect_kernel.  FP64 division is slow on
 // this part, so the FP64 work is spent only where FP32 cannot separate eigenvalues.
-__global__ void __launch_bounds__(32) bisect32_kernel(int n, const float* __restrict__ df, const float* __restrict__ e2f,
-                                                      float glo, float ghi, float pivminf, double* __restrict__ w) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__global__ void __launch_bounds__(256) bisect32_kernel(int n, int lp, int rounds, const float* __restrict__ df,
+                                                       const float* __restrict__ e2f, float glo, float ghi, float pivminf,
+                                                       double* __restrict__ w) {
+    // P = 2^lp lanes per eigenvalue evaluate the Sturm count at P interior points of the current
+    // interval ((P+1)-section): small problems spread each eigenvalue over a whole warp to fill
+    // the GPU, large ones keep plain bisection (P = 1), where more points would only add work
+    const int P = 1 << lp, lane = threadIdx.x & 31, grp = lane >> lp, gl = lane & (P - 1);
+    const int i = (((blockIdx.x * blockDim.x + threadIdx.x) >> 5) << (5 - lp)) + grp;
+    const bool valid = i < n;
+    const int ii = valid ? i : n - 1;
     float a = glo, b = ghi;
-    for (int it = 0; it < 40; it++) {
-        const float mid = 0.5f * (a + b);
-        if (!(mid > a && mid < b)) break;
-        if (sturm<float>(n, df, e2f, mid, pivminf) > i) b = mid;
-        else a = mid;
+    bool done = false;
+    for (int it = 0; it < rounds; it++) {
+        const float h = (b - a) / (float)(P + 1);
+        // P = 1: plain bisection at the midpoint (the FP64 path keeps this arithmetic exactly)
+        const float x = P == 1 ? 0.5f * (a + b) : a + h * (float)(gl + 1);
+        if (P == 1 ? !(x > a && x < b) : !(a + h > a && a + h < b)) done = true;
+        if (__all_sync(0xffffffffu, done)) break;
+        const int cnt = done ? 0 : sturm<float>(n, df, e2f, x, pivminf);
+        const unsigned ball = __ballot_sync(0xffffffffu, cnt > ii);
+        const unsigned mine = P == 32 ? ball : (ball >> (grp * P)) & ((1u << P) - 1u);
+        if (!done) {
+            if (P == 1) {
+                if (mine) b = x;
+                else a = x;
+            } else if (mine == 0) {
+                a = a + h * (float)P;
+            } else {
+                const int l0 = __ffs(mine) - 1;   // first point at or above eigenvalue ii
+                b = a + h * (float)(l0 + 1);
+                a = a + h * (float)l0;
+            }
+        }
     }
-    w[i] = 0.5 * ((double)a + (double)b);
+    if (valid && gl == 0) w[i] = 0.5 * ((double)a + (double)b);
 }
 
 __device__ __forceinline__ double start_value(unsigned i, unsigned k) {
@@ -1414,7 +1439,15 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const float pivminf = 1.17549435e-38f * (float)std::max(1.0, emax2);
     signed char* cl = (signed char*)(w + o_cl);
     stage_begin(c, 9);
-    bisect32_kernel<<<(n + 31) / 32, 32, 0, c->stream>>>(n, df, e2f, (float)glo, (float)ghi, pivminf, dW);
+    {
+        // lanes per eigenvalue: enough threads to hold ~16 warps per SM, at most a warp
+        int lp = 0;
+        while (!fp64 && lp < 5 && (int64_t)n * (2 << lp) <= (int64_t)nsm * 512) lp++;
+        const int P = 1 << lp;
+        const int rounds = (int)std::ceil(40.0 / std::log2((double)P + 1.0)) + 2;
+        const int64_t threads = ((int64_t)n * P + 255) / 256 * 256;
+        bisect32_kernel<<<(unsigned)(threads / 256), 256, 0, c->stream>>>(n, lp, rounds, df, e2f, (float)glo, (float)ghi, pivminf, dW);
+    }
     c->launches++;
     // clusters: runs of eigenvalues closer than FP32 bisection can resolve
     std::vector<double> hw(n);
