@@ -313,7 +313,7 @@ int run_refine(bse_ctx* c) {
     if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, m, m, n, &one, (cuDoubleComplex*)X, n,
                                           (cuDoubleComplex*)Y, n, &zero, (cuDoubleComplex*)G, m), "gemm XhY"))) return st;
     if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m,
-                                                        CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo), "heevd m"))) return st;
+                                                 CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo), "heevd m"))) return st;
     cusolverDnDestroyParams(prm);
     // XZ = X Z (refined Ritz vectors) and HXZ = (H X) Z; residuals r_j = HXZ_j - theta_j XZ_j
     double2* XZ = (double2*)(base + oZ);
