@@ -76,6 +76,17 @@ __device__ __forceinline__ void twoacc(float& s, float& t, float a, float b) {
     t = __fadd_rn(t, __fadd_rn(e, pe));
 }
 
+// (sr + tr, si + ti) += h * x for split operands h, x = (re hi, im hi, re lo, im lo)
+__device__ __forceinline__ void cmac_df(float& sr, float& tr, float& si, float& ti, float4 h, float4 x) {
+    // real: hr xr - hi xi;  imag: hr xi + hi xr
+    twoacc(sr, tr, h.x, x.x);
+    twoacc(sr, tr, -h.y, x.y);
+    tr = __fmaf_rn(h.x, x.z, __fmaf_rn(h.z, x.x, __fmaf_rn(-h.y, x.w, __fmaf_rn(-h.w, x.y, tr))));
+    twoacc(si, ti, h.x, x.y);
+    twoacc(si, ti, h.y, x.x);
+    ti = __fmaf_rn(h.x, x.w, __fmaf_rn(h.z, x.y, __fmaf_rn(h.y, x.z, __fmaf_rn(h.w, x.x, ti))));
+}
+
 __global__ void __launch_bounds__(256) hemm_df_kernel(int n, int m, const double2* __restrict__ H,
                                                       const double2* __restrict__ X, double2* __restrict__ Y) {
     __shared__ float4 Hs[HM_TK][HM_TM + 1];   // (re hi, im hi, re lo, im lo), [k][row]
@@ -121,16 +132,7 @@ __global__ void __launch_bounds__(256) hemm_df_kernel(int n, int m, const double
         for (int jj = 0; jj < HM_TK; jj++) {
             const float4 x = Xs[jj][tx];
 #pragma unroll
-            for (int r = 0; r < 8; r++) {
-                const float4 h = Hs[jj][ty * 8 + r];
-                // real: hr xr - hi xi;  imag: hr xi + hi xr
-                twoacc(sr[r], tr[r], h.x, x.x);
-                twoacc(sr[r], tr[r], -h.y, x.y);
-                tr[r] = __fmaf_rn(h.x, x.z, __fmaf_rn(h.z, x.x, __fmaf_rn(-h.y, x.w, __fmaf_rn(-h.w, x.y, tr[r]))));
-                twoacc(si[r], ti[r], h.x, x.y);
-                twoacc(si[r], ti[r], h.y, x.x);
-                ti[r] = __fmaf_rn(h.x, x.w, __fmaf_rn(h.z, x.y, __fmaf_rn(h.y, x.z, __fmaf_rn(h.w, x.x, ti[r]))));
-            }
+            for (int r = 0; r < 8; r++) cmac_df(sr[r], tr[r], si[r], ti[r], Hs[jj][ty * 8 + r], x);
         }
         __syncthreads();
     }
@@ -140,6 +142,99 @@ __global__ void __launch_bounds__(256) hemm_df_kernel(int n, int m, const double
         if (row < n && col < m)
             Y[row + (size_t)col * n] = make_double2((double)sr[r] + (double)tr[r], (double)si[r] + (double)ti[r]);
     }
+}
+
+// C = op(A) B (op = identity or conjugate transpose; A, B FP64, column-major) in the same
+// compensated FP32 arithmetic, split over K: block z writes the partial product over its K range
+// to C + z * split_stride, and sum_splits_kernel adds the partials in FP64.
+template <bool CONJ_A>
+__global__ void __launch_bounds__(256) gemm_df_kernel(int M, int N, int K, int kchunk, const double2* __restrict__ A,
+                                                      int64_t lda, const double2* __restrict__ B, int64_t ldb,
+                                                      double2* __restrict__ C, int64_t ldc, int64_t split_stride) {
+    __shared__ float4 As[HM_TK][HM_TM + 1];
+    __shared__ float4 Bs[HM_TK][HM_TN + 1];
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int i0 = blockIdx.x * HM_TM, c0 = blockIdx.y * HM_TN;
+    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    float sr[8], tr[8], si[8], ti[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) sr[r] = tr[r] = si[r] = ti[r] = 0.0f;
+    for (int j0 = kb; j0 < ke; j0 += HM_TK) {
+        if (CONJ_A) {   // op(A)(i, k) = conj(A[k + i lda]): read along k
+            for (int e = tid; e < HM_TM * HM_TK; e += 256) {
+                const int jj = e % HM_TK, ii = e / HM_TK, i = i0 + ii, k = j0 + jj;
+                double2 v = make_double2(0.0, 0.0);
+                if (i < M && k < ke) {
+                    v = A[k + (size_t)i * lda];
+                    v.y = -v.y;
+                }
+                As[jj][ii] = split2(v);
+            }
+        } else {
+            for (int e = tid; e < HM_TM * HM_TK; e += 256) {
+                const int ii = e % HM_TM, jj = e / HM_TM, i = i0 + ii, k = j0 + jj;
+                As[jj][ii] = split2((i < M && k < ke) ? A[i + (size_t)k * lda] : make_double2(0.0, 0.0));
+            }
+        }
+        for (int e = tid; e < HM_TK * HM_TN; e += 256) {
+            const int jj = e % HM_TK, cc = e / HM_TK, k = j0 + jj, col = c0 + cc;
+            Bs[jj][cc] = split2((k < ke && col < N) ? B[k + (size_t)col * ldb] : make_double2(0.0, 0.0));
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int jj = 0; jj < HM_TK; jj++) {
+            const float4 x = Bs[jj][tx];
+#pragma unroll
+            for (int r = 0; r < 8; r++) cmac_df(sr[r], tr[r], si[r], ti[r], As[jj][ty * 8 + r], x);
+        }
+        __syncthreads();
+    }
+    double2* Cz = C + blockIdx.z * split_stride;
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const int row = i0 + ty * 8 + r, col = c0 + tx;
+        if (row < M && col < N)
+            Cz[row + (size_t)col * ldc] = make_double2((double)sr[r] + (double)tr[r], (double)si[r] + (double)ti[r]);
+    }
+}
+
+__global__ void sum_splits_kernel(int64_t len, int splits, const double2* __restrict__ P, double2* __restrict__ C) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= len) return;
+    double x = 0, y = 0;
+    for (int z = 0; z < splits; z++) {
+        x += P[t + z * len].x;
+        y += P[t + z * len].y;
+    }
+    C[t] = make_double2(x, y);
+}
+
+constexpr int kMaxSplits = 16;
+
+// C (M x N, leading dimension M when split) = op(A) B; P: scratch of pcap elements for the
+// split-K partials (used when the output tiles alone would not fill the GPU).
+int gemm_df(bse_ctx* c, bool conj_a, int M, int N, int K, const double2* A, int64_t lda, const double2* B, int64_t ldb,
+            double2* C, int64_t ldc, double2* P, int64_t pcap) {
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+    const int tiles = ((M + HM_TM - 1) / HM_TM) * ((N + HM_TN - 1) / HM_TN);
+    int splits = std::max(1, std::min(kMaxSplits, (2 * nsm + tiles - 1) / tiles));
+    splits = (int)std::max<int64_t>(1, std::min<int64_t>(splits, pcap / ((int64_t)M * N)));
+    int kchunk = ((K + splits - 1) / splits + HM_TK - 1) / HM_TK * HM_TK;
+    splits = (K + kchunk - 1) / kchunk;
+    const dim3 grid((M + HM_TM - 1) / HM_TM, (N + HM_TN - 1) / HM_TN, splits);
+    double2* out = splits > 1 ? P : C;
+    const int64_t ldo = splits > 1 ? M : ldc;
+    if (conj_a) gemm_df_kernel<true><<<grid, 256, 0, c->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out, ldo, (int64_t)M * N);
+    else gemm_df_kernel<false><<<grid, 256, 0, c->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out, ldo, (int64_t)M * N);
+    c->launches++;
+    if (splits > 1) {
+        if (ldc != M) return fail(c, BSE_ERR_CUDA, "split product needs a packed output");
+        const int64_t len = (int64_t)M * N;
+        sum_splits_kernel<<<(unsigned)((len + 255) / 256), 256, 0, c->stream>>>(len, splits, P, C);
+        c->launches++;
+    }
+    return cuda_check(c, cudaGetLastError(), "compensated product");
 }
 
 int cusolver_check(bse_ctx* c, cusolverStatus_t s, const char* what) {
@@ -257,6 +352,7 @@ int run_refine(bse_ctx* c) {
     const size_t oX = carve(n * m * sizeof(double2)), oY = carve(n * m * sizeof(double2));
     const size_t oZ = carve(n * m * sizeof(double2)), oN = carve(m * sizeof(double));
     const size_t oG = carve(m * m * sizeof(double2)), oT = carve(m * sizeof(double));
+    const size_t oP = carve((size_t)kMaxSplits * m * m * sizeof(double2));
     const size_t oB = c->S ? carve((size_t)n * n * sizeof(double2)) : 0;
     // potrf / heevd workspaces on top
     cusolverDnParams_t prm;
@@ -273,6 +369,8 @@ int run_refine(bse_ctx* c) {
     double2* X = (double2*)(base + oX);
     double2* Y = (double2*)(base + oY);
     double2* G = (double2*)(base + oG);
+    double2* Pw = (double2*)(base + oP);
+    const int64_t pcap = (int64_t)kMaxSplits * m * m;
     double* theta = (double*)(base + oT);
     int* dinfo = (int*)(base + oW);
     void* dws = base + oW + 256;
@@ -294,12 +392,10 @@ int run_refine(bse_ctx* c) {
     widen_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, c->stream>>>(n * m, (const float2*)c->d_A, X);
     c->launches++;
     const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
-    const double done = 1.0, dzero = 0.0;
     cublasSetStream(c->cublas, c->stream);
     cusolverDnSetStream(c->cusolver, c->stream);
     for (int pass = 0; pass < 1; pass++) {   // CholeskyQR: the FP32 Ritz vectors are orthonormal to ~1e-7
-        if ((st = cublas_check(c, cublasZherk(c->cublas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, m, n, &done, (cuDoubleComplex*)X, n,
-                                              &dzero, (cuDoubleComplex*)G, m), "herk"))) return st;
+        if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, X, n, G, m, Pw, pcap))) return st;   // X^H X
         if ((st = cusolver_check(c, cusolverDnXpotrf(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m, CUDA_C_64F,
                                                      dws, dws1, hws.data(), hws1, dinfo), "potrf"))) return st;
         if ((st = cublas_check(c, cublasZtrsm(c->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
@@ -310,17 +406,14 @@ int run_refine(bse_ctx* c) {
         (int)n, (int)m, H64, X, Y);
     c->launches++;
     if ((st = cuda_check(c, cudaGetLastError(), "refinement product"))) return st;
-    if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, m, m, n, &one, (cuDoubleComplex*)X, n,
-                                          (cuDoubleComplex*)Y, n, &zero, (cuDoubleComplex*)G, m), "gemm XhY"))) return st;
+    if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, Y, n, G, m, Pw, pcap))) return st;   // X^H Y
     if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m,
                                                  CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo), "heevd m"))) return st;
     cusolverDnDestroyParams(prm);
     // XZ = X Z (refined Ritz vectors) and HXZ = (H X) Z; residuals r_j = HXZ_j - theta_j XZ_j
     double2* XZ = (double2*)(base + oZ);
-    if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, (cuDoubleComplex*)X, n,
-                                          (cuDoubleComplex*)G, m, &zero, (cuDoubleComplex*)XZ, n), "gemm XZ"))) return st;
-    if ((st = cublas_check(c, cublasZgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, (cuDoubleComplex*)Y, n,
-                                          (cuDoubleComplex*)G, m, &zero, (cuDoubleComplex*)X, n), "gemm HXZ"))) return st;
+    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, X, n, G, m, XZ, n, Pw, pcap))) return st;   // X Z
+    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, Y, n, G, m, X, n, Pw, pcap))) return st;    // (H X) Z
     double* rn = (double*)(base + oN);
     residual_kernel<<<(unsigned)nref, 256, 0, c->stream>>>(n, X, XZ, theta, rn);
     c->launches++;
