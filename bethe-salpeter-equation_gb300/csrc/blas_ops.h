@@ -43,4 +43,13 @@ inline cublasStatus_t xher2k(cublasHandle_t h, int n, int k, const double2* al, 
     return cublasZher2k(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, k, al, A, lda, B, ldb, be, C, ldc);
 }
 
+inline cublasStatus_t xherk(cublasHandle_t h, int n, int k, const float2* A, int lda, float2* C, int ldc) {
+    const float one = 1.0f, zero = 0.0f;
+    return cublasCherk(h, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C, n, k, &one, A, lda, &zero, C, ldc);
+}
+inline cublasStatus_t xherk(cublasHandle_t h, int n, int k, const double2* A, int lda, double2* C, int ldc) {
+    const double one = 1.0, zero = 0.0;
+    return cublasZherk(h, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C, n, k, &one, A, lda, &zero, C, ldc);
+}
+
 }  // namespace bse

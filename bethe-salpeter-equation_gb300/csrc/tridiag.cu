@@ -1206,26 +1206,19 @@ __device__ __forceinline__ T2 vpanel(const T2* __restrict__ A, int64_t lda, int 
 }
 
 template <typename T2>
-__global__ void __launch_bounds__(256) larft_kernel(int n, const T2* __restrict__ A, int64_t lda,
-                                                    const T2* __restrict__ tau, T2* __restrict__ Tout) {
-    typedef typename Real<T2>::t R;
+__global__ void __launch_bounds__(256) larft_kernel(int n, const T2* __restrict__ Gram, const T2* __restrict__ tau,
+                                                    T2* __restrict__ Tout) {
     constexpr int NB = 32;
     __shared__ T2 G[NB][NB + 1];
     __shared__ T2 Tm[NB][NB + 1];
     const int p = blockIdx.x, k0 = p * NB, nref = n - 1;
     const int nb = min(NB, nref - k0);
     const int tid = threadIdx.x;
-    // Gram matrix G[j][i] = sum_r conj(V[r][j]) V[r][i], j < i (pairs spread over threads)
+    // Gram matrix G[j][i] = sum_r conj(V[r][j]) V[r][i] of the panel (upper triangle, column-major,
+    // formed by herk on the explicit panel)
     for (int pr = tid; pr < NB * NB; pr += blockDim.x) {
-        const int j = pr / NB, i = pr % NB;
-        if (!(j < i && i < nb)) continue;
-        R sx = 0, sy = 0;
-        for (int r = k0 + i + 1; r < n; r++) {
-            const T2 q = cconjmul(vpanel(A, lda, k0, j, r), vpanel(A, lda, k0, i, r));
-            sx += q.x;
-            sy += q.y;
-        }
-        G[j][i] = C2<T2>(sx, sy);
+        const int j = pr % NB, i = pr / NB;
+        G[j][i] = Gram[(size_t)p * NB * NB + j + (size_t)i * NB];
     }
     __syncthreads();
     if (tid == 0) {
@@ -1598,10 +1591,18 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             if ((st = cuda_check(c, cudaMallocAsync((void**)&Vall, (size_t)vsize * sizeof(T2), c->stream), "WY panels"))) return st;
             if ((st = cuda_check(c, cudaMallocAsync((void**)&W1, 2 * (size_t)32 * n_vec * sizeof(T2), c->stream), "WY work"))) return st;
             T2* W2 = W1 + (size_t)32 * n_vec;
-            larft_kernel<T2><<<npanel, 256, 0, c->stream>>>(n, A, lda, tau, Tf);
             build_vpanels_kernel<T2><<<dim3((n + 255) / 256, npanel), 256, 0, c->stream>>>(n, A, lda, Vall);
-            c->launches += 2;
+            c->launches++;
             cublasSetStream(c->cublas, c->stream);
+            // per-panel Gram matrices V^H V (into Tf, turned into T in place by larft_kernel)
+            for (int p = 0; p < npanel && !st; p++) {
+                const int k0 = 32 * p, m = n - k0 - 1;
+                const T2* Vp = Vall + 32 * ((int64_t)p * (n - 1) - 32 * (int64_t)p * (p - 1) / 2);
+                if (xherk(c->cublas, 32, m, Vp, m, Tf + (size_t)p * 32 * 32, 32) != CUBLAS_STATUS_SUCCESS)
+                    st = fail(c, BSE_ERR_CUDA, "cuBLAS failed in the back-transformation (Gram)");
+            }
+            larft_kernel<T2><<<npanel, 256, 0, c->stream>>>(n, Tf, tau, Tf);
+            c->launches++;
             T2 one, zero, mone;
             one.x = 1; one.y = 0; zero.x = 0; zero.y = 0; mone.x = -1; mone.y = 0;
             for (int p = npanel - 1; p >= 0 && !st; p--) {
