@@ -35,32 +35,52 @@ template <typename T2> __device__ __forceinline__ T2 cinv(T2 a) {
 
 constexpr unsigned kSpinLimit = 1u << 26;   // ~seconds of polling before a barrier gives up
 
-// Grid-wide barrier for a cooperative launch.  bar[0] arrivals, bar[1] generation.
-// Returns false (after setting *err) if a block did not arrive in time or another block failed.
+// Grid-wide barrier for a cooperative launch.  bar[0] holds the arrivals of the current
+// barrier in its low 16 bits and a generation number in its high 16 bits: each block adds 1
+// (acquire-release, so its writes are published and the earlier arrivals' are seen); the last
+// arrival adds 2^16 - gridDim.x (release), which clears the count and starts the next
+// generation; the others poll with acquire loads until the generation changes.  One atomic
+// round trip for the last block and one poll for the rest, and the word is back to a zero count
+// after every completed barrier, so kernels with different grid sizes can share it.
+// Returns false (after setting *err on a timeout) if a block did not arrive in time or another
+// block failed.
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void red_add_release(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned* vgen = bar + 1;
-        volatile int* verr = err;
-        const unsigned gen = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
+        int ok = 1;
+        const unsigned old = atom_add_acq_rel(bar, 1u);
+        const unsigned gen = old >> 16;
+        if ((old & 0xffffu) == gridDim.x - 1) {
+            red_add_release(bar, 0x10000u - gridDim.x);
         } else {
             unsigned it = 0;
-            while (*vgen == gen) {
-                if (*verr != 0) break;
-                if (++it > kSpinLimit) { atomicExch(err, 1); break; }
-                __nanosleep(32);
+            while ((ld_acquire(bar) >> 16) == gen) {
+                if ((++it & 255u) == 0) {
+                    if (*(volatile int*)err != 0) { ok = 0; break; }
+                    if (it > kSpinLimit) { atomicExch(err, 1); ok = 0; break; }
+                    __nanosleep(64);
+                }
             }
         }
-        __threadfence();
+        s_ok = ok;
     }
     __syncthreads();
-    return *(volatile int*)err == 0;
+    return s_ok != 0;
 }
 
 template <typename R>

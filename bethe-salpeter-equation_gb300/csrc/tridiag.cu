@@ -49,7 +49,8 @@ struct TriArgs {
     T2* tau;                   // n-1
     T2* vbuf;                  // reflectors: [2][n] shared, or [B][n] per block (redundant mode)
     T2* pbuf;                  // p = tau A v: [2][n] shared, or [B][n] per block
-    T2* ppart;                 // [nt][n] column partial sums of the fused pass
+    T2* ppart;                 // [2][nt][n] column partial sums of the fused pass (by reflector parity)
+    int64_t ppstride;          // elements between the two parities
     T2* dpart;                 // [2][gridDim] block partial dots (shared mode)
     T2* y;                     // Q^H applied in place: [n] shared, or [B][n] per block (may be null)
     unsigned* bar;
@@ -123,6 +124,9 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
         // ---- phase B: pending rank-2 update of A[k+1:, k+1:] and column sums of A_new^H v_k ----
         const int m = n - (k + 1);
         const int nt = (m + a.TR - 1) / a.TR;
+        // partial sums alternate between two buffers: in redundant mode a block may start the
+        // next reflector's pass while another still reads this one's sums
+        T2* ppk = a.ppart + (size_t)(k & 1) * a.ppstride;
         const int64_t items = (int64_t)nt * m;
         const int64_t lo = items * b / B, hi = items * (b + 1) / B;
         for (int t = (int)(lo / m); t < nt && (int64_t)t * m < hi; t++) {
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
                 }
                 accx = warp_sum(accx);
                 accy = warp_sum(accy);
-                if (lane == 0) a.ppart[(size_t)t * n + c] = C2<T2>(accx, accy);
+                if (lane == 0) ppk[(size_t)t * n + c] = C2<T2>(accx, accy);
             }
         }
         if (!grid_barrier(a.bar, a.err)) return;
@@ -185,7 +189,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
             R acc[4] = {0, 0, 0, 0};
             for (int c = k + 1 + tid; c < n; c += nthr) {
                 T2 s = zero;
-                for (int t = 0; t < nt; t++) s = cadd(s, a.ppart[(size_t)t * n + c]);
+                for (int t = 0; t < nt; t++) s = cadd(s, ppk[(size_t)t * n + c]);
                 const T2 p = cmul(tauk, s);
                 const T2 v = (c == k + 1) ? C2<T2>(1, 0) : cmul(upd_colk(c), scal);
                 pk[c] = p;
@@ -213,7 +217,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
             R acc[4] = {0, 0, 0, 0};
             for (int c = k + 1 + b * nthr + tid; c < n; c += B * nthr) {
                 T2 s = zero;
-                for (int t = 0; t < nt; t++) s = cadd(s, a.ppart[(size_t)t * n + c]);
+                for (int t = 0; t < nt; t++) s = cadd(s, ppk[(size_t)t * n + c]);
                 const T2 p = cmul(tauk, s);
                 const T2 v = (c == k + 1) ? C2<T2>(1, 0) : cmul(upd_colk(c), scal);
                 pk[c] = p;
@@ -266,6 +270,201 @@ __global__ void __launch_bounds__(512, 1) tridiag_kernel(TriArgs<T2> a) {
         } else {
             a.d[0] = A[0].x;
         }
+    }
+}
+
+// Segments per trailing column in the fused pass, and loads in flight per lane.
+constexpr int kSegMax = 8;
+constexpr int kPassUnroll = 16;
+
+// Shared-memory footprint of tridiag_fused_kernel: reduction scratch, the alpha slot, the
+// pending reflector v, the pending w = p + alpha v, the new column / reflector, and y.
+template <typename T2>
+size_t fused_smem(int n, bool with_y) {
+    return 1056 + (size_t)(with_y ? 4 : 3) * n * sizeof(T2);
+}
+
+// One-stage reduction with the working vectors in shared memory (one grid barrier per
+// reflector).  Same algorithm and storage as tridiag_kernel's redundant mode; what changes is
+// where the vectors live and how the latency of each step is hidden:
+//  A. every block reads column k once, applies the pending rank-2 update and keeps the result
+//     in shared memory (it is both the reflector's source and, scaled, the new v);
+//  B. the block's share of the trailing columns is split into (column, row segment) items so
+//     that every warp has work, and each lane keeps 16 loads of its column in flight; the
+//     partial column sums of A^H v go to a double-buffered global array;
+//  C. after the barrier every block sums the partials of all columns, forms p, alpha, w and
+//     y <- H_k^H y in shared memory.
+// v, w and y never go through global memory, so a step costs one read of column k, the pass,
+// the barrier and one read of the partial sums.
+template <typename T2>
+__global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
+    typedef typename Real<T2>::t R;
+    extern __shared__ unsigned char smraw[];
+    R* red = reinterpret_cast<R*>(smraw);                                // 4 x 32 R (1024 bytes reserved)
+    T2* s_alpha = reinterpret_cast<T2*>(smraw + 1024);
+    const int n = a.n, tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarp = nthr >> 5, B = gridDim.x, b = blockIdx.x;
+    const int64_t lda = a.lda;
+    T2* A = a.A;
+    T2* sV = reinterpret_cast<T2*>(smraw + 1056);
+    T2* sW = sV + n;
+    T2* sX = sW + n;
+    T2* sY = a.y ? sX + n : nullptr;
+    const T2 zero = C2<T2>(0, 0), one = C2<T2>(1, 0);
+    for (int r = tid; r < n; r += nthr) {
+        sV[r] = zero;
+        sW[r] = zero;
+        if (sY) sY[r] = a.y[r];
+    }
+    __syncthreads();
+    for (int k = 0; k <= n - 2; k++) {
+        const int m = n - (k + 1);
+        const bool have_prev = k > 0;
+        const T2 vkk = sV[k], wkk = sW[k];
+        // ---- A: column k with the pending update of reflector k-1 ----
+        R loc[1] = {0};
+        for (int r0 = k + 1 + tid; r0 < n; r0 += 4 * nthr) {
+            T2 x[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int r = r0 + u * nthr;
+                x[u] = r < n ? A[r + (int64_t)k * lda] : zero;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int r = r0 + u * nthr;
+                if (r < n) {
+                    const T2 xv = csub(csub(x[u], cmulc(sV[r], wkk)), cmulc(sW[r], vkk));
+                    sX[r] = xv;
+                    if (r == k + 1) *s_alpha = xv;
+                    else loc[0] += xv.x * xv.x + xv.y * xv.y;
+                }
+            }
+        }
+        R dk = 0;
+        if (b == 0 && tid == 0) dk = csub(csub(A[k + (int64_t)k * lda], cmulc(vkk, wkk)), cmulc(wkk, vkk)).x;
+        block_sums<R, 1>(loc, red);
+        const R xnorm2 = loc[0];
+        const T2 alpha = *s_alpha;
+        T2 tauk, scal;
+        R beta;
+        if (xnorm2 == R(0) && alpha.y == R(0)) {
+            tauk = zero;
+            beta = alpha.x;
+            scal = zero;
+        } else {
+            beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2), alpha.x);
+            tauk = C2<T2>((beta - alpha.x) / beta, -alpha.y / beta);
+            scal = cinv(csub(alpha, C2<T2>(beta, 0)));
+        }
+        if (b == 0 && tid == 0) {
+            a.d[k] = dk;
+            a.e[k] = beta;
+            a.tau[k] = tauk;
+        }
+        // v_k in place (each thread rescales the rows it wrote)
+        for (int r = k + 1 + tid; r < n; r += nthr) sX[r] = r == k + 1 ? one : cmul(sX[r], scal);
+        __syncthreads();
+        // ---- B: pending update of this block's trailing columns, partial sums of A^H v_k ----
+        const int c_lo = k + 1 + (int)((int64_t)m * b / B), c_hi = k + 1 + (int)((int64_t)m * (b + 1) / B);
+        const int ncols = c_hi - c_lo;
+        const int cmax = (m + B - 1) / B;
+        // segments per column: fewest sequential rounds of kPassUnroll loads per warp (same on
+        // every block, since the partial sums of all blocks are added in phase C)
+        int nseg = 1, best = 1 << 30;
+        for (int g = 1; g <= kSegMax && (g == 1 || (m + g - 1) / g >= 32); g++) {
+            const int rounds = ((cmax * g + nwarp - 1) / nwarp) * (((m + g - 1) / g + 32 * kPassUnroll - 1) / (32 * kPassUnroll));
+            if (rounds < best) { best = rounds; nseg = g; }
+        }
+        const int L = (m + nseg - 1) / nseg;
+        T2* pout = a.ppart + (size_t)(k & 1) * kSegMax * n;
+        for (int it = warp; it < ncols * nseg; it += nwarp) {
+            const int c = c_lo + it % ncols, g = it / ncols;
+            const int r0 = k + 1 + g * L, r1 = min(n, r0 + L);
+            const T2 vc = sV[c], wc = sW[c];
+            T2* col = A + (int64_t)c * lda;
+            R ax = 0, ay = 0;
+            for (int r = r0 + lane; r < r1; r += 32 * kPassUnroll) {
+                T2 x[kPassUnroll];
+#pragma unroll
+                for (int u = 0; u < kPassUnroll; u++) x[u] = r + 32 * u < r1 ? col[r + 32 * u] : zero;
+#pragma unroll
+                for (int u = 0; u < kPassUnroll; u++) {
+                    const int i = r + 32 * u;
+                    if (i < r1) {
+                        T2 xv = x[u];
+                        if (have_prev) {
+                            xv = csub(csub(xv, cmulc(sV[i], wc)), cmulc(sW[i], vc));
+                            col[i] = xv;
+                        }
+                        const T2 q = cconjmul(xv, sX[i]);
+                        ax += q.x;
+                        ay += q.y;
+                    }
+                }
+            }
+            ax = warp_sum(ax);
+            ay = warp_sum(ay);
+            if (lane == 0) pout[(size_t)g * n + c] = C2<T2>(ax, ay);
+        }
+        if (!grid_barrier(a.bar, a.err)) return;
+        // ---- C: p_k = tau A^H v_k, alpha_k, w_k = p_k + alpha_k v_k, y <- H_k^H y ----
+        // reflector k-1 goes to column k-1 (read by nobody any more); column k is still the
+        // source of d_k / e_k only through shared memory
+        if (b == 0 && k >= 1)
+            for (int r = k + 1 + tid; r < n; r += nthr) A[r + (int64_t)(k - 1) * lda] = sV[r];
+        R acc[4] = {0, 0, 0, 0};
+        for (int c0 = k + 1 + tid; c0 < n; c0 += 4 * nthr) {
+            T2 sum[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int c = c0 + u * nthr;
+                sum[u] = zero;
+                if (c < n)
+                    for (int g = 0; g < nseg; g++) sum[u] = cadd(sum[u], pout[(size_t)g * n + c]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int c = c0 + u * nthr;
+                if (c < n) {
+                    const T2 p = cmul(tauk, sum[u]);
+                    const T2 v = sX[c];
+                    sW[c] = p;
+                    const T2 q = cconjmul(p, v);
+                    acc[0] += q.x;
+                    acc[1] += q.y;
+                    if (sY) {
+                        const T2 t = cconjmul(v, sY[c]);
+                        acc[2] += t.x;
+                        acc[3] += t.y;
+                    }
+                }
+            }
+        }
+        block_sums<R, 4>(acc, red);
+        const T2 alpha_k = cmul(C2<T2>(-0.5 * tauk.x, -0.5 * tauk.y), C2<T2>(acc[0], acc[1]));
+        const T2 coef = cmulc(C2<T2>(acc[2], acc[3]), tauk);   // conj(tau) (v^H y)
+        for (int c = k + 1 + tid; c < n; c += nthr) {
+            const T2 v = sX[c];
+            sW[c] = cadd(sW[c], cmul(alpha_k, v));
+            if (sY) sY[c] = csub(sY[c], cmul(coef, v));
+        }
+        __syncthreads();
+        T2* t = sV;
+        sV = sX;
+        sX = t;
+    }
+    if (b == 0) {
+        if (tid == 0) {
+            if (n >= 2) {
+                const T2 v = sV[n - 1], w = sW[n - 1];
+                a.d[n - 1] = csub(csub(A[(n - 1) + (int64_t)(n - 1) * lda], cmulc(v, w)), cmulc(w, v)).x;
+            } else {
+                a.d[0] = A[0].x;
+            }
+        }
+        if (sY)
+            for (int r = tid; r < n; r += nthr) a.y[r] = sY[r];
     }
 }
 
@@ -1345,18 +1544,25 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     // one barrier per reflector while every block can afford to finish all column sums itself;
     // BSE_TRIDIAG_MODE=shared|redundant overrides (tests run the large-n path at small n)
     // BSE_TRIDIAG_MODE=shared|redundant|twostage overrides (tests run every path at small n)
+    // BSE_TRIDIAG_MODE=fused|shared|redundant|twostage overrides (tests run every path at small n)
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t fused_max = optin > 2048 ? (size_t)optin - 1024 : 0;   // room for the barrier's static word
     bool redundant = n <= 8192;
     bool two_stage = n > kTwoStageMin;
+    bool fused = !two_stage && fused_smem<T2>(n, rho0 != nullptr) <= fused_max;
     if (const char* mode = std::getenv("BSE_TRIDIAG_MODE")) {
         const std::string md(mode);
-        if (md == "shared") redundant = two_stage = false;
-        else if (md == "redundant") { redundant = true; two_stage = false; }
-        else if (md == "twostage") { redundant = false; two_stage = n >= 3; }
+        if (md == "shared") redundant = two_stage = fused = false;
+        else if (md == "redundant") { redundant = true; two_stage = fused = false; }
+        else if (md == "twostage") { redundant = fused = false; two_stage = n >= 3; }
+        else if (md == "fused" && fused_smem<T2>(n, rho0 != nullptr) <= fused_max) { fused = true; two_stage = false; }
     }
-    if (two_stage) redundant = false;
-    const size_t nbuf = two_stage ? 0 : (redundant ? (size_t)B : 2);
+    if (two_stage || fused) redundant = false;
+    const size_t nbuf = (two_stage || fused) ? 0 : (redundant ? (size_t)B : 2);
     const size_t o_v = carve(nbuf * n * sizeof(T2)), o_p = carve(nbuf * n * sizeof(T2));
-    const size_t o_pp = carve(two_stage ? 0 : (size_t)nt_max * n * sizeof(T2)), o_dp = carve(2 * (size_t)B * sizeof(T2));
+    const int64_t ppstride = (int64_t)(fused ? kSegMax : nt_max) * n;
+    const size_t o_pp = carve(two_stage ? 0 : 2 * (size_t)ppstride * sizeof(T2)), o_dp = carve(2 * (size_t)B * sizeof(T2));
     const size_t o_y = carve((redundant ? (size_t)B : 1) * n * sizeof(T2)), o_bar = carve(64);
     const size_t o_band = carve(two_stage ? band_workspace(n, fp64, n_vec > 0, n_vec, nsm) : 0);
     // FP32 copies padded by 8 floats: the staged sweeps copy them in 16-byte pieces
@@ -1389,11 +1595,26 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     TriArgs<T2> ta;
     ta.n = n; ta.A = A; ta.lda = lda; ta.d = d; ta.e = e; ta.tau = tau;
     ta.vbuf = (T2*)(w + o_v); ta.pbuf = (T2*)(w + o_p); ta.ppart = (T2*)(w + o_pp); ta.dpart = (T2*)(w + o_dp);
-    ta.y = y; ta.bar = bar; ta.err = err; ta.TR = TR; ta.redundant = redundant ? 1 : 0;
+    ta.y = y; ta.bar = bar; ta.err = err; ta.TR = TR; ta.redundant = redundant ? 1 : 0; ta.ppstride = ppstride;
     void* kargs[] = {&ta};
     stage_begin(c, 8);
     if (two_stage) {
         if ((st = band_tridiag(c, n, A, lda, fp64, d, e, y, n_vec > 0, w + o_band, bar, err, n_vec))) return st;
+    } else if (fused) {
+        static std::once_flag fused_once;
+        static cudaError_t fused_err = cudaSuccess;
+        std::call_once(fused_once, [fused_max] {
+            fused_err = cudaFuncSetAttribute(tridiag_fused_kernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_max);
+        });
+        if ((st = cuda_check(c, fused_err, "fused tridiagonal smem"))) return st;
+        const size_t fsm = fused_smem<T2>(n, y != nullptr);
+        int fper = 0;
+        if ((st = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, tridiag_fused_kernel<T2>, threads, fsm), "occupancy"))) return st;
+        if (fper < 1) return fail(c, BSE_ERR_CUDA, "fused tridiagonal kernel does not fit on an SM");
+        const int FB = std::min(B, nsm * fper);
+        if ((st = cuda_check(c, cudaLaunchCooperativeKernel((void*)tridiag_fused_kernel<T2>, dim3(FB), dim3(threads), kargs, fsm,
+                                                            c->stream), "tridiagonal kernel launch"))) return st;
+        c->launches++;
     } else {
         if ((st = cuda_check(c, cudaLaunchCooperativeKernel((void*)tridiag_kernel<T2>, dim3(B), dim3(threads), kargs, smem,
                                                             c->stream), "tridiagonal kernel launch"))) return st;

@@ -161,11 +161,12 @@ def test_degenerate_spectrum_weights(synth, oracle, gpu, solver):
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-8 * np.linalg.norm(ref["eps2"])
 
 
-@pytest.mark.parametrize("mode", ["shared", "redundant", "twostage"])
+@pytest.mark.parametrize("mode", ["fused", "shared", "redundant", "twostage"])
 def test_tridiagonal_barrier_modes(synth, oracle, gpu, monkeypatch, mode):
-    """Every variant of the tridiagonal reduction (one-stage with one grid barrier per reflector
-    and per-block copies, or two barriers with shared vectors; the two-stage dense -> band ->
-    tridiagonal path of the largest matrices) gives the oracle's spectrum."""
+    """Every variant of the tridiagonal reduction (one-stage with the working vectors in shared
+    memory, or with per-block copies in global memory, both one grid barrier per reflector, or
+    two barriers with shared vectors; the two-stage dense -> band -> tridiagonal path of the
+    largest matrices) gives the oracle's spectrum."""
     monkeypatch.setenv("BSE_TRIDIAG_MODE", mode)
     prob = synth.orb8_problem(grid=4)
     ref = oracle.solve(prob, OMEGA, GAMMA)
