@@ -43,6 +43,15 @@ inline cublasStatus_t xher2k(cublasHandle_t h, int n, int k, const double2* al, 
     return cublasZher2k(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, k, al, A, lda, B, ldb, be, C, ldc);
 }
 
+// B <- U^{-1} B, U upper triangular (left side, no transpose, non-unit diagonal)
+inline cublasStatus_t xtrsm_lu(cublasHandle_t h, int m, int n, const float2* U, int ldu, float2* B, int ldb) {
+    const float2 one = make_float2(1.f, 0.f);
+    return cublasCtrsm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, m, n, &one, U, ldu, B, ldb);
+}
+inline cublasStatus_t xtrsm_lu(cublasHandle_t h, int m, int n, const double2* U, int ldu, double2* B, int ldb) {
+    const double2 one = make_double2(1.0, 0.0);
+    return cublasZtrsm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, m, n, &one, U, ldu, B, ldb);
+}
 inline cublasStatus_t xherk(cublasHandle_t h, int n, int k, const float2* A, int lda, float2* C, int ldc) {
     const float one = 1.0f, zero = 0.0f;
     return cublasCherk(h, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C, n, k, &one, A, lda, &zero, C, ldc);

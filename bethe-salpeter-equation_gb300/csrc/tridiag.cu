@@ -18,9 +18,9 @@
 //     dlagtf/dlagts style): three FP32 iterations (operands staged through shared memory), then
 //     in the FP64 path two FP64 Rayleigh-quotient iterations; one lane per eigenvalue, f_l on the
 //     fly.  cluster_kernel / cluster64_kernel: clusters by block inverse iteration + Rayleigh-Ritz.
-//  4. larft_kernel + build_vpanels_kernel: X = Q Z, in compact-WY panels of 32 reflectors applied
-//     by cuBLAS gemm / trmm, only for the eigenvectors that are asked for (the FP64 refinement
-//     subspace, or all of them when the caller wants A).
+//  4. build_vpanels_kernel + ut_diag_kernel + cuBLAS herk / gemm / trsm: X = Q Z in panels of 256
+//     reflectors (compact WY in its triangular-solve form), only for the eigenvectors that are
+//     asked for (the FP64 refinement subspace, or all of them when the caller wants A).
 // Every wait on another block is bounded: a barrier that times out sets an error word and
 // the kernel returns; the host reports BSE_ERR_NOT_CONVERGED.
 #include <cooperative_groups.h>
@@ -1393,9 +1393,15 @@ __global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, cons
     }
 }
 
-// Compact-WY factors of the reflector panels: panel p holds reflectors k0 = 32p .. k0+nb-1 and
-// Q_p = H_k0 ... H_{k0+nb-1} = I - V T V^H with T upper triangular (forward zlarft).
-// V[r][i] = 0 above row k0+i+1, 1 at row k0+i+1, A[r, k0+i] below.  One block per panel.
+// Back-transformation X <- Q X, Q = H_0 H_1 ... H_{n-2}, in panels of kWY reflectors.  Panel p
+// holds reflectors k0 = kWY p .. k0+nb-1 and acts on rows k0+1 .. n-1 (m_p = n-1-k0 of them);
+// V[r][i] = 0 above row k0+i+1, 1 at row k0+i+1, A[r, k0+i] below.  With U = diag(1/tau_i) +
+// striu(V^H V) (the "UT transform" form of compact WY: U^{-1} is zlarft's T),
+//     Q_p = H_k0 ... H_{k0+nb-1} = I - V U^{-1} V^H,
+// so X[k0+1:] -= V (U^{-1} (V^H X[k0+1:])) costs two GEMMs and a triangular solve per panel.
+// A reflector with tau = 0 is the identity: its column of V is set to zero and U_ii = 1.
+constexpr int kWY = 256;
+
 template <typename T2>
 __device__ __forceinline__ T2 vpanel(const T2* __restrict__ A, int64_t lda, int k0, int i, int r) {
     const int top = k0 + i + 1;
@@ -1404,55 +1410,41 @@ __device__ __forceinline__ T2 vpanel(const T2* __restrict__ A, int64_t lda, int 
     return A[r + (int64_t)(k0 + i) * lda];
 }
 
+// Offset of panel p in the explicit panel array: kWY * sum_{q<p} m_q with m_q = n - 1 - kWY q.
+__host__ __device__ __forceinline__ int64_t vpanel_offset(int n, int p) {
+    return kWY * ((int64_t)p * (n - 1) - kWY * (int64_t)p * (p - 1) / 2);
+}
+
+// Explicit panels, column-major with leading dimension m_p; reflectors past nb are zero.
+// Grid (row blocks, kWY / 8 column groups, panels).
 template <typename T2>
-__global__ void __launch_bounds__(256) larft_kernel(int n, const T2* __restrict__ Gram, const T2* __restrict__ tau,
-                                                    T2* __restrict__ Tout) {
-    constexpr int NB = 32;
-    __shared__ T2 G[NB][NB + 1];
-    __shared__ T2 Tm[NB][NB + 1];
-    const int p = blockIdx.x, k0 = p * NB, nref = n - 1;
-    const int nb = min(NB, nref - k0);
-    const int tid = threadIdx.x;
-    // Gram matrix G[j][i] = sum_r conj(V[r][j]) V[r][i] of the panel (upper triangle, column-major,
-    // formed by herk on the explicit panel)
-    for (int pr = tid; pr < NB * NB; pr += blockDim.x) {
-        const int j = pr % NB, i = pr / NB;
-        G[j][i] = Gram[(size_t)p * NB * NB + j + (size_t)i * NB];
-    }
-    __syncthreads();
-    if (tid == 0) {
-        for (int i = 0; i < nb; i++) {
-            const T2 ti = tau[k0 + i];
-            // w = -tau_i * G[0:i, i];  T[0:i, i] = T[0:i, 0:i] w
-            for (int j = 0; j < i; j++) Tm[j][i] = cmul(C2<T2>(-ti.x, -ti.y), G[j][i]);
-            for (int j = 0; j < i; j++) {
-                T2 acc = C2<T2>(0, 0);
-                for (int l = j; l < i; l++) acc = cadd(acc, cmul(Tm[j][l], Tm[l][i]));
-                G[j][0] = acc;   // G column 0 is free now (rows j < i only)
-            }
-            for (int j = 0; j < i; j++) Tm[j][i] = G[j][0];
-            Tm[i][i] = ti;
-            for (int j = i + 1; j < NB; j++) Tm[j][i] = C2<T2>(0, 0);
-        }
-    }
-    __syncthreads();
-    for (int pr = tid; pr < NB * NB; pr += blockDim.x) {
-        const int j = pr / NB, i = pr % NB;
-        Tout[(size_t)p * NB * NB + j + (size_t)i * NB] = (j <= i && i < nb) ? Tm[j][i] : C2<T2>(0, 0);   // column-major
+__global__ void __launch_bounds__(256) build_vpanels_kernel(int n, const T2* __restrict__ A, int64_t lda, const T2* __restrict__ tau,
+                                                            T2* __restrict__ V) {
+    const int p = blockIdx.z, k0 = kWY * p, m = n - 1 - k0, nb = min(kWY, m);
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    T2* Vp = V + vpanel_offset(n, p);
+    for (int i = 8 * blockIdx.y; i < 8 * blockIdx.y + 8; i++) {
+        const bool live = i < nb && (tau[k0 + i].x != 0 || tau[k0 + i].y != 0);
+        Vp[r + (int64_t)i * m] = live ? vpanel(A, lda, k0, i, k0 + 1 + r) : C2<T2>(0, 0);
     }
 }
 
-// Explicit reflector panels for the back-transformation: panel p (reflectors k0 = 32p ..
-// k0+nb-1, rows k0+1 .. n-1, m_p = n - k0 - 1 of them) at offset 32 * sum_{q<p} m_q, leading
-// dimension m_p; columns past nb are zero.
+// U of every panel from its Gram matrix (strict upper triangle from herk): diagonal 1/tau_i
+// (1 for tau_i = 0 and for the padding past nb), strict upper triangle kept, lower part zero.
 template <typename T2>
-__global__ void build_vpanels_kernel(int n, const T2* __restrict__ A, int64_t lda, T2* __restrict__ V) {
-    const int p = blockIdx.y, k0 = 32 * p, m = n - k0 - 1, nb = min(32, n - 1 - k0);
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= m) return;
-    const int64_t off = 32 * ((int64_t)p * (n - 1) - 32 * (int64_t)p * (p - 1) / 2);
-    for (int i = 0; i < 32; i++)
-        V[off + r + (int64_t)i * m] = i < nb ? vpanel(A, lda, k0, i, k0 + 1 + r) : C2<T2>(0, 0);
+__global__ void ut_diag_kernel(int n, int npanel, const T2* __restrict__ tau, T2* __restrict__ U) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)npanel * kWY * kWY) return;
+    const int p = (int)(t / ((int64_t)kWY * kWY)), e = (int)(t % ((int64_t)kWY * kWY));
+    const int j = e % kWY, i = e / kWY;   // row j, column i (column-major)
+    const int k = kWY * p + i, nb = min(kWY, n - 1 - kWY * p);
+    if (j > i) {
+        U[t] = C2<T2>(0, 0);
+    } else if (j == i) {
+        const bool live = i < nb && (tau[k].x != 0 || tau[k].y != 0);
+        U[t] = live ? cinv(tau[k]) : C2<T2>(1, 0);
+    }
 }
 
 template <typename T2>
@@ -1804,39 +1796,39 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             c->launches++;
         }
         if (n > 1 && !two_stage) {
-            // X <- Q X in compact-WY panels of 32 reflectors, last to first: X[r0:] -= V (T (V^H X[r0:]))
-            const int npanel = (n - 1 + 31) / 32;
-            const int64_t vsize = 32 * ((int64_t)npanel * (n - 1) - 32 * (int64_t)npanel * (npanel - 1) / 2);
+            // X <- Q X, panels of kWY reflectors from the last to the first
+            const int npanel = (n - 1 + kWY - 1) / kWY;
+            const int64_t vsize = vpanel_offset(n, npanel);
             T2 *Tf = nullptr, *Vall = nullptr, *W1 = nullptr;
-            if ((st = cuda_check(c, cudaMallocAsync((void**)&Tf, (size_t)npanel * 32 * 32 * sizeof(T2), c->stream), "WY factors"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&Tf, (size_t)npanel * kWY * kWY * sizeof(T2), c->stream), "WY factors"))) return st;
             if ((st = cuda_check(c, cudaMallocAsync((void**)&Vall, (size_t)vsize * sizeof(T2), c->stream), "WY panels"))) return st;
-            if ((st = cuda_check(c, cudaMallocAsync((void**)&W1, 2 * (size_t)32 * n_vec * sizeof(T2), c->stream), "WY work"))) return st;
-            T2* W2 = W1 + (size_t)32 * n_vec;
-            build_vpanels_kernel<T2><<<dim3((n + 255) / 256, npanel), 256, 0, c->stream>>>(n, A, lda, Vall);
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&W1, (size_t)kWY * n_vec * sizeof(T2), c->stream), "WY work"))) return st;
+            build_vpanels_kernel<T2><<<dim3((n - 1 + 255) / 256, kWY / 8, npanel), 256, 0, c->stream>>>(n, A, lda, tau, Vall);
             c->launches++;
             cublasSetStream(c->cublas, c->stream);
-            // per-panel Gram matrices V^H V (into Tf, turned into T in place by larft_kernel)
             for (int p = 0; p < npanel && !st; p++) {
-                const int k0 = 32 * p, m = n - k0 - 1;
-                const T2* Vp = Vall + 32 * ((int64_t)p * (n - 1) - 32 * (int64_t)p * (p - 1) / 2);
-                if (xherk(c->cublas, 32, m, Vp, m, Tf + (size_t)p * 32 * 32, 32) != CUBLAS_STATUS_SUCCESS)
+                const int m = n - 1 - kWY * p;
+                if (xherk(c->cublas, kWY, m, Vall + vpanel_offset(n, p), m, Tf + (size_t)p * kWY * kWY, kWY) != CUBLAS_STATUS_SUCCESS)
                     st = fail(c, BSE_ERR_CUDA, "cuBLAS failed in the back-transformation (Gram)");
             }
-            larft_kernel<T2><<<npanel, 256, 0, c->stream>>>(n, Tf, tau, Tf);
-            c->launches++;
+            if (!st) {
+                const int64_t nu = (int64_t)npanel * kWY * kWY;
+                ut_diag_kernel<T2><<<(unsigned)((nu + 255) / 256), 256, 0, c->stream>>>(n, npanel, tau, Tf);
+                c->launches++;
+            }
             T2 one, zero, mone;
             one.x = 1; one.y = 0; zero.x = 0; zero.y = 0; mone.x = -1; mone.y = 0;
             for (int p = npanel - 1; p >= 0 && !st; p--) {
-                const int k0 = 32 * p, m = n - k0 - 1, nb = std::min(32, n - 1 - k0);
-                const T2* Vp = Vall + 32 * ((int64_t)p * (n - 1) - 32 * (int64_t)p * (p - 1) / 2);
-                const T2* Tp = Tf + (size_t)p * 32 * 32;
-                cublasStatus_t bs = xgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nb, n_vec, m, &one, Vp, m, X + k0 + 1, n, &zero, W1, 32);
+                const int k0 = kWY * p, m = n - 1 - k0, nb = std::min(kWY, m);
+                const T2* Vp = Vall + vpanel_offset(n, p);
+                const T2* Up = Tf + (size_t)p * kWY * kWY;
+                cublasStatus_t bs = xgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nb, n_vec, m, &one, Vp, m, X + k0 + 1, n, &zero, W1, kWY);
+                if (bs == CUBLAS_STATUS_SUCCESS) bs = xtrsm_lu(c->cublas, nb, n_vec, Up, kWY, W1, kWY);
                 if (bs == CUBLAS_STATUS_SUCCESS)
-                    bs = xtrmm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, nb, n_vec, &one, Tp, 32, W1, 32, W2, 32);
-                if (bs == CUBLAS_STATUS_SUCCESS)
-                    bs = xgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m, n_vec, nb, &mone, Vp, m, W2, 32, &one, X + k0 + 1, n);
+                    bs = xgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m, n_vec, nb, &mone, Vp, m, W1, kWY, &one, X + k0 + 1, n);
                 if (bs != CUBLAS_STATUS_SUCCESS) st = fail(c, BSE_ERR_CUDA, "cuBLAS failed in the back-transformation");
             }
+            if (!st) st = cuda_check(c, cudaGetLastError(), "back-transformation");
             for (void* q : {(void*)Tf, (void*)Vall, (void*)W1}) cudaFreeAsync(q, c->stream);
             if (st) {
                 cudaFreeAsync(X, c->stream);
