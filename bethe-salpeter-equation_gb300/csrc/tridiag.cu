@@ -278,27 +278,30 @@ constexpr int kSegMax = 8;
 constexpr int kPassUnroll = 16;
 
 // Shared-memory footprint of tridiag_fused_kernel: reduction scratch, the alpha slot, the
-// pending reflector v, the pending w = p + alpha v, the new column / reflector, and y.
+// pending reflector v, the pending w = p + alpha v, the new column / reflector, y, and the
+// per-segment column sums of the block's columns.
 template <typename T2>
-size_t fused_smem(int n, bool with_y) {
-    return 1056 + (size_t)(with_y ? 4 : 3) * n * sizeof(T2);
+size_t fused_smem(int n, bool with_y, int blocks) {
+    return 1056 + (size_t)(with_y ? 4 : 3) * n * sizeof(T2) + (size_t)kSegMax * ((n + blocks - 1) / blocks) * sizeof(T2);
 }
 
 // One-stage reduction with the working vectors in shared memory (one grid barrier per
 // reflector).  Same algorithm and storage as tridiag_kernel's redundant mode; what changes is
-// where the vectors live and how the latency of each step is hidden:
-//  A. every block reads column k once, applies the pending rank-2 update and keeps the result
-//     in shared memory (it is both the reflector's source and, scaled, the new v);
-//  B. the block's share of the trailing columns is split into (column, row segment) items so
+// where the vectors live and how the latency of each step is hidden.  Iteration k:
+//  1. after the barrier, one round of loads per thread (no dependent loads): the column sums
+//     p_{k-1} = tau A^H v_{k-1} of reflector k-1 and the raw column k.  Every block then forms
+//     alpha_{k-1}, w_{k-1} = p + alpha v and y <- H_{k-1}^H y, applies the pending rank-2
+//     update of reflector k-1 to column k and builds reflector k, all in shared memory;
+//  2. the block's share of the trailing columns is split into (column, row segment) items so
 //     that every warp has work, and each lane keeps 16 loads of its column in flight; the
-//     partial column sums of A^H v go to a double-buffered global array;
-//  C. after the barrier every block sums the partials of all columns, forms p, alpha, w and
-//     y <- H_k^H y in shared memory.
-// v, w and y never go through global memory, so a step costs one read of column k, the pass,
-// the barrier and one read of the partial sums.
+//     segment sums of a column are added in a fixed order in shared memory and published as
+//     one value per column (double-buffered by reflector parity);
+//  3. grid barrier.
+// Block 0 stores reflector k-1 into column k-1 in iteration k, when no block reads it any more.
 template <typename T2>
 __global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
     typedef typename Real<T2>::t R;
+    constexpr int JB = 8;   // columns per thread and load round after the barrier
     extern __shared__ unsigned char smraw[];
     R* red = reinterpret_cast<R*>(smraw);                                // 4 x 32 R (1024 bytes reserved)
     T2* s_alpha = reinterpret_cast<T2*>(smraw + 1024);
@@ -310,39 +313,83 @@ __global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
     T2* sW = sV + n;
     T2* sX = sW + n;
     T2* sY = a.y ? sX + n : nullptr;
+    T2* sSeg = sX + (a.y ? 2 : 1) * (size_t)n;                           // [kSegMax][ceil(n / B)]
+    const int cstride = (n + B - 1) / B;
     const T2 zero = C2<T2>(0, 0), one = C2<T2>(1, 0);
     for (int r = tid; r < n; r += nthr) {
         sV[r] = zero;
         sW[r] = zero;
+        sX[r] = zero;
         if (sY) sY[r] = a.y[r];
     }
     __syncthreads();
-    for (int k = 0; k <= n - 2; k++) {
-        const int m = n - (k + 1);
-        const bool have_prev = k > 0;
-        const T2 vkk = sV[k], wkk = sW[k];
-        // ---- A: column k with the pending update of reflector k-1 ----
-        R loc[1] = {0};
-        for (int r0 = k + 1 + tid; r0 < n; r0 += 4 * nthr) {
-            T2 x[4];
+    T2 tau_prev = zero;
+    for (int k = 0; k < n; k++) {
+        const bool has_c = k >= 1, has_a = k <= n - 2;
+        const T2* pin = a.ppart + (size_t)((k + 1) & 1) * n;             // column sums of reflector k-1
+        // ---- 1a. loads: p_{k-1} (pre-tau column sums) and the raw column k, rows/columns i >= k ----
+        R acc[4] = {0, 0, 0, 0};
+        const T2 pk_raw = has_c ? pin[k] : zero;
+        for (int i0 = k + tid; i0 < n; i0 += JB * nthr) {
+            T2 raw[JB], ps[JB];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int r = r0 + u * nthr;
-                x[u] = r < n ? A[r + (int64_t)k * lda] : zero;
+            for (int u = 0; u < JB; u++) {
+                const int i = i0 + u * nthr;
+                raw[u] = i < n ? A[i + (int64_t)k * lda] : zero;
+                ps[u] = (has_c && i < n) ? pin[i] : zero;
             }
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int r = r0 + u * nthr;
-                if (r < n) {
-                    const T2 xv = csub(csub(x[u], cmulc(sV[r], wkk)), cmulc(sW[r], vkk));
-                    sX[r] = xv;
-                    if (r == k + 1) *s_alpha = xv;
-                    else loc[0] += xv.x * xv.x + xv.y * xv.y;
+            for (int u = 0; u < JB; u++) {
+                const int i = i0 + u * nthr;
+                if (i < n) {
+                    sV[i] = raw[u];                                        // v_{k-2} is no longer needed
+                    if (has_c) {
+                        const T2 p = cmul(tau_prev, ps[u]);
+                        const T2 v = sX[i];
+                        sW[i] = p;                                         // w_{k-2} is no longer needed
+                        const T2 q = cconjmul(p, v);
+                        acc[0] += q.x;
+                        acc[1] += q.y;
+                        if (sY) {
+                            const T2 t = cconjmul(v, sY[i]);
+                            acc[2] += t.x;
+                            acc[3] += t.y;
+                        }
+                    }
                 }
             }
         }
-        R dk = 0;
-        if (b == 0 && tid == 0) dk = csub(csub(A[k + (int64_t)k * lda], cmulc(vkk, wkk)), cmulc(wkk, vkk)).x;
+        // ---- 1b. alpha_{k-1}, w_{k-1}, y <- H_{k-1}^H y, pending update of column k ----
+        T2 alpha_c = zero, coef = zero, wkk = zero;
+        const T2 vkk = sX[k];
+        if (has_c) {
+            block_sums<R, 4>(acc, red);
+            alpha_c = cmul(C2<T2>(-0.5 * tau_prev.x, -0.5 * tau_prev.y), C2<T2>(acc[0], acc[1]));
+            coef = cmulc(C2<T2>(acc[2], acc[3]), tau_prev);                // conj(tau) (v^H y)
+            wkk = cadd(cmul(tau_prev, pk_raw), cmul(alpha_c, vkk));
+        }
+        R loc[1] = {0};
+        for (int i = k + tid; i < n; i += nthr) {
+            const T2 v = sX[i];
+            T2 w = zero;
+            if (has_c) {
+                w = cadd(sW[i], cmul(alpha_c, v));
+                sW[i] = w;
+                if (sY) sY[i] = csub(sY[i], cmul(coef, v));
+                if (b == 0 && i >= k + 1) A[i + (int64_t)(k - 1) * lda] = v;
+            }
+            const T2 xv = csub(csub(sV[i], cmulc(v, wkk)), cmulc(w, vkk));
+            sV[i] = xv;
+            if (i == k) {
+                if (b == 0) a.d[k] = xv.x;
+            } else if (i == k + 1) {
+                *s_alpha = xv;
+            } else {
+                loc[0] += xv.x * xv.x + xv.y * xv.y;
+            }
+        }
+        if (!has_a) break;
+        // ---- 1c. reflector k ----
         block_sums<R, 1>(loc, red);
         const R xnorm2 = loc[0];
         const T2 alpha = *s_alpha;
@@ -358,28 +405,32 @@ __global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
             scal = cinv(csub(alpha, C2<T2>(beta, 0)));
         }
         if (b == 0 && tid == 0) {
-            a.d[k] = dk;
             a.e[k] = beta;
             a.tau[k] = tauk;
         }
-        // v_k in place (each thread rescales the rows it wrote)
-        for (int r = k + 1 + tid; r < n; r += nthr) sX[r] = r == k + 1 ? one : cmul(sX[r], scal);
+        for (int i = k + 1 + ((tid + nthr - 1) % nthr); i < n; i += nthr) sV[i] = i == k + 1 ? one : cmul(sV[i], scal);
         __syncthreads();
-        // ---- B: pending update of this block's trailing columns, partial sums of A^H v_k ----
+        {
+            T2* t = sV;   // sV <- v_{k-1}, sX <- v_k
+            sV = sX;
+            sX = t;
+        }
+        tau_prev = tauk;
+        // ---- 2. pending update of this block's trailing columns, column sums of A^H v_k ----
+        const int m = n - (k + 1);
+        const bool have_prev = k > 0;
         const int c_lo = k + 1 + (int)((int64_t)m * b / B), c_hi = k + 1 + (int)((int64_t)m * (b + 1) / B);
         const int ncols = c_hi - c_lo;
         const int cmax = (m + B - 1) / B;
-        // segments per column: fewest sequential rounds of kPassUnroll loads per warp (same on
-        // every block, since the partial sums of all blocks are added in phase C)
+        // segments per column: fewest sequential rounds of kPassUnroll loads per warp
         int nseg = 1, best = 1 << 30;
         for (int g = 1; g <= kSegMax && (g == 1 || (m + g - 1) / g >= 32); g++) {
             const int rounds = ((cmax * g + nwarp - 1) / nwarp) * (((m + g - 1) / g + 32 * kPassUnroll - 1) / (32 * kPassUnroll));
             if (rounds < best) { best = rounds; nseg = g; }
         }
         const int L = (m + nseg - 1) / nseg;
-        T2* pout = a.ppart + (size_t)(k & 1) * kSegMax * n;
         for (int it = warp; it < ncols * nseg; it += nwarp) {
-            const int c = c_lo + it % ncols, g = it / ncols;
+            const int cl = it % ncols, g = it / ncols, c = c_lo + cl;
             const int r0 = k + 1 + g * L, r1 = min(n, r0 + L);
             const T2 vc = sV[c], wc = sW[c];
             T2* col = A + (int64_t)c * lda;
@@ -405,67 +456,21 @@ __global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
             }
             ax = warp_sum(ax);
             ay = warp_sum(ay);
-            if (lane == 0) pout[(size_t)g * n + c] = C2<T2>(ax, ay);
-        }
-        if (!grid_barrier(a.bar, a.err)) return;
-        // ---- C: p_k = tau A^H v_k, alpha_k, w_k = p_k + alpha_k v_k, y <- H_k^H y ----
-        // reflector k-1 goes to column k-1 (read by nobody any more); column k is still the
-        // source of d_k / e_k only through shared memory
-        if (b == 0 && k >= 1)
-            for (int r = k + 1 + tid; r < n; r += nthr) A[r + (int64_t)(k - 1) * lda] = sV[r];
-        R acc[4] = {0, 0, 0, 0};
-        for (int c0 = k + 1 + tid; c0 < n; c0 += 4 * nthr) {
-            T2 sum[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int c = c0 + u * nthr;
-                sum[u] = zero;
-                if (c < n)
-                    for (int g = 0; g < nseg; g++) sum[u] = cadd(sum[u], pout[(size_t)g * n + c]);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int c = c0 + u * nthr;
-                if (c < n) {
-                    const T2 p = cmul(tauk, sum[u]);
-                    const T2 v = sX[c];
-                    sW[c] = p;
-                    const T2 q = cconjmul(p, v);
-                    acc[0] += q.x;
-                    acc[1] += q.y;
-                    if (sY) {
-                        const T2 t = cconjmul(v, sY[c]);
-                        acc[2] += t.x;
-                        acc[3] += t.y;
-                    }
-                }
-            }
-        }
-        block_sums<R, 4>(acc, red);
-        const T2 alpha_k = cmul(C2<T2>(-0.5 * tauk.x, -0.5 * tauk.y), C2<T2>(acc[0], acc[1]));
-        const T2 coef = cmulc(C2<T2>(acc[2], acc[3]), tauk);   // conj(tau) (v^H y)
-        for (int c = k + 1 + tid; c < n; c += nthr) {
-            const T2 v = sX[c];
-            sW[c] = cadd(sW[c], cmul(alpha_k, v));
-            if (sY) sY[c] = csub(sY[c], cmul(coef, v));
+            if (lane == 0) sSeg[(size_t)g * cstride + cl] = C2<T2>(ax, ay);
         }
         __syncthreads();
-        T2* t = sV;
-        sV = sX;
-        sX = t;
-    }
-    if (b == 0) {
-        if (tid == 0) {
-            if (n >= 2) {
-                const T2 v = sV[n - 1], w = sW[n - 1];
-                a.d[n - 1] = csub(csub(A[(n - 1) + (int64_t)(n - 1) * lda], cmulc(v, w)), cmulc(w, v)).x;
-            } else {
-                a.d[0] = A[0].x;
-            }
+        T2* pout = a.ppart + (size_t)(k & 1) * n;
+        for (int cl = tid; cl < ncols; cl += nthr) {
+            T2 sum = zero;
+            for (int g = 0; g < nseg; g++) sum = cadd(sum, sSeg[(size_t)g * cstride + cl]);
+            pout[c_lo + cl] = sum;
         }
-        if (sY)
-            for (int r = tid; r < n; r += nthr) a.y[r] = sY[r];
+        // ---- 3. ----
+        if (!grid_barrier(a.bar, a.err)) return;
     }
+    __syncthreads();   // the last update of y was made by other threads
+    if (b == 0 && sY)
+        for (int r = tid; r < n; r += nthr) a.y[r] = sY[r];
 }
 
 // Sturm count: number of eigenvalues of T (diag d, squared off-diagonal e2) that are <= x.
@@ -1542,18 +1547,18 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const size_t fused_max = optin > 2048 ? (size_t)optin - 1024 : 0;   // room for the barrier's static word
     bool redundant = n <= 8192;
     bool two_stage = n > kTwoStageMin;
-    bool fused = !two_stage && fused_smem<T2>(n, rho0 != nullptr) <= fused_max;
+    bool fused = !two_stage && fused_smem<T2>(n, rho0 != nullptr, B) <= fused_max;
     if (const char* mode = std::getenv("BSE_TRIDIAG_MODE")) {
         const std::string md(mode);
         if (md == "shared") redundant = two_stage = fused = false;
         else if (md == "redundant") { redundant = true; two_stage = fused = false; }
         else if (md == "twostage") { redundant = fused = false; two_stage = n >= 3; }
-        else if (md == "fused" && fused_smem<T2>(n, rho0 != nullptr) <= fused_max) { fused = true; two_stage = false; }
+        else if (md == "fused" && fused_smem<T2>(n, rho0 != nullptr, B) <= fused_max) { fused = true; two_stage = false; }
     }
     if (two_stage || fused) redundant = false;
     const size_t nbuf = (two_stage || fused) ? 0 : (redundant ? (size_t)B : 2);
     const size_t o_v = carve(nbuf * n * sizeof(T2)), o_p = carve(nbuf * n * sizeof(T2));
-    const int64_t ppstride = (int64_t)(fused ? kSegMax : nt_max) * n;
+    const int64_t ppstride = (int64_t)(fused ? 1 : nt_max) * n;
     const size_t o_pp = carve(two_stage ? 0 : 2 * (size_t)ppstride * sizeof(T2)), o_dp = carve(2 * (size_t)B * sizeof(T2));
     const size_t o_y = carve((redundant ? (size_t)B : 1) * n * sizeof(T2)), o_bar = carve(64);
     const size_t o_band = carve(two_stage ? band_workspace(n, fp64, n_vec > 0, n_vec, nsm) : 0);
@@ -1599,11 +1604,11 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             fused_err = cudaFuncSetAttribute(tridiag_fused_kernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_max);
         });
         if ((st = cuda_check(c, fused_err, "fused tridiagonal smem"))) return st;
-        const size_t fsm = fused_smem<T2>(n, y != nullptr);
+        const size_t fsm = fused_smem<T2>(n, y != nullptr, B);
         int fper = 0;
         if ((st = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, tridiag_fused_kernel<T2>, threads, fsm), "occupancy"))) return st;
-        if (fper < 1) return fail(c, BSE_ERR_CUDA, "fused tridiagonal kernel does not fit on an SM");
-        const int FB = std::min(B, nsm * fper);
+        if (fper < 1 || B > nsm * fper) return fail(c, BSE_ERR_CUDA, "fused tridiagonal kernel does not fit on the GPU");
+        const int FB = B;
         if ((st = cuda_check(c, cudaLaunchCooperativeKernel((void*)tridiag_fused_kernel<T2>, dim3(FB), dim3(threads), kargs, fsm,
                                                             c->stream), "tridiagonal kernel launch"))) return st;
         c->launches++;
