@@ -61,6 +61,7 @@ struct bse_ctx {
     cusolverDnHandle_t cusolver = nullptr;
     cudaEvent_t ev[2 * bse::kStages] = {};
     double stage_ms[bse::kStages] = {};
+    int stage_mute = 0;          // >0: stage timers untouched (nested solves)
     int64_t launches = 0;
     std::string err;
 
@@ -130,11 +131,13 @@ int run_refine(bse_ctx* c);
 int run_oscillators(bse_ctx* c);
 int run_eps(bse_ctx* c, const double* omega, int n_omega, double gamma, double* eps2, double* eps1);
 
-// own dense eigensolver (eigensolve.cu)
+// own dense eigensolver (tridiag.cu)
 // Eigenvalues of the Hermitian n x n matrix dA (full storage) into dW; the first n_vec
 // eigenvectors overwrite dA's first columns; with rho0 given, f_out[l] = rho0^H x_l for all l.
+// nested: a small solve inside another stage (the refinement's projected matrix): its own
+// stream-ordered workspace instead of the context arena, no stage timers, no diagnostics.
 int own_heevd(bse_ctx* c, int n, void* dA, int lda, bool fp64, double* dW, int n_vec, const double2* rho0,
-              double2* f_out);
+              double2* f_out, bool nested = false);
 
 // two-stage reduction (band.cu): dense -> band -> real tridiagonal (d, e), y <- Q^H y; with keep_q the
 // reflectors stay in ws for band_backtransform (X = Q Z, Z real n x n_vec).  bar/err: barrier words.

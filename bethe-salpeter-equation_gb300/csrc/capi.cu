@@ -51,8 +51,11 @@ int ensure_work(bse_ctx* c, size_t bytes) {
     return BSE_OK;
 }
 
-void stage_begin(bse_ctx* c, int s) { cudaEventRecord(c->ev[2 * s], c->stream); }
+void stage_begin(bse_ctx* c, int s) {
+    if (!c->stage_mute) cudaEventRecord(c->ev[2 * s], c->stream);
+}
 void stage_end(bse_ctx* c, int s) {
+    if (c->stage_mute) return;
     cudaEventRecord(c->ev[2 * s + 1], c->stream);
     c->stage_ms[s] = -1.0;   // resolved lazily in bse_stage_times
 }

@@ -10,6 +10,9 @@
 // used as the FP64 GPU baseline).  In BSE_MIXED the solve runs on the complex64 matrix
 // and the lowest n_refine eigenpairs are then refined in FP64 by one Rayleigh-Ritz step
 // on the FP64 matrix (Cholesky-QR orthonormalisation, H*X, projected m x m solve).
+#include <cstdlib>
+#include <string>
+
 #include "bse_internal.h"
 
 namespace bse {
@@ -24,6 +27,19 @@ __global__ void widen_kernel(int64_t n, const float2* __restrict__ a, double2* _
 __global__ void narrow_kernel(int64_t n, const double2* __restrict__ a, float2* __restrict__ b) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t < n) b[t] = make_float2((float)a[t].x, (float)a[t].y);
+}
+// Full Hermitian storage of an m x m matrix from its lower triangle (the projected matrix of the
+// refinement is formed as X^H (H X), Hermitian only up to rounding).
+__global__ void hermitize_lower_kernel(int m, double2* __restrict__ G) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)m * m) return;
+    const int i = (int)(t % m), j = (int)(t / m);   // row i, column j
+    if (i < j) {
+        const double2 l = G[j + (int64_t)i * m];
+        G[t] = make_double2(l.x, -l.y);
+    } else if (i == j) {
+        G[t].y = 0;
+    }
 }
 __global__ void f2d_kernel(int64_t n, const float* __restrict__ a, double* __restrict__ b) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -407,8 +423,22 @@ int run_refine(bse_ctx* c) {
     c->launches++;
     if ((st = cuda_check(c, cudaGetLastError(), "refinement product"))) return st;
     if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, Y, n, G, m, Pw, pcap))) return st;   // X^H Y
-    if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m,
-                                                 CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo), "heevd m"))) return st;
+    // eigenpairs of the projected matrix: this library's FP64 solver (the m x m solve is a fixed
+    // cost of every refinement; cuSOLVER's heevd spends ~8 ms on it, mostly in latency-bound
+    // reduction kernels).  BSE_REFINE_EIG=cusolver selects heevd.
+    static const bool refine_cusolver = [] {
+        const char* v = std::getenv("BSE_REFINE_EIG");
+        return v && std::string(v) == "cusolver";
+    }();
+    if (refine_cusolver) {
+        if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G,
+                                                     m, CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo),
+                                 "heevd m"))) return st;
+    } else {
+        hermitize_lower_kernel<<<(unsigned)((m * m + 255) / 256), 256, 0, c->stream>>>((int)m, G);
+        c->launches++;
+        if ((st = own_heevd(c, (int)m, G, (int)m, true, theta, (int)m, nullptr, nullptr, true))) return st;
+    }
     cusolverDnDestroyParams(prm);
     // XZ = X Z (refined Ritz vectors) and HXZ = (H X) Z; residuals r_j = HXZ_j - theta_j XZ_j
     double2* XZ = (double2*)(base + oZ);

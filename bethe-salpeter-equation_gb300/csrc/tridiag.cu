@@ -392,17 +392,33 @@ __global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
         // ---- 1c. reflector k ----
         block_sums<R, 1>(loc, red);
         const R xnorm2 = loc[0];
-        const T2 alpha = *s_alpha;
         T2 tauk, scal;
         R beta;
-        if (xnorm2 == R(0) && alpha.y == R(0)) {
-            tauk = zero;
-            beta = alpha.x;
-            scal = zero;
-        } else {
-            beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2), alpha.x);
-            tauk = C2<T2>((beta - alpha.x) / beta, -alpha.y / beta);
-            scal = cinv(csub(alpha, C2<T2>(beta, 0)));
+        // FP64 square roots and divisions are slow on this part: one thread forms the scalars
+        // and the block reads them back; FP32 blocks form them in every thread
+        const bool one_thread = sizeof(R) == 8;
+        if (!one_thread || tid == 0) {
+            const T2 alpha = *s_alpha;
+            if (xnorm2 == R(0) && alpha.y == R(0)) {
+                tauk = zero;
+                beta = alpha.x;
+                scal = zero;
+            } else {
+                beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2), alpha.x);
+                tauk = C2<T2>((beta - alpha.x) / beta, -alpha.y / beta);
+                scal = cinv(csub(alpha, C2<T2>(beta, 0)));
+            }
+            if (one_thread) {
+                s_alpha[0] = tauk;   // every thread has read alpha (block_sums synchronised after it was set)
+                s_alpha[1] = scal;
+                red[127] = beta;
+            }
+        }
+        if (one_thread) {
+            __syncthreads();
+            tauk = s_alpha[0];
+            scal = s_alpha[1];
+            beta = red[127];
         }
         if (b == 0 && tid == 0) {
             a.e[k] = beta;
@@ -1493,12 +1509,15 @@ size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 constexpr int kTwoStageMin = 8192;
 
 template <typename T2>
-int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, const double2* rho0, double2* f_out) {
+int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, const double2* rho0, double2* f_out,
+                bool nested) {
     typedef typename Real<T2>::t R;
     int st;
     int dev = c->device, nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = 512;
+    // nested FP64 solves are small and bound by FP64 instruction throughput: 4 warps per block keep
+    // the per-block work (every block forms the reflector) low
+    const int threads = nested ? 128 : 512;
     // tuning overrides (sweeps): BSE_TRIDIAG_BLOCKS (grid size) and BSE_TRIDIAG_TR (tile rows)
     int TR = std::min(4096, std::max(256, (n + 255) / 256 * 256));   // one tile for n <= 4096
     if (const char* v = std::getenv("BSE_TRIDIAG_TR")) TR = std::max(64, std::min(4096, std::atoi(v)));
@@ -1524,8 +1543,11 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     if ((st = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_kernel<T2>, threads, smem), "occupancy"))) return st;
     if (per_sm < 1) return fail(c, BSE_ERR_CUDA, "tridiagonal kernel does not fit on an SM");
     // one block per SM (16 warps of loads in flight each) once the matrix is large enough; small
-    // matrices (batched runs) use ~n/16 blocks so several models' reductions can share the GPU
+    // matrices (batched runs) use ~n/16 blocks so several models' reductions can share the GPU;
+    // a nested FP64 solve runs alone and is bound by FP64 arithmetic (slow on this part), so it
+    // spreads the trailing columns over up to one block per SM
     int B = std::max(4, std::min(nsm, n / 16));
+    if (nested) B = std::max(4, std::min(nsm, n / 2));
     if (const char* v = std::getenv("BSE_TRIDIAG_BLOCKS")) B = std::max(1, std::min(nsm * per_sm, std::atoi(v)));
     const int nt_max = (n + TR - 1) / TR;
     // inverse-iteration batch: per (eigenvalue, row) 21 bytes of FP32 scratch, plus 40 bytes of FP64
@@ -1571,8 +1593,19 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const size_t o_scr = carve(fp64 ? 5 * (size_t)n * cpad * 8 : 0), o_scr32 = carve(5 * (size_t)n * cpad * 4);
     const size_t o_piv = carve((size_t)n * cpad);
     const size_t o_z = carve((size_t)n * std::max(n_vec, 1) * sizeof(R));
-    if ((st = ensure_work(c, off))) return st;
-    char* w = (char*)c->d_work;
+    // nested solves keep the context arena (it holds the caller's buffers) and use their own
+    // stream-ordered workspace, released on every return path
+    struct StreamBuf {
+        void* p;
+        cudaStream_t s;
+        ~StreamBuf() { if (p) cudaFreeAsync(p, s); }
+    } priv{nullptr, c->stream};
+    if (nested) {
+        if ((st = cuda_check(c, cudaMallocAsync(&priv.p, off, c->stream), "nested eigensolver workspace"))) return st;
+    } else if ((st = ensure_work(c, off))) {
+        return st;
+    }
+    char* w = nested ? (char*)priv.p : (char*)c->d_work;
     R* d = (R*)(w + o_d);
     R* e = (R*)(w + o_e);
     T2* tau = (T2*)(w + o_tau);
@@ -1699,7 +1732,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         i = g1 + 1;
     }
     const int ncl = (int)cs.size();
-    c->last_clusters = ncl;
+    if (!nested) c->last_clusters = ncl;
     if ((st = cuda_check(c, cudaMemcpyAsync(cl, hcl.data(), n, cudaMemcpyHostToDevice, c->stream), "cluster flags"))) return st;
     stage_begin(c, 10);
     double2* y64 = nullptr;
@@ -1856,9 +1889,13 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
 
 }  // namespace
 
-int own_heevd(bse_ctx* c, int n, void* dA, int lda, bool fp64, double* dW, int n_vec, const double2* rho0, double2* f_out) {
-    if (fp64) return own_heevd_t<double2>(c, n, (double2*)dA, lda, dW, n_vec, rho0, f_out);
-    return own_heevd_t<float2>(c, n, (float2*)dA, lda, dW, n_vec, rho0, f_out);
+int own_heevd(bse_ctx* c, int n, void* dA, int lda, bool fp64, double* dW, int n_vec, const double2* rho0, double2* f_out,
+              bool nested) {
+    if (nested) c->stage_mute++;
+    const int st = fp64 ? own_heevd_t<double2>(c, n, (double2*)dA, lda, dW, n_vec, rho0, f_out, nested)
+                        : own_heevd_t<float2>(c, n, (float2*)dA, lda, dW, n_vec, rho0, f_out, nested);
+    if (nested) c->stage_mute--;
+    return st;
 }
 
 }  // namespace bse
