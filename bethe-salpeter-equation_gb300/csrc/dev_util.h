@@ -83,6 +83,34 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
     return s_ok != 0;
 }
 
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// All-to-all flag barrier for a cooperative launch: block b publishes `epoch` in flags[32 b]
+// (release; one flag per 128-byte line) and threads t, t + blockDim.x, ... wait until every
+// block's flag has reached it (acquire).  No atomic round trip: a block passes one flag store
+// and one poll after the last block arrives.  Epochs increase within a launch and the flags are
+// zeroed before it.  *s_fail (shared, zero at kernel start) records a timeout or another block's
+// failure; returns false then.
+__device__ __forceinline__ bool flag_barrier(unsigned* flags, unsigned epoch, int* err, int* s_fail) {
+    __syncthreads();
+    if (threadIdx.x == 0) st_release(flags + 32 * blockIdx.x, epoch);
+    for (unsigned t = threadIdx.x; t < gridDim.x; t += blockDim.x) {
+        const unsigned* f = flags + 32 * t;
+        unsigned it = 0;
+        while ((int)(ld_acquire(f) - epoch) < 0) {
+            if ((++it & 255u) == 0) {
+                if (*(volatile int*)err != 0) { *s_fail = 1; break; }
+                if (it > kSpinLimit) { atomicExch(err, 1); *s_fail = 1; break; }
+                __nanosleep(64);
+            }
+        }
+    }
+    __syncthreads();
+    return *s_fail == 0;
+}
+
 template <typename R>
 __device__ __forceinline__ R warp_sum(R v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -54,6 +54,7 @@ struct TriArgs {
     T2* dpart;                 // [2][gridDim] block partial dots (shared mode)
     T2* y;                     // Q^H applied in place: [n] shared, or [B][n] per block (may be null)
     unsigned* bar;
+    unsigned* flags;           // fused kernel: one barrier flag per block, 128 bytes apart
     int* err;
     int TR;                    // rows per tile
     int redundant;             // 1: one barrier per reflector, every block finishes p itself
@@ -316,6 +317,8 @@ __global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
     T2* sSeg = sX + (a.y ? 2 : 1) * (size_t)n;                           // [kSegMax][ceil(n / B)]
     const int cstride = (n + B - 1) / B;
     const T2 zero = C2<T2>(0, 0), one = C2<T2>(1, 0);
+    __shared__ int s_fail;
+    if (tid == 0) s_fail = 0;
     for (int r = tid; r < n; r += nthr) {
         sV[r] = zero;
         sW[r] = zero;
@@ -482,7 +485,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
             pout[c_lo + cl] = sum;
         }
         // ---- 3. ----
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!flag_barrier(a.flags, (unsigned)(k + 1), a.err, &s_fail)) return;
     }
     __syncthreads();   // the last update of y was made by other threads
     if (b == 0 && sY)
@@ -1583,6 +1586,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const int64_t ppstride = (int64_t)(fused ? 1 : nt_max) * n;
     const size_t o_pp = carve(two_stage ? 0 : 2 * (size_t)ppstride * sizeof(T2)), o_dp = carve(2 * (size_t)B * sizeof(T2));
     const size_t o_y = carve((redundant ? (size_t)B : 1) * n * sizeof(T2)), o_bar = carve(64);
+    const size_t o_flags = carve((size_t)B * 128);
     const size_t o_band = carve(two_stage ? band_workspace(n, fp64, n_vec > 0, n_vec, nsm) : 0);
     // FP32 copies padded by 8 floats: the staged sweeps copy them in 16-byte pieces
     const size_t o_dd = carve(n * 8), o_ee = carve(n * 8), o_e2 = carve(n * 8), o_df = carve((n + 8) * 4),
@@ -1611,8 +1615,10 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     T2* tau = (T2*)(w + o_tau);
     T2* y = rho0 ? (T2*)(w + o_y) : nullptr;
     unsigned* bar = (unsigned*)(w + o_bar);
+    unsigned* flags = (unsigned*)(w + o_flags);
     int* err = (int*)(w + o_bar + 16);
     if ((st = cuda_check(c, cudaMemsetAsync(bar, 0, 64, c->stream), "barrier reset"))) return st;
+    if ((st = cuda_check(c, cudaMemsetAsync(flags, 0, (size_t)B * 128, c->stream), "barrier flags reset"))) return st;
     if ((st = cuda_check(c, cudaMemsetAsync(w + o_v, 0, nbuf * n * sizeof(T2), c->stream), "v reset"))) return st;
     if ((st = cuda_check(c, cudaMemsetAsync(w + o_p, 0, nbuf * n * sizeof(T2), c->stream), "p reset"))) return st;
     if ((st = cuda_check(c, cudaMemsetAsync(tau, 0, n * sizeof(T2), c->stream), "tau reset"))) return st;
@@ -1625,7 +1631,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     TriArgs<T2> ta;
     ta.n = n; ta.A = A; ta.lda = lda; ta.d = d; ta.e = e; ta.tau = tau;
     ta.vbuf = (T2*)(w + o_v); ta.pbuf = (T2*)(w + o_p); ta.ppart = (T2*)(w + o_pp); ta.dpart = (T2*)(w + o_dp);
-    ta.y = y; ta.bar = bar; ta.err = err; ta.TR = TR; ta.redundant = redundant ? 1 : 0; ta.ppstride = ppstride;
+    ta.y = y; ta.bar = bar; ta.flags = flags; ta.err = err; ta.TR = TR; ta.redundant = redundant ? 1 : 0; ta.ppstride = ppstride;
     void* kargs[] = {&ta};
     stage_begin(c, 8);
     if (two_stage) {
