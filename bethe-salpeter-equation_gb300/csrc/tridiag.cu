@@ -554,7 +554,18 @@ __device__ __forceinline__ double start_value(unsigned i, unsigned k) {
     h ^= h >> 12;
     h *= 0x297A2D39u;
     h ^= h >> 15;
-    return 0.5 + (double)(h & 0xFFFFFF) / (double)0x1000000;   // (0.5, 1.5)
+    return 0.5 + (double)(h & 0xFFFFFF) * (1.0 / 16777216.0);   // (0.5, 1.5)
+}
+// The same value rounded to FP32 (one rounding of the exact sum, as (float)start_value), without
+// FP64 arithmetic: FP64 is slow on this part and the sweeps run one warp per SM.
+__device__ __forceinline__ float start_value32(unsigned i, unsigned k) {
+    unsigned h = i * 0x9E3779B9u ^ (k + 0x7F4A7C15u) * 0x85EBCA6Bu;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return 0.5f + (float)(h & 0xFFFFFF) * (1.0f / 16777216.0f);
 }
 
 // Sequential sweeps over per-thread vectors are latency-bound (one warp per SM on the GPU):
@@ -719,14 +730,17 @@ __device__ void tri_factor_staged(int n, const float* __restrict__ d, const floa
             ak = sd[off] - s;
             bk = n > 1 ? se[off] : 0.0f;
         }
+#pragma unroll 4
         for (int k = r0; k < r1; k++) {
             const int q = k - r0 + off;
             const float ck = se[q];
             const float anext = sd[q + 1] - s;
             const float bnext = (k + 1 < n - 1) ? se[q + 1] : 0.0f;
+            // pivots are at least `pert` in magnitude: the fast reciprocal (2 ulp) is safe, and the
+            // factor and the solves use the same stored values
             if (fabsf(ck) <= fabsf(ak)) {
                 const float u = fabsf(ak) < pert ? (ak < 0 ? -pert : pert) : ak;
-                const float r = 1.0f / u;
+                const float r = __fdividef(1.0f, u);
                 const float mult = ck * r;
                 Urw[(size_t)k * 32 + lane] = r;
                 Ubw[(size_t)k * 32 + lane] = bk;
@@ -736,7 +750,7 @@ __device__ void tri_factor_staged(int n, const float* __restrict__ d, const floa
                 ak = anext - mult * bk;
                 bk = bnext;
             } else {
-                const float r = 1.0f / ck;
+                const float r = __fdividef(1.0f, ck);
                 const float mult = ak * r;
                 Urw[(size_t)k * 32 + lane] = r;
                 Ubw[(size_t)k * 32 + lane] = anext;
@@ -783,6 +797,7 @@ __device__ float tri_solve_staged(int n, const float* __restrict__ Urw, const fl
         const float* sL = sm + (st * 4 + 0) * SRW;
         const float* sY = sm + (st * 4 + 1) * SRW;
         const signed char* sP = smp + st * SRW;
+#pragma unroll 8
         for (int k = r0; k < r1; k++) {
             const int q = (k - r0) * 32 + lane;
             const float mult = sL[q];
@@ -826,6 +841,7 @@ __device__ float tri_solve_staged(int n, const float* __restrict__ Urw, const fl
         const float* sB = sm + (st * 4 + 1) * SRW;
         const float* sD = sm + (st * 4 + 2) * SRW;
         const float* sY = sm + (st * 4 + 3) * SRW;
+#pragma unroll 8
         for (int k = r1 - 1; k >= r0; k--) {
             const int q = (k - r0) * 32 + lane;
             const float x = (sY[q] - sB[q] * x1 - sD[q] * x2) * sR[q];
@@ -876,7 +892,7 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
                                                    int i0, int count, double tnorm, const double2* __restrict__ y,
                                                    double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz,
                                                    int n_store, double* __restrict__ scr, float* __restrict__ scr32,
-                                                   signed char* __restrict__ piv, int fp64) {
+                                                   signed char* __restrict__ piv, float* __restrict__ scs, int fp64) {
     extern __shared__ float stage_sm[];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = i0 + t;
@@ -896,7 +912,8 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
     float* Y = Yw + lane;
     signed char* pv = pvw + lane;
     tri_factor_staged(n, df, ef, (float)lam0, 1.1920929e-7f * (float)fmax(tnorm, 1e-30), Urw, Ubw, Udw, Lcw, pvw, stage_sm);
-    for (int k = 0; k < n; k++) Y[(size_t)k * 32] = act ? (float)start_value(i, k) : 0.0f;
+#pragma unroll 4
+    for (int k = 0; k < n; k++) Y[(size_t)k * 32] = act ? start_value32(i, k) : 0.0f;
     __threadfence();
     __syncwarp();
     float sc = 1.0f;
@@ -907,22 +924,9 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
     if (!act) return;
     const bool keep = i < n_store;
     if (!fp64) {
-        double den = 1;
-        const double lam = tri_rq<32, 32>(n, d, e, Y, (double)sc, &den);
-        const double inv = (double)sc / sqrt(den);
-        w[i] = lam;
-        double fx = 0, fy = 0;
-        for (int k = 0; k < n; k++) {
-            if (k + 32 < n) pf_l1(Y + (size_t)(k + 32) * 32);
-            const double x = (double)Y[(size_t)k * 32] * inv;
-            if (f) {
-                const double2 yy = y[k];
-                fx += yy.x * x;
-                fy -= yy.y * x;
-            }
-            if (keep) z[(size_t)k + (size_t)i * ldz] = (TZ)x;
-        }
-        if (f) f[i] = make_double2(fx, fy);
+        // mixed path: invit_finish_kernel forms the Rayleigh quotient, f_i and z_i from Y and the
+        // scale of the last sweep, a warp per eigenvalue
+        scs[t] = sc;
         return;
     }
     double* Vr = scr + (size_t)blockIdx.x * 5 * W32 + lane;
@@ -965,6 +969,55 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
 __device__ __forceinline__ double warp_dsum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+// Mixed path, after invit_kernel: one warp per eigenvalue (lanes over rows) reads the FP32
+// vector Y from the sweep scratch and forms, in FP64, the Rayleigh quotient z^T T z / z^T z (FP32
+// bisection leaves an error of a few eps32 |T|; the quotient's is the squared residual), the norm,
+// f_i = sum_k conj(y_k) z_k from FP32 products, and stores z_i (i < n_store) with coalesced writes.
+// FP64 arithmetic is slow on this part: spread over all SMs it costs little, in the sweeps'
+// one-warp-per-SM layout it cost more than the sweeps.
+template <typename TZ>
+__global__ void __launch_bounds__(256) invit_finish_kernel(int n, const double* __restrict__ d, const double* __restrict__ e,
+                                                           const signed char* __restrict__ cl, int i0, int count,
+                                                           const float2* __restrict__ y32, const float* __restrict__ scr32,
+                                                           const float* __restrict__ scs, double* __restrict__ w,
+                                                           double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz, int n_store) {
+    const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (t >= count) return;
+    const int i = i0 + t;
+    if (cl[i]) return;
+    const size_t W32 = (size_t)n * 32;
+    const float* Y = scr32 + (size_t)(t >> 5) * 5 * W32 + 4 * W32 + (t & 31);   // row k at Y[k * 32]
+    const float sc = scs[t];
+    double num = 0, den = 0, fx = 0, fy = 0;
+    for (int k = lane; k < n; k += 32) {
+        const float xf = Y[(size_t)k * 32] * sc;
+        const double x = xf;
+        double tk = d[k] * x;
+        if (k > 0) tk += e[k - 1] * (double)(Y[(size_t)(k - 1) * 32] * sc);
+        if (k + 1 < n) tk += e[k] * (double)(Y[(size_t)(k + 1) * 32] * sc);
+        num += x * tk;
+        den += (double)(xf * xf);
+        if (y32) {
+            const float2 yy = y32[k];
+            fx += (double)(yy.x * xf);
+            fy -= (double)(yy.y * xf);
+        }
+    }
+    num = warp_sum(num);
+    den = warp_sum(den);
+    fx = warp_sum(fx);
+    fy = warp_sum(fy);
+    const double inv = 1.0 / sqrt(den);
+    if (lane == 0) {
+        w[i] = num / den;
+        if (f) f[i] = make_double2(fx * inv, fy * inv);
+    }
+    if (i < n_store) {
+        const float invf = (float)inv;
+        for (int k = lane; k < n; k += 32) z[(size_t)k + (size_t)i * ldz] = (TZ)(Y[(size_t)k * 32] * sc * invf);
+    }
 }
 
 template <typename TZ>
@@ -1361,7 +1414,7 @@ __global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, cons
     if (wid == 0) tri_factor_staged(n, df, ef, (float)sh, pert32, Urw, Ubw, Udw, Lcw, pvw, stage_sm);
     int kb, ke;
     warp_rows(n, kb, ke);
-    for (int k = kb; k < ke; k++) Y[(size_t)k * 32] = act ? (float)start_value(s0 + m, k) - 1.0f : 0.0f;
+    for (int k = kb; k < ke; k++) Y[(size_t)k * 32] = act ? start_value32(s0 + m, k) - 1.0f : 0.0f;
     __threadfence();
     __syncthreads();
     for (int it = 0; it < 3; it++) {
@@ -1595,7 +1648,7 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const size_t o_y64 = carve(n * sizeof(double2));
     const size_t cpad = (size_t)(count_max + 31) / 32 * 32;   // whole warps of scratch
     const size_t o_scr = carve(fp64 ? 5 * (size_t)n * cpad * 8 : 0), o_scr32 = carve(5 * (size_t)n * cpad * 4);
-    const size_t o_piv = carve((size_t)n * cpad);
+    const size_t o_piv = carve((size_t)n * cpad), o_scs = carve((size_t)cpad * sizeof(float));
     const size_t o_z = carve((size_t)n * std::max(n_vec, 1) * sizeof(R));
     // nested solves keep the context arena (it holds the caller's buffers) and use their own
     // stream-ordered workspace, released on every return path
@@ -1752,8 +1805,14 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         const int cnt = std::min(count_max, n - i0);
         invit_kernel<R><<<(cnt + 31) / 32, 32, kStageSmem, c->stream>>>(n, dd, ee, df, ef, dW, cl, i0, cnt, tnorm, y64, f_out, z, n,
                                                                  n_vec, (double*)(w + o_scr), (float*)(w + o_scr32),
-                                                                 (signed char*)(w + o_piv), fp64 ? 1 : 0);
+                                                                 (signed char*)(w + o_piv), (float*)(w + o_scs), fp64 ? 1 : 0);
         c->launches++;
+        if (!fp64) {
+            invit_finish_kernel<R><<<(cnt + 7) / 8, 256, 0, c->stream>>>(n, dd, ee, cl, i0, cnt, y ? (const float2*)y : nullptr,
+                                                                        (const float*)(w + o_scr32), (const float*)(w + o_scs), dW,
+                                                                        f_out, z, n, n_vec);
+            c->launches++;
+        }
     }
     stage_end(c, 10);
     if (ncl > 0) {
