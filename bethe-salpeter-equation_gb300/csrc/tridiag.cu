@@ -1370,7 +1370,7 @@ __global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, cons
                                                      const double* __restrict__ w0, double* __restrict__ w,
                                                      const int* __restrict__ cstart, const int* __restrict__ csize,
                                                      const int* __restrict__ cout, const int* __restrict__ wfirst,
-                                                     int wbase, double tnorm, const double2* __restrict__ y,
+                                                     int wbase, double tnorm, const float2* __restrict__ y,
                                                      double2* __restrict__ f, TZ* __restrict__ z, int64_t ldz,
                                                      int n_store, float* __restrict__ scr32, signed char* __restrict__ piv) {
     __shared__ double Gs[CMAX * CMAX], Rinv[CMAX * CMAX], M[CMAX * CMAX], Q[CMAX * CMAX];
@@ -1427,11 +1427,12 @@ __global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, cons
     const int blk = slo * (CMAX + 1);
     if (wid == 0 && act && lane == slo) cluster_rr(sc, Gs + blk, Rinv + blk, M + blk, Q + blk, ord + slo);
     __syncthreads();
-    // member m (lane slo + m) = Z Q[:, ord[m]] of its segment; f = y^H z
-    double qcol[CMAX];
+    // member m (lane slo + m) = Z Q[:, ord[m]] of its segment, in FP32 (Z is FP32; FP64 arithmetic
+    // is slow on this part); f = y^H z with FP64 sums of FP32 products
+    float qcol[CMAX];
     const int col = act ? slo + ord[slo + m] : 0;
 #pragma unroll
-    for (int b = 0; b < CMAX; b++) qcol[b] = (act && b >= slo && b < slo + sc) ? Q[b + col * CMAX] : 0.0;
+    for (int b = 0; b < CMAX; b++) qcol[b] = (act && b >= slo && b < slo + sc) ? (float)Q[b + col * CMAX] : 0.0f;
     const int i = s0 + m;
     const bool outp = act && i >= cout[2 * t] && i < cout[2 * t + 1];
     const bool keep = outp && i < n_store;
@@ -1444,13 +1445,13 @@ __global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, cons
         for (int q = 0; q < 16; q++) {
             const int k = k0 + q;
             if (k < ke) {
-                double v = 0;
+                float v = 0;
 #pragma unroll
-                for (int b = 0; b < CMAX; b++) v += (double)__shfl_sync(0xffffffffu, yb[q], b) * qcol[b];
+                for (int b = 0; b < CMAX; b++) v += __shfl_sync(0xffffffffu, yb[q], b) * qcol[b];
                 if (y && outp) {
-                    const double2 yy = y[k];
-                    fx += yy.x * v;
-                    fy -= yy.y * v;
+                    const float2 yy = y[k];
+                    fx += (double)(yy.x * v);
+                    fy -= (double)(yy.y * v);
                 }
                 if (keep) z[(size_t)k + (size_t)i * ldz] = (TZ)v;
             }
@@ -1873,7 +1874,8 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             cudaMemcpyAsync(dwf, wfirst.data(), wfirst.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream);
             for (int wb = 0; wb < nwarps; wb += wmax) {
                 const int nb = std::min(wmax, nwarps - wb);
-                cluster_kernel<R><<<nb, 32 * kClusterWarps, kStageSmem, c->stream>>>(n, df, ef, w0, dW, dcs, dcz, dco, dwf, wb, tnorm, y64, f_out, z, n,
+                cluster_kernel<R><<<nb, 32 * kClusterWarps, kStageSmem, c->stream>>>(n, df, ef, w0, dW, dcs, dcz, dco, dwf, wb, tnorm,
+                                                            y ? (const float2*)y : nullptr, f_out, z, n,
                                                             n_vec, (float*)(w + o_scr32), (signed char*)(w + o_piv));
                 c->launches++;
             }
