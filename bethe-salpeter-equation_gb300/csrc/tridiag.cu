@@ -737,29 +737,20 @@ __device__ void tri_factor_staged(int n, const float* __restrict__ d, const floa
             const float anext = sd[q + 1] - s;
             const float bnext = (k + 1 < n - 1) ? se[q + 1] : 0.0f;
             // pivots are at least `pert` in magnitude: the fast reciprocal (2 ulp) is safe, and the
-            // factor and the solves use the same stored values
-            if (fabsf(ck) <= fabsf(ak)) {
-                const float u = fabsf(ak) < pert ? (ak < 0 ? -pert : pert) : ak;
-                const float r = __fdividef(1.0f, u);
-                const float mult = ck * r;
-                Urw[(size_t)k * 32 + lane] = r;
-                Ubw[(size_t)k * 32 + lane] = bk;
-                Udw[(size_t)k * 32 + lane] = 0.0f;
-                Lcw[(size_t)k * 32 + lane] = mult;
-                pvw[(size_t)k * 32 + lane] = 0;
-                ak = anext - mult * bk;
-                bk = bnext;
-            } else {
-                const float r = __fdividef(1.0f, ck);
-                const float mult = ak * r;
-                Urw[(size_t)k * 32 + lane] = r;
-                Ubw[(size_t)k * 32 + lane] = anext;
-                Udw[(size_t)k * 32 + lane] = bnext;
-                Lcw[(size_t)k * 32 + lane] = mult;
-                pvw[(size_t)k * 32 + lane] = 1;
-                ak = bk - mult * anext;
-                bk = -mult * bnext;
-            }
+            // factor and the solves use the same stored values.  Both pivot choices are formed and
+            // selected (the lanes of a warp pivot differently; a branch would run both paths).
+            const bool sw = fabsf(ck) > fabsf(ak);
+            const float ua = fabsf(ak) < pert ? (ak < 0 ? -pert : pert) : ak;
+            const float r = __fdividef(1.0f, sw ? ck : ua);
+            const float mult = (sw ? ak : ck) * r;
+            Urw[(size_t)k * 32 + lane] = r;
+            Ubw[(size_t)k * 32 + lane] = sw ? anext : bk;
+            Udw[(size_t)k * 32 + lane] = sw ? bnext : 0.0f;
+            Lcw[(size_t)k * 32 + lane] = mult;
+            pvw[(size_t)k * 32 + lane] = sw ? 1 : 0;
+            const float ak_n = sw ? fmaf(-mult, anext, bk) : fmaf(-mult, bk, anext);
+            bk = sw ? -mult * bnext : bnext;
+            ak = ak_n;
         }
         __syncwarp();
     }
@@ -802,14 +793,9 @@ __device__ float tri_solve_staged(int n, const float* __restrict__ Urw, const fl
             const int q = (k - r0) * 32 + lane;
             const float mult = sL[q];
             const float ynext = sY[q] * sin;
-            float out;
-            if (sP[q] == 0) {
-                out = ycur;
-                ycur = ynext - mult * ycur;
-            } else {
-                out = ynext;
-                ycur = ycur - mult * ynext;
-            }
+            const bool sw = sP[q] != 0;   // selects, not a branch: the lanes pivot differently
+            const float out = sw ? ynext : ycur;
+            ycur = sw ? fmaf(-mult, ynext, ycur) : fmaf(-mult, ycur, ynext);
             Yw[(size_t)k * 32 + lane] = out;
         }
         __syncwarp();
