@@ -13,10 +13,17 @@
 #include <cstdlib>
 #include <string>
 
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
 #include "bse_internal.h"
+#include "dev_util.h"
 
 namespace bse {
 namespace {
+
+using namespace dev;
 
 const int kGuard = 32;   // extra Ritz vectors above n_refine so the last refined ones converge
 
@@ -253,6 +260,290 @@ int gemm_df(bse_ctx* c, bool conj_a, int M, int N, int K, const double2* A, int6
     return cuda_check(c, cudaGetLastError(), "compensated product");
 }
 
+// ---- eigenpairs of the projected pencil (S, M) by iterative refinement ----
+// S = X^H H X and M = X^H X for the FP32 Ritz vectors X: S is nearly diagonal and M nearly the
+// identity, so instead of a dense eigensolve the eigenvectors Z (Z^H M Z = I, Z^H S Z = diag)
+// are refined from Z = I by the Ogita-Aishima iteration (Ogita & Aishima, "Iterative refinement
+// for symmetric eigenvalue decomposition", Japan J. Indust. Appl. Math. 35, 2018):
+//     R = I - Z^H M Z,  T = Z^H S Z,  lambda_i = T_ii / (1 - R_ii),
+//     E_ij = (T_ij + lambda_j R_ij) / (lambda_j - lambda_i)  (different clusters),
+//     E_ij = R_ij / 2  (same cluster),  Z <- Z + Z E,
+// which converges quadratically; products in compensated FP32.  Eigenvalues closer than
+// max_ij |S_ij - d_j M_ij| / kOaEta (d = diag S / diag M) form clusters, whose blocks of T are
+// diagonalised exactly at the end (complex Jacobi, one block per cluster).  Clusters wider than
+// kOaMaxCluster, or a last correction above kOaTol, hand the pencil to the dense solver.
+constexpr int kOaMaxCluster = 8;
+constexpr double kOaEta = 0.05;
+constexpr double kOaTol = 1e-4;
+constexpr int kOaIters = 3;
+constexpr int kOaParts = 128;
+
+__device__ __forceinline__ double block_max(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
+}
+
+// d_i = Re S_ii / Re M_ii; part[block] = max_{i != j} |S_ij - M_ij d_j|^2
+__global__ void oa_coupling_kernel(int m, const double2* __restrict__ S, const double2* __restrict__ Mg, double* __restrict__ d,
+                                   double* __restrict__ part) {
+    __shared__ double red[32];
+    const int64_t len = (int64_t)m * m;
+    double mx = 0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < len; t += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % m), j = (int)(t / m);
+        const int64_t jj = j + (int64_t)j * m;
+        const double dj = S[jj].x / Mg[jj].x;
+        if (i == j) {
+            d[i] = dj;
+            continue;
+        }
+        const double rx = S[t].x - Mg[t].x * dj, ry = S[t].y - Mg[t].y * dj;
+        mx = fmax(mx, rx * rx + ry * ry);
+    }
+    mx = block_max(mx, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = mx;
+}
+
+// E from T and Q = Z^H M Z (R = I - Q); part[block] = max |E_ij|^2 over pairs in different clusters
+__global__ void oa_e_kernel(int m, const double2* __restrict__ T, const double2* __restrict__ Q, const int* __restrict__ cid,
+                            double2* __restrict__ E, double* __restrict__ part) {
+    __shared__ double red[32];
+    const int64_t len = (int64_t)m * m;
+    double mx = 0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < len; t += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % m), j = (int)(t / m);
+        const int64_t ii = i + (int64_t)i * m, jj = j + (int64_t)j * m;
+        const double rx = (i == j ? 1.0 : 0.0) - Q[t].x, ry = -Q[t].y;
+        if (cid[i] == cid[j]) {
+            E[t] = make_double2(0.5 * rx, 0.5 * ry);
+        } else {
+            const double li = T[ii].x / Q[ii].x, lj = T[jj].x / Q[jj].x;
+            const double inv = 1.0 / (lj - li);
+            const double ex = (T[t].x + lj * rx) * inv, ey = (T[t].y + lj * ry) * inv;
+            E[t] = make_double2(ex, ey);
+            mx = fmax(mx, ex * ex + ey * ey);
+        }
+    }
+    mx = block_max(mx, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = mx;
+}
+
+// Z <- Z + W, or Z <- I + W when `identity`
+__global__ void oa_add_kernel(int m, double2* __restrict__ Z, const double2* __restrict__ W, int identity) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)m * m) return;
+    double2 z = identity ? make_double2((t % m) == (t / m) ? 1.0 : 0.0, 0.0) : Z[t];
+    z.x += W[t].x;
+    z.y += W[t].y;
+    Z[t] = z;
+}
+
+__global__ void oa_theta_kernel(int m, const double2* __restrict__ T, const double2* __restrict__ Q, double* __restrict__ theta) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) theta[i] = T[i + (int64_t)i * m].x / Q[i + (int64_t)i * m].x;
+}
+
+// Cyclic complex Jacobi on a small Hermitian matrix (one thread): A <- U^H A U diagonal, V <- V U.
+// Each rotation first turns A_pq real with a phase on column q, then applies the real rotation.
+__device__ void jacobi_herm(int c, double2 (*A)[kOaMaxCluster], double2 (*V)[kOaMaxCluster]) {
+    for (int sweep = 0; sweep < 40; sweep++) {
+        double off = 0, dia = 0;
+        for (int p = 0; p < c; p++) {
+            dia += A[p][p].x * A[p][p].x;
+            for (int q = p + 1; q < c; q++) off += A[p][q].x * A[p][q].x + A[p][q].y * A[p][q].y;
+        }
+        if (off <= 1e-32 * dia || off == 0.0) break;
+        for (int p = 0; p < c; p++)
+            for (int q = p + 1; q < c; q++) {
+                const double2 b = A[p][q];
+                const double ab = sqrt(b.x * b.x + b.y * b.y);
+                if (ab == 0.0) continue;
+                const double phx = b.x / ab, phy = b.y / ab;
+                const double tau = (A[q][q].x - A[p][p].x) / (2.0 * ab);
+                const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                const double cs = 1.0 / sqrt(1.0 + tt * tt), sn = tt * cs;
+                // U_pp = cs, U_qp = -sn conj(ph), U_pq = sn, U_qq = cs conj(ph)
+                const double2 upp = make_double2(cs, 0), uqp = make_double2(-sn * phx, sn * phy);
+                const double2 upq = make_double2(sn, 0), uqq = make_double2(cs * phx, -cs * phy);
+                for (int k = 0; k < c; k++) {
+                    const double2 x = A[k][p], y = A[k][q];
+                    A[k][p] = cadd(cmul(x, upp), cmul(y, uqp));
+                    A[k][q] = cadd(cmul(x, upq), cmul(y, uqq));
+                }
+                for (int k = 0; k < c; k++) {
+                    const double2 x = A[p][k], y = A[q][k];
+                    A[p][k] = cadd(cconjmul(upp, x), cconjmul(uqp, y));
+                    A[q][k] = cadd(cconjmul(upq, x), cconjmul(uqq, y));
+                }
+                for (int k = 0; k < c; k++) {
+                    const double2 x = V[k][p], y = V[k][q];
+                    V[k][p] = cadd(cmul(x, upp), cmul(y, uqp));
+                    V[k][q] = cadd(cmul(x, upq), cmul(y, uqq));
+                }
+            }
+    }
+}
+
+// One block per cluster: diagonalise the cluster's block of T, rotate its columns of Z.
+__global__ void __launch_bounds__(256) oa_cluster_kernel(int m, const int* __restrict__ off, const int* __restrict__ idx,
+                                                         const double2* __restrict__ T, double2* __restrict__ Z,
+                                                         double* __restrict__ theta) {
+    __shared__ double2 A[kOaMaxCluster][kOaMaxCluster], V[kOaMaxCluster][kOaMaxCluster];
+    __shared__ int ix[kOaMaxCluster];
+    const int o = off[blockIdx.x], c = off[blockIdx.x + 1] - o, tid = threadIdx.x;
+    if (tid < c) ix[tid] = idx[o + tid];
+    __syncthreads();
+    for (int e = tid; e < c * c; e += blockDim.x) {
+        const int a = e % c, b = e / c;
+        const double2 u = T[ix[a] + (int64_t)ix[b] * m], w = T[ix[b] + (int64_t)ix[a] * m];
+        A[a][b] = make_double2(0.5 * (u.x + w.x), 0.5 * (u.y - w.y));
+        V[a][b] = make_double2(a == b ? 1.0 : 0.0, 0.0);
+    }
+    __syncthreads();
+    if (tid == 0) jacobi_herm(c, A, V);
+    __syncthreads();
+    if (tid < c) theta[ix[tid]] = A[tid][tid].x;
+    for (int r = tid; r < m; r += blockDim.x) {
+        double2 zr[kOaMaxCluster];
+#pragma unroll
+        for (int a = 0; a < kOaMaxCluster; a++) zr[a] = a < c ? Z[r + (int64_t)ix[a] * m] : make_double2(0, 0);
+#pragma unroll
+        for (int b = 0; b < kOaMaxCluster; b++) {
+            if (b < c) {
+                double2 acc = make_double2(0, 0);
+#pragma unroll
+                for (int a = 0; a < kOaMaxCluster; a++)
+                    if (a < c) acc = cadd(acc, cmul(zr[a], V[a][b]));
+                Z[r + (int64_t)ix[b] * m] = acc;
+            }
+        }
+    }
+}
+
+// Zo[:, j] = Z[:, perm[j]], tho[j] = th[perm[j]]
+__global__ void oa_permute_kernel(int m, const int* __restrict__ perm, const double2* __restrict__ Z, const double* __restrict__ th,
+                                  double2* __restrict__ Zo, double* __restrict__ tho) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)m * m) return;
+    const int r = (int)(t % m), j = (int)(t / m);
+    Zo[t] = Z[r + (int64_t)perm[j] * m];
+    if (r == 0) tho[j] = th[perm[j]];
+}
+
+// Host side of the refinement of the pencil (S, M) (kernels above).  ws: oa_workspace(m) bytes.
+// On return *ok tells whether Z / theta hold the eigenpairs (ascending); otherwise the caller
+// solves the pencil densely.
+size_t oa_workspace(int64_t m) { return 6 * (size_t)m * m * sizeof(double2) + (size_t)m * 64 + kOaParts * 8 + 4096; }
+
+int oa_refine(bse_ctx* c, int m, const double2* S, const double2* Mg, double2* Zout, double* theta, double2* Pw, int64_t pcap,
+              char* ws, bool* ok) {
+    int st;
+    *ok = false;
+    const size_t mm = (size_t)m * m;
+    double2* Z = (double2*)ws;
+    double2* E = Z + mm;
+    double2* Q = E + mm;
+    double2* T = Q + mm;
+    double2* W1 = T + mm;
+    double2* W2 = W1 + mm;
+    double* d = (double*)(W2 + mm);
+    double* th = d + m;
+    double* part = th + m;
+    int* cid = (int*)(part + kOaParts);
+    int* perm = cid + m;
+    int* coff = perm + m;              // cluster offsets (<= m / 2 + 1) and members (<= m)
+    int* cidx = coff + (m / 2 + 2);
+    const unsigned gm = (unsigned)((mm + 255) / 256);
+    // clusters from the diagonal and the largest coupling
+    oa_coupling_kernel<<<kOaParts, 256, 0, c->stream>>>(m, S, Mg, d, part);
+    c->launches++;
+    std::vector<double> hd(m), hp(kOaParts);
+    if ((st = cuda_check(c, cudaMemcpyAsync(hd.data(), d, m * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "pencil diagonal"))) return st;
+    if ((st = cuda_check(c, cudaMemcpyAsync(hp.data(), part, kOaParts * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "coupling"))) return st;
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "pencil diagonal"))) return st;
+    const double coup = std::sqrt(*std::max_element(hp.begin(), hp.end()));
+    for (double v : hd)
+        if (!std::isfinite(v)) return BSE_OK;
+    const double tau = coup / kOaEta;
+    std::vector<int> order(m), hcid(m), hoff, hidx;
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return hd[a] < hd[b]; });
+    int ncl = 0;
+    for (int a = 0; a < m;) {
+        int b = a + 1;
+        while (b < m && hd[order[b]] - hd[order[b - 1]] <= tau) b++;
+        if (b - a > kOaMaxCluster) return BSE_OK;   // too wide: dense solve
+        if (b - a >= 2) {
+            hoff.push_back((int)hidx.size());
+            for (int q = a; q < b; q++) hidx.push_back(order[q]);
+        }
+        for (int q = a; q < b; q++) hcid[order[q]] = ncl;
+        ncl++;
+        a = b;
+    }
+    const int nbig = (int)hoff.size();
+    hoff.push_back((int)hidx.size());
+    if ((st = cuda_check(c, cudaMemcpyAsync(cid, hcid.data(), m * sizeof(int), cudaMemcpyHostToDevice, c->stream), "clusters"))) return st;
+    if (nbig && (st = cuda_check(c, cudaMemcpyAsync(coff, hoff.data(), hoff.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream), "clusters"))) return st;
+    if (nbig && (st = cuda_check(c, cudaMemcpyAsync(cidx, hidx.data(), hidx.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream), "clusters"))) return st;
+    // iterations: the first from Z = I needs no product (T = S, Q = M)
+    for (int it = 0; it < kOaIters; it++) {
+        const double2* Tk = S;
+        const double2* Qk = Mg;
+        if (it > 0) {
+            if ((st = gemm_df(c, false, m, m, m, Mg, m, Z, m, W1, m, Pw, pcap))) return st;   // M Z
+            if ((st = gemm_df(c, true, m, m, m, Z, m, W1, m, Q, m, Pw, pcap))) return st;     // Z^H M Z
+            if ((st = gemm_df(c, false, m, m, m, S, m, Z, m, W2, m, Pw, pcap))) return st;    // S Z
+            if ((st = gemm_df(c, true, m, m, m, Z, m, W2, m, T, m, Pw, pcap))) return st;     // Z^H S Z
+            Tk = T;
+            Qk = Q;
+        }
+        oa_e_kernel<<<kOaParts, 256, 0, c->stream>>>(m, Tk, Qk, cid, E, part);
+        c->launches++;
+        if (it == 0) {
+            oa_add_kernel<<<gm, 256, 0, c->stream>>>(m, Z, E, 1);
+        } else {
+            if ((st = gemm_df(c, false, m, m, m, Z, m, E, m, W1, m, Pw, pcap))) return st;    // Z E
+            oa_add_kernel<<<gm, 256, 0, c->stream>>>(m, Z, W1, 0);
+        }
+        c->launches++;
+    }
+    // Rayleigh quotients at the final Z, cluster blocks diagonalised
+    if ((st = gemm_df(c, false, m, m, m, Mg, m, Z, m, W1, m, Pw, pcap))) return st;
+    if ((st = gemm_df(c, true, m, m, m, Z, m, W1, m, Q, m, Pw, pcap))) return st;
+    if ((st = gemm_df(c, false, m, m, m, S, m, Z, m, W2, m, Pw, pcap))) return st;
+    if ((st = gemm_df(c, true, m, m, m, Z, m, W2, m, T, m, Pw, pcap))) return st;
+    oa_theta_kernel<<<(m + 255) / 256, 256, 0, c->stream>>>(m, T, Q, th);
+    c->launches++;
+    if (nbig) {
+        oa_cluster_kernel<<<nbig, 256, 0, c->stream>>>(m, coff, cidx, T, Z, th);
+        c->launches++;
+    }
+    // the last correction (converged?) and the order of the eigenvalues
+    std::vector<double> hth(m);
+    if ((st = cuda_check(c, cudaMemcpyAsync(hp.data(), part, kOaParts * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "correction"))) return st;
+    if ((st = cuda_check(c, cudaMemcpyAsync(hth.data(), th, m * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "eigenvalues"))) return st;
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "pencil refinement"))) return st;
+    const double last = std::sqrt(*std::max_element(hp.begin(), hp.end()));
+    if (!(last <= kOaTol)) return BSE_OK;
+    for (double v : hth)
+        if (!std::isfinite(v)) return BSE_OK;
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return hth[a] < hth[b]; });
+    if ((st = cuda_check(c, cudaMemcpyAsync(perm, order.data(), m * sizeof(int), cudaMemcpyHostToDevice, c->stream), "order"))) return st;
+    oa_permute_kernel<<<gm, 256, 0, c->stream>>>(m, perm, Z, th, Zout, theta);
+    c->launches++;
+    if ((st = cuda_check(c, cudaGetLastError(), "pencil refinement"))) return st;
+    *ok = true;
+    return BSE_OK;
+}
+
 int cusolver_check(bse_ctx* c, cusolverStatus_t s, const char* what) {
     if (s == CUSOLVER_STATUS_SUCCESS) return BSE_OK;
     if (s == CUSOLVER_STATUS_ALLOC_FAILED) return fail(c, BSE_ERR_OOM, std::string(what) + ": cuSOLVER allocation failed");
@@ -368,6 +659,7 @@ int run_refine(bse_ctx* c) {
     const size_t oX = carve(n * m * sizeof(double2)), oY = carve(n * m * sizeof(double2));
     const size_t oZ = carve(n * m * sizeof(double2)), oN = carve(m * sizeof(double));
     const size_t oG = carve(m * m * sizeof(double2)), oT = carve(m * sizeof(double));
+    const size_t oGm = carve(m * m * sizeof(double2)), oZb = carve(m * m * sizeof(double2)), oOA = carve(oa_workspace(m));
     const size_t oP = carve((size_t)kMaxSplits * m * m * sizeof(double2));
     const size_t oB = c->S ? carve((size_t)n * n * sizeof(double2)) : 0;
     // potrf / heevd workspaces on top
@@ -410,40 +702,55 @@ int run_refine(bse_ctx* c) {
     const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
     cublasSetStream(c->cublas, c->stream);
     cusolverDnSetStream(c->cusolver, c->stream);
-    for (int pass = 0; pass < 1; pass++) {   // CholeskyQR: the FP32 Ritz vectors are orthonormal to ~1e-7
-        if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, X, n, G, m, Pw, pcap))) return st;   // X^H X
-        if ((st = cusolver_check(c, cusolverDnXpotrf(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G, m, CUDA_C_64F,
-                                                     dws, dws1, hws.data(), hws1, dinfo), "potrf"))) return st;
-        if ((st = cublas_check(c, cublasZtrsm(c->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
-                                              n, m, &one, (cuDoubleComplex*)G, m, (cuDoubleComplex*)X, n), "trsm"))) return st;
-    }
-    // Y = H X (Hermitian, lower triangle; compensated FP32);  G = X^H Y
+    // M = X^H X, Y = H X (Hermitian, lower triangle), S = X^H Y: products in compensated FP32
+    double2* Gm = (double2*)(base + oGm);
+    double2* Zb = (double2*)(base + oZb);
+    if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, X, n, Gm, m, Pw, pcap))) return st;   // X^H X
     hemm_df_kernel<<<dim3((unsigned)((n + HM_TM - 1) / HM_TM), (unsigned)((m + HM_TN - 1) / HM_TN)), 256, 0, c->stream>>>(
         (int)n, (int)m, H64, X, Y);
     c->launches++;
     if ((st = cuda_check(c, cudaGetLastError(), "refinement product"))) return st;
     if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, Y, n, G, m, Pw, pcap))) return st;   // X^H Y
-    // eigenpairs of the projected matrix: this library's FP64 solver (the m x m solve is a fixed
-    // cost of every refinement; cuSOLVER's heevd spends ~8 ms on it, mostly in latency-bound
-    // reduction kernels).  BSE_REFINE_EIG=cusolver selects heevd.
-    static const bool refine_cusolver = [] {
+    // eigenpairs of the pencil (S, M): iterative refinement from Z = I (the FP32 Ritz vectors nearly
+    // diagonalise it), or, for wide clusters / BSE_REFINE_EIG=cusolver|dense, a dense solve of
+    // L^{-1} S L^{-H} (M = L L^H) by this library's FP64 solver or cuSOLVER heevd
+    const int refine_mode = [] {
         const char* v = std::getenv("BSE_REFINE_EIG");
-        return v && std::string(v) == "cusolver";
+        if (!v) return 0;
+        const std::string md(v);
+        return md == "cusolver" ? 2 : (md == "dense" ? 1 : 0);
     }();
-    if (refine_cusolver) {
-        if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, G,
-                                                     m, CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo),
-                                 "heevd m"))) return st;
-    } else {
-        hermitize_lower_kernel<<<(unsigned)((m * m + 255) / 256), 256, 0, c->stream>>>((int)m, G);
-        c->launches++;
-        if ((st = own_heevd(c, (int)m, G, (int)m, true, theta, (int)m, nullptr, nullptr, true))) return st;
+    bool refined = false;
+    if (refine_mode == 0) {
+        if ((st = oa_refine(c, (int)m, G, Gm, Zb, theta, Pw, pcap, base + oOA, &refined))) return st;
+    }
+    if (!refined) {
+        if ((st = cusolver_check(c, cusolverDnXpotrf(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F, Gm, m, CUDA_C_64F,
+                                                     dws, dws1, hws.data(), hws1, dinfo), "potrf"))) return st;
+        cuDoubleComplex* L = (cuDoubleComplex*)Gm;
+        cuDoubleComplex* Gc = (cuDoubleComplex*)G;
+        if ((st = cublas_check(c, cublasZtrsm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
+                                              m, m, &one, L, m, Gc, m), "trsm"))) return st;
+        if ((st = cublas_check(c, cublasZtrsm(c->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
+                                              m, m, &one, L, m, Gc, m), "trsm"))) return st;
+        if (refine_mode == 2) {
+            if ((st = cusolver_check(c, cusolverDnXsyevd(c->cusolver, prm, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, CUDA_C_64F,
+                                                         G, m, CUDA_R_64F, theta, CUDA_C_64F, dws, dws2, hws.data(), hws2, dinfo),
+                                     "heevd m"))) return st;
+        } else {
+            hermitize_lower_kernel<<<(unsigned)((m * m + 255) / 256), 256, 0, c->stream>>>((int)m, G);
+            c->launches++;
+            if ((st = own_heevd(c, (int)m, G, (int)m, true, theta, (int)m, nullptr, nullptr, true))) return st;
+        }
+        if ((st = cublas_check(c, cublasZtrsm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
+                                              m, m, &one, L, m, Gc, m), "trsm"))) return st;
+        if ((st = cuda_check(c, cudaMemcpyAsync(Zb, G, m * m * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream), "Z"))) return st;
     }
     cusolverDnDestroyParams(prm);
     // XZ = X Z (refined Ritz vectors) and HXZ = (H X) Z; residuals r_j = HXZ_j - theta_j XZ_j
     double2* XZ = (double2*)(base + oZ);
-    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, X, n, G, m, XZ, n, Pw, pcap))) return st;   // X Z
-    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, Y, n, G, m, X, n, Pw, pcap))) return st;    // (H X) Z
+    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, X, n, Zb, m, XZ, n, Pw, pcap))) return st;   // X Z
+    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, Y, n, Zb, m, X, n, Pw, pcap))) return st;    // (H X) Z
     double* rn = (double*)(base + oN);
     residual_kernel<<<(unsigned)nref, 256, 0, c->stream>>>(n, X, XZ, theta, rn);
     c->launches++;

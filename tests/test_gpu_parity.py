@@ -243,3 +243,23 @@ def test_two_stage_repeatable_mixed(synth, gpu, monkeypatch):
     for E in runs[1:]:
         assert np.array_equal(E, runs[0])
     assert np.abs(runs[0] - E1).max() < max(1e-5, 1e-6 * np.abs(E1).max())
+
+
+def test_refinement_pencil_modes(synth, oracle, gpu, monkeypatch):
+    """The FP64 refinement's projected pencil (S, M) solved by iterative refinement from the FP32
+    Ritz vectors (default), by the dense FP64 solver, and by cuSOLVER heevd gives the same refined
+    eigenvalues (the magnetic model has exactly degenerate pairs, which form clusters)."""
+    prob = synth.magnetic4_problem(grid=12)
+    ref = oracle.solve(prob, OMEGA, GAMMA)
+    Es = {}
+    for mode in ("", "dense", "cusolver"):
+        monkeypatch.setenv("BSE_REFINE_EIG", mode)
+        with gpu.BSEContext(prob, precision=1, eig_solver=0, n_refine=64) as ctx:
+            E, e2, _ = ctx.solve(OMEGA, GAMMA)
+            diag = ctx.diagnostics()
+        assert np.abs(E[:64] - ref["E"][:64]).max() < 1e-8
+        assert np.linalg.norm(e2 - ref["eps2"]) < 1e-4 * np.linalg.norm(ref["eps2"])
+        assert diag["max_refined_residual"] < 1e-3
+        Es[mode] = E[:64]
+    assert np.abs(Es[""] - Es["dense"]).max() < 1e-10
+    assert np.abs(Es[""] - Es["cusolver"]).max() < 1e-10
