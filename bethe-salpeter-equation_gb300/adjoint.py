@@ -246,7 +246,13 @@ def backward(pm: ParamModel, prob: Problem, fwd: Dict[str, np.ndarray], omega, w
     om = torch.as_tensor(omega, dtype=torch.float64, device=dev)
     ws = torch.as_tensor(weights, dtype=torch.float64, device=dev)
     E = torch.as_tensor(fwd["E"], dtype=torch.float64, device=dev)
-    A = torch.as_tensor(fwd["A"], dtype=c128, device=dev)
+    Ah = np.asarray(fwd["A"])
+    if not Ah.flags.c_contiguous and Ah.T.flags.c_contiguous:
+        # column-major eigenvectors (the C ABI's layout, seen as a transposed view): move the
+        # contiguous buffer and transpose on the device instead of gathering 16 N^2 bytes on the host
+        A = torch.as_tensor(Ah.T, dtype=c128, device=dev).T
+    else:
+        A = torch.as_tensor(Ah, dtype=c128, device=dev)
     f = torch.as_tensor(fwd["f"], dtype=c128, device=dev)
     # ---- eps2 level ----
     g, gp = lorentz_g(E, om, ws, gamma, F)
