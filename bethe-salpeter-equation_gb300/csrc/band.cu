@@ -309,7 +309,10 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
     __shared__ T2 sx[NB];
     __shared__ T2 sred[4][NB];
     __shared__ T2 sred2[4][NB];
+    __shared__ int s_abort;
     const int tid = threadIdx.x, lane = tid & 31, wy = tid >> 5;
+    if (tid == 0) s_abort = 0;
+    __syncthreads();
     const int n = a.n;
     const T2 zero = C2<T2>(0, 0);
     T2* AB = a.AB;
@@ -321,27 +324,31 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
         for (int k = 0; k < 8; k++) L[k] = zero;
         for (int t = 0; t < Tn; t++) {
             if (s > 0) {
+                // wait (acquire) until sweep s-1 has finished step t+2; only the polling thread
+                // reads the error word, and it tells the block through shared memory
                 if (tid == 0) {
                     const int need = min(t + 3, Tp);
-                    volatile int* vp = a.prog + (s - 1);
-                    volatile int* verr = a.err;
+                    const unsigned* vp = reinterpret_cast<const unsigned*>(a.prog + (s - 1));
                     unsigned it = 0;
-                    while (*vp < need) {
-                        if (*verr != 0) break;
-                        if (++it > kSpinLimit) {
-                            atomicExch(a.err, 2);
-                            break;
+                    while ((int)ld_acquire(vp) < need) {
+                        if ((++it & 255u) == 0) {
+                            if (*(volatile int*)a.err != 0) { s_abort = 1; break; }
+                            if (it > kSpinLimit) {
+                                atomicExch(a.err, 2);
+                                s_abort = 1;
+                                break;
+                            }
+                            __nanosleep(32);
                         }
-                        __nanosleep(64);
                     }
-                    __threadfence();
                 }
                 __syncthreads();
-                if (*(volatile int*)a.err != 0) return;
+                if (s_abort) return;
             }
             const int lo = s + 1 + t * NB, len = min(NB, n - lo), hi = lo + len;
             const int len2 = max(0, min(NB, n - hi));
-            // loads of D (Hermitian, from the lower band) and of the block below
+            // loads of D (Hermitian, from the lower band), of the block below and of y, together
+            const T2 yi = (wy == 0 && a.y && lane < len) ? ld(a.y + lo + lane) : zero;
             T2 D[8], Rb[8];
 #pragma unroll
             for (int k = 0; k < 8; k++) {
@@ -412,7 +419,6 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
             }
             if (wy == 0) {
                 if (a.y) {
-                    const T2 yi = lane < len ? ld(a.y + lo + lane) : zero;
                     const T2 q = cconjmul(v, yi);
                     const T2 sy = C2<T2>(warp_sum(q.x), warp_sum(q.y));
                     if (lane < len) __stcg(a.y + lo + lane, csub(yi, cmul(ctau, cmul(sy, v))));
@@ -421,9 +427,9 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
             }
 #pragma unroll
             for (int k = 0; k < 8; k++) L[k] = Rb[k];
-            __threadfence();
+            // publish step t (release: the block's band and y stores before it)
             __syncthreads();
-            if (tid == 0) atomicExch(a.prog + s, t + 1);
+            if (tid == 0) st_release(reinterpret_cast<unsigned*>(a.prog + s), (unsigned)(t + 1));
         }
     }
 }
