@@ -91,7 +91,8 @@ struct PanelArgs {
     T2* pw;                     // [G][NB] partial v^H P
     T2* pgram;                  // [G][NB*NB + NB] partial V^H V and V^H y
     T2* bc;                     // [NB + 1] broadcast: T^H V^H y, alpha
-    unsigned* bar;
+    unsigned* flags;            // flag barrier, epochs from `epoch0` up (monotonic over the panels)
+    unsigned epoch0;
     int* err;
 };
 
@@ -110,6 +111,10 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_qr_kernel(PanelArgs<T2
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     const int g = blockIdx.x, G = gridDim.x;
     const int row0 = g * S, nr = max(0, min(S, a.m - row0));
+    __shared__ int s_fail;
+    if (tid == 0) s_fail = 0;
+    unsigned epoch = a.epoch0;
+    auto barrier = [&]() { return flag_barrier(a.flags, ++epoch, a.err, &s_fail); };
     const int kk = a.kk;
     const int64_t lda = a.lda;
     const T2 zero = C2<T2>(0, 0), one = C2<T2>(1, 0);
@@ -139,7 +144,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_qr_kernel(PanelArgs<T2
             a.pnorm[g] = C2<T2>(loc[0], 0);
             if (g == 0) a.bc[NB] = col[i];   // alpha: row i < NB <= S lies in block 0
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!barrier()) return;
         R tot[1] = {0};
         for (int q = tid; q < G; q += nthr) tot[0] += ld(a.pnorm + q).x;
         block_sums<R, 1>(tot, red);
@@ -167,7 +172,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_qr_kernel(PanelArgs<T2
             ay = warp_sum(ay);
             if (lane == 0) a.pw[(size_t)g * NB + cc] = C2<T2>(ax, ay);
         }
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!barrier()) return;
         {
             // 8 threads per column sum the block partials
             const int cc = tid >> 3, sub = tid & 7;
@@ -227,7 +232,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_qr_kernel(PanelArgs<T2
         }
         a.pgram[(size_t)g * (NB * NB + NB) + e] = C2<T2>(sx, sy);
     }
-    if (!grid_barrier(a.bar, a.err)) return;
+    if (!barrier()) return;
     if (g == 0) {
         for (int e = tid; e < NB * NB + NB; e += nthr) {
             R sx = 0, sy = 0;
@@ -266,7 +271,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_qr_kernel(PanelArgs<T2
         }
     }
     if (!a.y) return;
-    if (!grid_barrier(a.bar, a.err)) return;
+    if (!barrier()) return;
     // y <- y - V (T^H V^H y)
     for (int r = tid; r < nr; r += nthr) {
         T2 s = ys[r];
@@ -448,7 +453,10 @@ __global__ void band_diag_kernel(int n, const T2* __restrict__ AB, R* __restrict
 // A warp applies one reflector to 32 columns: lane = column, the reflector's rows in registers.
 template <typename T2>
 __global__ void __launch_bounds__(kQ2Threads, 1) apply_q2_kernel(int n, const T2* __restrict__ V2, T2* __restrict__ Z,
-                                                                 int nvec, unsigned* bar, int* err) {
+                                                                 int nvec, unsigned* flags, int* err) {
+    __shared__ int s_fail;
+    if (threadIdx.x == 0) s_fail = 0;
+    unsigned epoch = 0;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     const int nch = (nvec + 31) / 32;
@@ -477,7 +485,7 @@ __global__ void __launch_bounds__(kQ2Threads, 1) apply_q2_kernel(int n, const T2
                 if (i < len && ok) __stcg(Z + (int64_t)(lo + i) * nvec + col, csub(zr[i], cmul(vi, tw)));
             }
         }
-        if (!grid_barrier(bar, err)) return;
+        if (!flag_barrier(flags, ++epoch, err, &s_fail)) return;
     }
 }
 
@@ -511,7 +519,7 @@ int blas_check(bse_ctx* c, cublasStatus_t s, const char* what) {
 
 // Workspace of the two-stage path; the same layout is used by the reduction and the back-transform.
 struct Layout {
-    size_t vall, tall, tau, ybuf, xbuf, lr, small, pnorm, pw, pgram, bc, ab, prog, v2, zrm, total;
+    size_t vall, tall, tau, ybuf, xbuf, lr, small, pnorm, pw, pgram, bc, ab, prog, flags, v2, zrm, total;
     int npanel, gmax;
     int64_t vsize;
 };
@@ -544,6 +552,7 @@ Layout layout(int n, size_t e, bool keep_q, int gmax, int n_vec) {
     L.bc = carve((NB + 8) * e);
     L.ab = carve((size_t)LDB * n * e);
     L.prog = carve((size_t)n * sizeof(int));
+    L.flags = carve((size_t)gmax * 128);   // one barrier flag per block, 128 bytes apart
     L.v2 = carve(keep_q ? (size_t)v2_offset(n, n - 1) * e : 0);
     L.zrm = carve(keep_q ? (size_t)n * std::max(n_vec, 1) * e : 0);
     L.total = off;
@@ -613,6 +622,8 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
         }
     }
     int64_t voff = 0;
+    unsigned* flags = (unsigned*)(ws + Ly.flags);
+    if ((st = cuda_check(c, cudaMemsetAsync(flags, 0, (size_t)Ly.gmax * 128, c->stream), "barrier flags"))) return st;
     stage_begin(c, 13);
     for (int j = 0; j < Ly.npanel; j++) {
         const int c0 = j * NB, r0 = c0 + NB, m = n - r0, kk = std::min(NB, m);
@@ -630,7 +641,8 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
         pa.V = Vj; pa.T = Tj; pa.tau = taus + (size_t)j * NB;
         pa.y = y ? y + r0 : nullptr;
         pa.pnorm = (T2*)(ws + Ly.pnorm); pa.pw = (T2*)(ws + Ly.pw); pa.pgram = (T2*)(ws + Ly.pgram);
-        pa.bc = (T2*)(ws + Ly.bc); pa.bar = bar; pa.err = err;
+        pa.bc = (T2*)(ws + Ly.bc); pa.flags = flags; pa.err = err;
+        pa.epoch0 = (unsigned)j * (2 * NB + 4);   // at most 2 NB + 2 barriers per panel
         void* kargs[] = {&pa};
         if ((st = cuda_check(c, cudaLaunchCooperativeKernel((void*)panel_qr_kernel<T2>, dim3(G), dim3(kPanelThreads), kargs,
                                                             panel_smem<T2>(S), c->stream), "panel QR launch"))) return st;
@@ -708,7 +720,9 @@ int band_backtransform_t(bse_ctx* c, int n, const typename Real<T2>::t* z, int n
         if ((st = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, apply_q2_kernel<T2>, kQ2Threads, 0), "q2 occupancy"))) return st;
         const int G = nsm * std::max(1, std::min(per_sm, 1));
         const T2* V2 = (const T2*)(ws + Ly.v2);
-        void* kargs[] = {(void*)&n, (void*)&V2, (void*)&Zrm, (void*)&n_vec, (void*)&bar, (void*)&err};
+        unsigned* flags = (unsigned*)(ws + Ly.flags);
+        if ((st = cuda_check(c, cudaMemsetAsync(flags, 0, (size_t)Ly.gmax * 128, c->stream), "barrier flags"))) return st;
+        void* kargs[] = {(void*)&n, (void*)&V2, (void*)&Zrm, (void*)&n_vec, (void*)&flags, (void*)&err};
         if ((st = cuda_check(c, cudaLaunchCooperativeKernel((void*)apply_q2_kernel<T2>, dim3(G), dim3(kQ2Threads), kargs, 0,
                                                             c->stream), "Q2 launch"))) return st;
         c->launches++;
