@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_qr_kernel(PanelArgs<T2
     __shared__ int s_fail;
     if (tid == 0) s_fail = 0;
     unsigned epoch = a.epoch0;
-    auto barrier = [&]() { return flag_barrier(a.flags, ++epoch, a.err, &s_fail); };
+    auto barrier = [&]() { return flag_barrier<false>(a.flags, ++epoch, a.err, &s_fail); };
     const int kk = a.kk;
     const int64_t lda = a.lda;
     const T2 zero = C2<T2>(0, 0), one = C2<T2>(1, 0);
@@ -314,10 +314,7 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
     __shared__ T2 sx[NB];
     __shared__ T2 sred[4][NB];
     __shared__ T2 sred2[4][NB];
-    __shared__ int s_abort;
     const int tid = threadIdx.x, lane = tid & 31, wy = tid >> 5;
-    if (tid == 0) s_abort = 0;
-    __syncthreads();
     const int n = a.n;
     const T2 zero = C2<T2>(0, 0);
     T2* AB = a.AB;
@@ -329,31 +326,27 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
         for (int k = 0; k < 8; k++) L[k] = zero;
         for (int t = 0; t < Tn; t++) {
             if (s > 0) {
-                // wait (acquire) until sweep s-1 has finished step t+2; only the polling thread
-                // reads the error word, and it tells the block through shared memory
                 if (tid == 0) {
                     const int need = min(t + 3, Tp);
-                    const unsigned* vp = reinterpret_cast<const unsigned*>(a.prog + (s - 1));
+                    volatile int* vp = a.prog + (s - 1);
+                    volatile int* verr = a.err;
                     unsigned it = 0;
-                    while ((int)ld_acquire(vp) < need) {
-                        if ((++it & 255u) == 0) {
-                            if (*(volatile int*)a.err != 0) { s_abort = 1; break; }
-                            if (it > kSpinLimit) {
-                                atomicExch(a.err, 2);
-                                s_abort = 1;
-                                break;
-                            }
-                            __nanosleep(32);
+                    while (*vp < need) {
+                        if (*verr != 0) break;
+                        if (++it > kSpinLimit) {
+                            atomicExch(a.err, 2);
+                            break;
                         }
+                        __nanosleep(64);
                     }
+                    __threadfence();
                 }
                 __syncthreads();
-                if (s_abort) return;
+                if (*(volatile int*)a.err != 0) return;
             }
             const int lo = s + 1 + t * NB, len = min(NB, n - lo), hi = lo + len;
             const int len2 = max(0, min(NB, n - hi));
-            // loads of D (Hermitian, from the lower band), of the block below and of y, together
-            const T2 yi = (wy == 0 && a.y && lane < len) ? ld(a.y + lo + lane) : zero;
+            // loads of D (Hermitian, from the lower band) and of the block below
             T2 D[8], Rb[8];
 #pragma unroll
             for (int k = 0; k < 8; k++) {
@@ -424,6 +417,7 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
             }
             if (wy == 0) {
                 if (a.y) {
+                    const T2 yi = lane < len ? ld(a.y + lo + lane) : zero;
                     const T2 q = cconjmul(v, yi);
                     const T2 sy = C2<T2>(warp_sum(q.x), warp_sum(q.y));
                     if (lane < len) __stcg(a.y + lo + lane, csub(yi, cmul(ctau, cmul(sy, v))));
@@ -432,9 +426,9 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
             }
 #pragma unroll
             for (int k = 0; k < 8; k++) L[k] = Rb[k];
-            // publish step t (release: the block's band and y stores before it)
+            __threadfence();
             __syncthreads();
-            if (tid == 0) st_release(reinterpret_cast<unsigned*>(a.prog + s), (unsigned)(t + 1));
+            if (tid == 0) atomicExch(a.prog + s, t + 1);
         }
     }
 }
@@ -485,7 +479,7 @@ __global__ void __launch_bounds__(kQ2Threads, 1) apply_q2_kernel(int n, const T2
                 if (i < len && ok) __stcg(Z + (int64_t)(lo + i) * nvec + col, csub(zr[i], cmul(vi, tw)));
             }
         }
-        if (!flag_barrier(flags, ++epoch, err, &s_fail)) return;
+        if (!flag_barrier<true>(flags, ++epoch, err, &s_fail)) return;
     }
 }
 

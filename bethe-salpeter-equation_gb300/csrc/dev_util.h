@@ -88,23 +88,54 @@ __device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
 }
 
 // All-to-all flag barrier for a cooperative launch: block b publishes `epoch` in flags[32 b]
-// (release; one flag per 128-byte line) and threads t, t + blockDim.x, ... wait until every
-// block's flag has reached it (acquire).  No atomic round trip: a block passes one flag store
-// and one poll after the last block arrives.  Epochs increase within a launch and the flags are
-// zeroed before it.  *s_fail (shared, zero at kernel start) records a timeout or another block's
+// (release; one flag per 128-byte line) and the block waits until every block's flag has reached
+// it (acquire).  No atomic round trip: a block passes one flag store and one poll after the last
+// block arrives.  WIDE: thread t polls block t (fastest when the blocks arrive together); narrow:
+// warp 0 polls (lane l watches blocks l, l + 32, ... not yet seen) with a short sleep between
+// rounds, so waiting blocks do not crowd the L2 that a late block is still working in.  Epochs
+// increase within a launch (or across the launches that share the flags) and the flags are zeroed
+// before the first.  *s_fail (shared, zero at kernel start) records a timeout or another block's
 // failure; returns false then.
+template <bool WIDE>
 __device__ __forceinline__ bool flag_barrier(unsigned* flags, unsigned epoch, int* err, int* s_fail) {
     __syncthreads();
     if (threadIdx.x == 0) st_release(flags + 32 * blockIdx.x, epoch);
-    for (unsigned t = threadIdx.x; t < gridDim.x; t += blockDim.x) {
-        const unsigned* f = flags + 32 * t;
-        unsigned it = 0;
-        while ((int)(ld_acquire(f) - epoch) < 0) {
-            if ((++it & 255u) == 0) {
-                if (*(volatile int*)err != 0) { *s_fail = 1; break; }
-                if (it > kSpinLimit) { atomicExch(err, 1); *s_fail = 1; break; }
-                __nanosleep(64);
+    if (WIDE) {
+        for (unsigned t = threadIdx.x; t < gridDim.x; t += blockDim.x) {
+            const unsigned* f = flags + 32 * t;
+            unsigned it = 0;
+            while ((int)(ld_acquire(f) - epoch) < 0) {
+                if ((++it & 255u) == 0) {
+                    if (*(volatile int*)err != 0) { *s_fail = 1; break; }
+                    if (it > kSpinLimit) { atomicExch(err, 1); *s_fail = 1; break; }
+                    __nanosleep(64);
+                }
             }
+        }
+    } else if (threadIdx.x < 32) {
+        const unsigned G = gridDim.x, lane = threadIdx.x;
+        unsigned pending = 0;   // bit q: block lane + 32 q not seen yet
+        for (unsigned q = 0; lane + 32 * q < G && q < 32; q++) pending |= 1u << q;
+        unsigned it = 0;
+        while (true) {
+            unsigned still = 0;
+            for (unsigned q = 0; q < 32 && (pending >> q); q++)
+                if ((pending >> q) & 1u)
+                    if ((int)(ld_acquire(flags + 32 * (lane + 32 * q)) - epoch) < 0) still |= 1u << q;
+            pending = still;
+            if (__all_sync(0xffffffffu, pending == 0)) break;
+            if ((++it & 63u) == 0) {
+                int bad = *(volatile int*)err != 0;
+                if (it > kSpinLimit) {
+                    if (lane == 0) atomicExch(err, 1);
+                    bad = 1;
+                }
+                if (__any_sync(0xffffffffu, bad)) {
+                    if (lane == 0) *s_fail = 1;
+                    break;
+                }
+            }
+            __nanosleep(20);
         }
     }
     __syncthreads();

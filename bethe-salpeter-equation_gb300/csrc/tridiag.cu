@@ -485,7 +485,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_fused_kernel(TriArgs<T2> a) {
             pout[c_lo + cl] = sum;
         }
         // ---- 3. ----
-        if (!flag_barrier(a.flags, (unsigned)(k + 1), a.err, &s_fail)) return;
+        if (!flag_barrier<true>(a.flags, (unsigned)(k + 1), a.err, &s_fail)) return;
     }
     __syncthreads();   // the last update of y was made by other threads
     if (b == 0 && sY)
