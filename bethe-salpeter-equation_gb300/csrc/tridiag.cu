@@ -506,10 +506,28 @@ __device__ __forceinline__ int sturm(int n, const R* __restrict__ d, const R* __
     return c;
 }
 
+// The same count with the fast FP32 division (2 ulp; |q| >= pivmin keeps it in range) for the
+// mixed path, where the eigenvalues are refined afterwards (FP64 Rayleigh quotients, the FP64
+// refinement): the dependent division is the latency of every step of the recurrence.
+__device__ __forceinline__ int sturm_fast(int n, const float* __restrict__ d, const float* __restrict__ e2, float x,
+                                          float pivmin) {
+    float q = d[0] - x;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    int c = q <= 0.0f;
+#pragma unroll 4
+    for (int j = 1; j < n; j++) {
+        q = d[j] - __fdividef(e2[j - 1], q) - x;
+        if (fabsf(q) < pivmin) q = -pivmin;
+        c += q <= 0.0f;
+    }
+    return c;
+}
+
 // i-th smallest eigenvalue of T by FP32 bisection to FP32 resolution.  cl[i] = 1 marks an
 // eigenvalue whose FP32 estimate lies within `ctol` of a neighbour's (a cluster at FP32
 // resolution); those get FP64 bisection in cluster_bisect_kernel.  FP64 division is slow on
 // this part, so the FP64 work is spent only where FP32 cannot separate eigenvalues.
+template <bool FAST>
 __global__ void __launch_bounds__(256) bisect32_kernel(int n, int lp, int rounds, const float* __restrict__ df,
                                                        const float* __restrict__ e2f, float glo, float ghi, float pivminf,
                                                        double* __restrict__ w) {
@@ -528,7 +546,7 @@ __global__ void __launch_bounds__(256) bisect32_kernel(int n, int lp, int rounds
         const float x = P == 1 ? 0.5f * (a + b) : a + h * (float)(gl + 1);
         if (P == 1 ? !(x > a && x < b) : !(a + h > a && a + h < b)) done = true;
         if (__all_sync(0xffffffffu, done)) break;
-        const int cnt = done ? 0 : sturm<float>(n, df, e2f, x, pivminf);
+        const int cnt = done ? 0 : (FAST ? sturm_fast(n, df, e2f, x, pivminf) : sturm<float>(n, df, e2f, x, pivminf));
         const unsigned ball = __ballot_sync(0xffffffffu, cnt > ii);
         const unsigned mine = P == 32 ? ball : (ball >> (grp * P)) & ((1u << P) - 1u);
         if (!done) {
@@ -1736,7 +1754,10 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         const int P = 1 << lp;
         const int rounds = (int)std::ceil(40.0 / std::log2((double)P + 1.0)) + 2;
         const int64_t threads = ((int64_t)n * P + 255) / 256 * 256;
-        bisect32_kernel<<<(unsigned)(threads / 256), 256, 0, c->stream>>>(n, lp, rounds, df, e2f, (float)glo, (float)ghi, pivminf, dW);
+        if (fp64)
+            bisect32_kernel<false><<<(unsigned)(threads / 256), 256, 0, c->stream>>>(n, lp, rounds, df, e2f, (float)glo, (float)ghi, pivminf, dW);
+        else
+            bisect32_kernel<true><<<(unsigned)(threads / 256), 256, 0, c->stream>>>(n, lp, rounds, df, e2f, (float)glo, (float)ghi, pivminf, dW);
     }
     c->launches++;
     // clusters: runs of eigenvalues closer than FP32 bisection can resolve
