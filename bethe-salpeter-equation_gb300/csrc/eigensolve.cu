@@ -110,8 +110,20 @@ __device__ __forceinline__ void cmac_df(float& sr, float& tr, float& si, float& 
     ti = __fmaf_rn(h.x, x.w, __fmaf_rn(h.z, x.y, __fmaf_rn(h.y, x.z, __fmaf_rn(h.w, x.x, ti))));
 }
 
-__global__ void __launch_bounds__(256) hemm_df_kernel(int n, int m, const double2* __restrict__ H,
-                                                      const double2* __restrict__ X, double2* __restrict__ Y) {
+// In-place / out-of-place split of FP64 complex values into (re hi, im hi, re lo, im lo) FP32
+// pairs, once per operand: the products then stage tiles without FP64 arithmetic (slow on this
+// part; every element of H used to be split by each of the m / HM_TN column blocks).
+__global__ void split_df_kernel(int64_t len, const double2* in, float4* out) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < len) {
+        const double2 v = in[t];
+        out[t] = split2(v);
+    }
+}
+__device__ __forceinline__ float4 conj_split(float4 h) { return make_float4(h.x, -h.y, h.z, -h.w); }
+
+__global__ void __launch_bounds__(256) hemm_df_kernel(int n, int m, const float4* __restrict__ H,
+                                                      const float4* __restrict__ X, double2* __restrict__ Y) {
     __shared__ float4 Hs[HM_TK][HM_TM + 1];   // (re hi, im hi, re lo, im lo), [k][row]
     __shared__ float4 Xs[HM_TK][HM_TN + 1];   // [k][column]
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
@@ -124,31 +136,19 @@ __global__ void __launch_bounds__(256) hemm_df_kernel(int n, int m, const double
             // tile strictly above the diagonal: conj of the stored lower tile, read along its columns
             for (int e = tid; e < HM_TM * HM_TK; e += 256) {
                 const int jj = e % HM_TK, ii = e / HM_TK, i = i0 + ii, j = j0 + jj;
-                double2 h = make_double2(0.0, 0.0);
-                if (i < n && j < n) {
-                    h = H[j + (size_t)i * n];
-                    h.y = -h.y;
-                }
-                Hs[jj][ii] = split2(h);
+                Hs[jj][ii] = (i < n && j < n) ? conj_split(H[j + (size_t)i * n]) : make_float4(0, 0, 0, 0);
             }
         } else {
             for (int e = tid; e < HM_TM * HM_TK; e += 256) {
                 const int ii = e % HM_TM, jj = e / HM_TM, i = i0 + ii, j = j0 + jj;
-                double2 h = make_double2(0.0, 0.0);
-                if (i < n && j < n) {
-                    if (i >= j) {
-                        h = H[i + (size_t)j * n];
-                    } else {
-                        h = H[j + (size_t)i * n];
-                        h.y = -h.y;
-                    }
-                }
-                Hs[jj][ii] = split2(h);
+                float4 h = make_float4(0, 0, 0, 0);
+                if (i < n && j < n) h = i >= j ? H[i + (size_t)j * n] : conj_split(H[j + (size_t)i * n]);
+                Hs[jj][ii] = h;
             }
         }
         for (int e = tid; e < HM_TK * HM_TN; e += 256) {
             const int jj = e % HM_TK, cc = e / HM_TK, j = j0 + jj, col = c0 + cc;
-            Xs[jj][cc] = split2((j < n && col < m) ? X[j + (size_t)col * n] : make_double2(0.0, 0.0));
+            Xs[jj][cc] = (j < n && col < m) ? X[j + (size_t)col * n] : make_float4(0, 0, 0, 0);
         }
         __syncthreads();
 #pragma unroll 4
@@ -660,6 +660,7 @@ int run_refine(bse_ctx* c) {
     const size_t oZ = carve(n * m * sizeof(double2)), oN = carve(m * sizeof(double));
     const size_t oG = carve(m * m * sizeof(double2)), oT = carve(m * sizeof(double));
     const size_t oGm = carve(m * m * sizeof(double2)), oZb = carve(m * m * sizeof(double2)), oOA = carve(oa_workspace(m));
+    const size_t oXs = carve(n * m * sizeof(float4));
     const size_t oP = carve((size_t)kMaxSplits * m * m * sizeof(double2));
     const size_t oB = c->S ? carve((size_t)n * n * sizeof(double2)) : 0;
     // potrf / heevd workspaces on top
@@ -706,8 +707,14 @@ int run_refine(bse_ctx* c) {
     double2* Gm = (double2*)(base + oGm);
     double2* Zb = (double2*)(base + oZb);
     if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, X, n, Gm, m, Pw, pcap))) return st;   // X^H X
+    // split H (in place: the FP64 copy is rebuilt by every build) and X into FP32 pairs once
+    float4* H4 = reinterpret_cast<float4*>(H64);
+    float4* X4 = (float4*)(base + oXs);
+    split_df_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, c->stream>>>(n * n, H64, H4);
+    split_df_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, c->stream>>>(n * m, X, X4);
+    c->launches += 2;
     hemm_df_kernel<<<dim3((unsigned)((n + HM_TM - 1) / HM_TM), (unsigned)((m + HM_TN - 1) / HM_TN)), 256, 0, c->stream>>>(
-        (int)n, (int)m, H64, X, Y);
+        (int)n, (int)m, H4, X4, Y);
     c->launches++;
     if ((st = cuda_check(c, cudaGetLastError(), "refinement product"))) return st;
     if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, Y, n, G, m, Pw, pcap))) return st;   // X^H Y
