@@ -170,9 +170,19 @@ __global__ void __launch_bounds__(256) hemm_df_kernel(int n, int m, const float4
 // C = op(A) B (op = identity or conjugate transpose; A, B FP64, column-major) in the same
 // compensated FP32 arithmetic, split over K: block z writes the partial product over its K range
 // to C + z * split_stride, and sum_splits_kernel adds the partials in FP64.
-template <bool CONJ_A>
-__global__ void __launch_bounds__(256) gemm_df_kernel(int M, int N, int K, int kchunk, const double2* __restrict__ A,
-                                                      int64_t lda, const double2* __restrict__ B, int64_t ldb,
+// operands are FP64 (split per tile) or already split into FP32 pairs (split_df_kernel)
+__device__ __forceinline__ float4 ld_split(const double2* p) { return split2(*p); }
+__device__ __forceinline__ float4 ld_split(const float4* p) { return *p; }
+__device__ __forceinline__ float4 ld_split_conj(const double2* p) {
+    double2 v = *p;
+    v.y = -v.y;
+    return split2(v);
+}
+__device__ __forceinline__ float4 ld_split_conj(const float4* p) { return conj_split(*p); }
+
+template <bool CONJ_A, typename TA, typename TB>
+__global__ void __launch_bounds__(256) gemm_df_kernel(int M, int N, int K, int kchunk, const TA* __restrict__ A,
+                                                      int64_t lda, const TB* __restrict__ B, int64_t ldb,
                                                       double2* __restrict__ C, int64_t ldc, int64_t split_stride) {
     __shared__ float4 As[HM_TK][HM_TM + 1];
     __shared__ float4 Bs[HM_TK][HM_TN + 1];
@@ -186,22 +196,17 @@ __global__ void __launch_bounds__(256) gemm_df_kernel(int M, int N, int K, int k
         if (CONJ_A) {   // op(A)(i, k) = conj(A[k + i lda]): read along k
             for (int e = tid; e < HM_TM * HM_TK; e += 256) {
                 const int jj = e % HM_TK, ii = e / HM_TK, i = i0 + ii, k = j0 + jj;
-                double2 v = make_double2(0.0, 0.0);
-                if (i < M && k < ke) {
-                    v = A[k + (size_t)i * lda];
-                    v.y = -v.y;
-                }
-                As[jj][ii] = split2(v);
+                As[jj][ii] = (i < M && k < ke) ? ld_split_conj(A + k + (size_t)i * lda) : make_float4(0, 0, 0, 0);
             }
         } else {
             for (int e = tid; e < HM_TM * HM_TK; e += 256) {
                 const int ii = e % HM_TM, jj = e / HM_TM, i = i0 + ii, k = j0 + jj;
-                As[jj][ii] = split2((i < M && k < ke) ? A[i + (size_t)k * lda] : make_double2(0.0, 0.0));
+                As[jj][ii] = (i < M && k < ke) ? ld_split(A + i + (size_t)k * lda) : make_float4(0, 0, 0, 0);
             }
         }
         for (int e = tid; e < HM_TK * HM_TN; e += 256) {
             const int jj = e % HM_TK, cc = e / HM_TK, k = j0 + jj, col = c0 + cc;
-            Bs[jj][cc] = split2((k < ke && col < N) ? B[k + (size_t)col * ldb] : make_double2(0.0, 0.0));
+            Bs[jj][cc] = (k < ke && col < N) ? ld_split(B + k + (size_t)col * ldb) : make_float4(0, 0, 0, 0);
         }
         __syncthreads();
 #pragma unroll 4
@@ -236,7 +241,8 @@ constexpr int kMaxSplits = 16;
 
 // C (M x N, leading dimension M when split) = op(A) B; P: scratch of pcap elements for the
 // split-K partials (used when the output tiles alone would not fill the GPU).
-int gemm_df(bse_ctx* c, bool conj_a, int M, int N, int K, const double2* A, int64_t lda, const double2* B, int64_t ldb,
+template <typename TA, typename TB>
+int gemm_df(bse_ctx* c, bool conj_a, int M, int N, int K, const TA* A, int64_t lda, const TB* B, int64_t ldb,
             double2* C, int64_t ldc, double2* P, int64_t pcap) {
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
@@ -248,8 +254,8 @@ int gemm_df(bse_ctx* c, bool conj_a, int M, int N, int K, const double2* A, int6
     const dim3 grid((M + HM_TM - 1) / HM_TM, (N + HM_TN - 1) / HM_TN, splits);
     double2* out = splits > 1 ? P : C;
     const int64_t ldo = splits > 1 ? M : ldc;
-    if (conj_a) gemm_df_kernel<true><<<grid, 256, 0, c->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out, ldo, (int64_t)M * N);
-    else gemm_df_kernel<false><<<grid, 256, 0, c->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out, ldo, (int64_t)M * N);
+    if (conj_a) gemm_df_kernel<true, TA, TB><<<grid, 256, 0, c->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out, ldo, (int64_t)M * N);
+    else gemm_df_kernel<false, TA, TB><<<grid, 256, 0, c->stream>>>(M, N, K, kchunk, A, lda, B, ldb, out, ldo, (int64_t)M * N);
     c->launches++;
     if (splits > 1) {
         if (ldc != M) return fail(c, BSE_ERR_CUDA, "split product needs a packed output");
@@ -660,7 +666,7 @@ int run_refine(bse_ctx* c) {
     const size_t oZ = carve(n * m * sizeof(double2)), oN = carve(m * sizeof(double));
     const size_t oG = carve(m * m * sizeof(double2)), oT = carve(m * sizeof(double));
     const size_t oGm = carve(m * m * sizeof(double2)), oZb = carve(m * m * sizeof(double2)), oOA = carve(oa_workspace(m));
-    const size_t oXs = carve(n * m * sizeof(float4));
+    const size_t oXs = carve(n * m * sizeof(float4)), oYs = carve(n * m * sizeof(float4));
     const size_t oP = carve((size_t)kMaxSplits * m * m * sizeof(double2));
     const size_t oB = c->S ? carve((size_t)n * n * sizeof(double2)) : 0;
     // potrf / heevd workspaces on top
@@ -706,18 +712,21 @@ int run_refine(bse_ctx* c) {
     // M = X^H X, Y = H X (Hermitian, lower triangle), S = X^H Y: products in compensated FP32
     double2* Gm = (double2*)(base + oGm);
     double2* Zb = (double2*)(base + oZb);
-    if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, X, n, Gm, m, Pw, pcap))) return st;   // X^H X
     // split H (in place: the FP64 copy is rebuilt by every build) and X into FP32 pairs once
     float4* H4 = reinterpret_cast<float4*>(H64);
     float4* X4 = (float4*)(base + oXs);
     split_df_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, c->stream>>>(n * n, H64, H4);
     split_df_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, c->stream>>>(n * m, X, X4);
     c->launches += 2;
+    if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, (const float4*)X4, n, (const float4*)X4, n, Gm, m, Pw, pcap))) return st;   // X^H X
     hemm_df_kernel<<<dim3((unsigned)((n + HM_TM - 1) / HM_TM), (unsigned)((m + HM_TN - 1) / HM_TN)), 256, 0, c->stream>>>(
         (int)n, (int)m, H4, X4, Y);
     c->launches++;
     if ((st = cuda_check(c, cudaGetLastError(), "refinement product"))) return st;
-    if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, X, n, Y, n, G, m, Pw, pcap))) return st;   // X^H Y
+    float4* Y4 = (float4*)(base + oYs);
+    split_df_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, c->stream>>>(n * m, Y, Y4);
+    c->launches++;
+    if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, (const float4*)X4, n, (const float4*)Y4, n, G, m, Pw, pcap))) return st;   // X^H Y
     // eigenpairs of the pencil (S, M): iterative refinement from Z = I (the FP32 Ritz vectors nearly
     // diagonalise it), or, for wide clusters / BSE_REFINE_EIG=cusolver|dense, a dense solve of
     // L^{-1} S L^{-H} (M = L L^H) by this library's FP64 solver or cuSOLVER heevd
@@ -756,8 +765,8 @@ int run_refine(bse_ctx* c) {
     cusolverDnDestroyParams(prm);
     // XZ = X Z (refined Ritz vectors) and HXZ = (H X) Z; residuals r_j = HXZ_j - theta_j XZ_j
     double2* XZ = (double2*)(base + oZ);
-    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, X, n, Zb, m, XZ, n, Pw, pcap))) return st;   // X Z
-    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, Y, n, Zb, m, X, n, Pw, pcap))) return st;    // (H X) Z
+    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, (const float4*)X4, n, (const double2*)Zb, m, XZ, n, Pw, pcap))) return st;   // X Z
+    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, (const float4*)Y4, n, (const double2*)Zb, m, X, n, Pw, pcap))) return st;    // (H X) Z
     double* rn = (double*)(base + oN);
     residual_kernel<<<(unsigned)nref, 256, 0, c->stream>>>(n, X, XZ, theta, rn);
     c->launches++;
