@@ -445,7 +445,7 @@ __global__ void oa_permute_kernel(int m, const int* __restrict__ perm, const dou
 // Host side of the refinement of the pencil (S, M) (kernels above).  ws: oa_workspace(m) bytes.
 // On return *ok tells whether Z / theta hold the eigenpairs (ascending); otherwise the caller
 // solves the pencil densely.
-size_t oa_workspace(int64_t m) { return 6 * (size_t)m * m * sizeof(double2) + (size_t)m * 64 + kOaParts * 8 + 4096; }
+size_t oa_workspace(int64_t m) { return 9 * (size_t)m * m * sizeof(double2) + (size_t)m * 64 + kOaParts * 8 + 4096; }
 
 int oa_refine(bse_ctx* c, int m, const double2* S, const double2* Mg, double2* Zout, double* theta, double2* Pw, int64_t pcap,
               char* ws, bool* ok) {
@@ -458,7 +458,10 @@ int oa_refine(bse_ctx* c, int m, const double2* S, const double2* Mg, double2* Z
     double2* T = Q + mm;
     double2* W1 = T + mm;
     double2* W2 = W1 + mm;
-    double* d = (double*)(W2 + mm);
+    float4* S4 = (float4*)(W2 + mm);   // S, M and the current Z split into FP32 pairs
+    float4* M4 = S4 + mm;
+    float4* Z4 = M4 + mm;
+    double* d = (double*)(Z4 + mm);
     double* th = d + m;
     double* part = th + m;
     int* cid = (int*)(part + kOaParts);
@@ -498,15 +501,21 @@ int oa_refine(bse_ctx* c, int m, const double2* S, const double2* Mg, double2* Z
     if ((st = cuda_check(c, cudaMemcpyAsync(cid, hcid.data(), m * sizeof(int), cudaMemcpyHostToDevice, c->stream), "clusters"))) return st;
     if (nbig && (st = cuda_check(c, cudaMemcpyAsync(coff, hoff.data(), hoff.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream), "clusters"))) return st;
     if (nbig && (st = cuda_check(c, cudaMemcpyAsync(cidx, hidx.data(), hidx.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream), "clusters"))) return st;
+    split_df_kernel<<<gm, 256, 0, c->stream>>>((int64_t)mm, S, S4);
+    split_df_kernel<<<gm, 256, 0, c->stream>>>((int64_t)mm, Mg, M4);
+    c->launches += 2;
+    const float4* cZ4 = Z4;
     // iterations: the first from Z = I needs no product (T = S, Q = M)
     for (int it = 0; it < kOaIters; it++) {
         const double2* Tk = S;
         const double2* Qk = Mg;
         if (it > 0) {
-            if ((st = gemm_df(c, false, m, m, m, Mg, m, Z, m, W1, m, Pw, pcap))) return st;   // M Z
-            if ((st = gemm_df(c, true, m, m, m, Z, m, W1, m, Q, m, Pw, pcap))) return st;     // Z^H M Z
-            if ((st = gemm_df(c, false, m, m, m, S, m, Z, m, W2, m, Pw, pcap))) return st;    // S Z
-            if ((st = gemm_df(c, true, m, m, m, Z, m, W2, m, T, m, Pw, pcap))) return st;     // Z^H S Z
+            split_df_kernel<<<gm, 256, 0, c->stream>>>((int64_t)mm, Z, Z4);
+            c->launches++;
+            if ((st = gemm_df(c, false, m, m, m, (const float4*)M4, m, cZ4, m, W1, m, Pw, pcap))) return st;   // M Z
+            if ((st = gemm_df(c, true, m, m, m, cZ4, m, (const double2*)W1, m, Q, m, Pw, pcap))) return st;     // Z^H M Z
+            if ((st = gemm_df(c, false, m, m, m, (const float4*)S4, m, cZ4, m, W2, m, Pw, pcap))) return st;    // S Z
+            if ((st = gemm_df(c, true, m, m, m, cZ4, m, (const double2*)W2, m, T, m, Pw, pcap))) return st;     // Z^H S Z
             Tk = T;
             Qk = Q;
         }
@@ -515,16 +524,18 @@ int oa_refine(bse_ctx* c, int m, const double2* S, const double2* Mg, double2* Z
         if (it == 0) {
             oa_add_kernel<<<gm, 256, 0, c->stream>>>(m, Z, E, 1);
         } else {
-            if ((st = gemm_df(c, false, m, m, m, Z, m, E, m, W1, m, Pw, pcap))) return st;    // Z E
+            if ((st = gemm_df(c, false, m, m, m, cZ4, m, (const double2*)E, m, W1, m, Pw, pcap))) return st;    // Z E
             oa_add_kernel<<<gm, 256, 0, c->stream>>>(m, Z, W1, 0);
         }
         c->launches++;
     }
     // Rayleigh quotients at the final Z, cluster blocks diagonalised
-    if ((st = gemm_df(c, false, m, m, m, Mg, m, Z, m, W1, m, Pw, pcap))) return st;
-    if ((st = gemm_df(c, true, m, m, m, Z, m, W1, m, Q, m, Pw, pcap))) return st;
-    if ((st = gemm_df(c, false, m, m, m, S, m, Z, m, W2, m, Pw, pcap))) return st;
-    if ((st = gemm_df(c, true, m, m, m, Z, m, W2, m, T, m, Pw, pcap))) return st;
+    split_df_kernel<<<gm, 256, 0, c->stream>>>((int64_t)mm, Z, Z4);
+    c->launches++;
+    if ((st = gemm_df(c, false, m, m, m, (const float4*)M4, m, cZ4, m, W1, m, Pw, pcap))) return st;
+    if ((st = gemm_df(c, true, m, m, m, cZ4, m, (const double2*)W1, m, Q, m, Pw, pcap))) return st;
+    if ((st = gemm_df(c, false, m, m, m, (const float4*)S4, m, cZ4, m, W2, m, Pw, pcap))) return st;
+    if ((st = gemm_df(c, true, m, m, m, cZ4, m, (const double2*)W2, m, T, m, Pw, pcap))) return st;
     oa_theta_kernel<<<(m + 255) / 256, 256, 0, c->stream>>>(m, T, Q, th);
     c->launches++;
     if (nbig) {
