@@ -57,6 +57,8 @@ struct bse_ctx {
     bse::DeltaMap dmap;
     int device;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;           // concurrent work of the own solver (joined before use)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
     cudaEvent_t ev[2 * bse::kStages] = {};

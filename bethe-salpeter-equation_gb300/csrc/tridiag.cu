@@ -1801,6 +1801,54 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     const int ncl = (int)cs.size();
     if (!nested) c->last_clusters = ncl;
     if ((st = cuda_check(c, cudaMemcpyAsync(cl, hcl.data(), n, cudaMemcpyHostToDevice, c->stream), "cluster flags"))) return st;
+    // mixed path: the cluster kernel runs on the side stream while inverse iteration runs on this
+    // one (disjoint eigenvalues and outputs, its own scratch, shifts from the bisection values),
+    // when that scratch is small; otherwise it follows inverse iteration on this stream
+    bool side_clusters = false;
+    int *sdcs = nullptr, *sdcz = nullptr, *sdco = nullptr, *sdwf = nullptr;
+    double* sw0 = nullptr;
+    float* sscr = nullptr;
+    signed char* spiv = nullptr;
+    if (!fp64 && ncl > 0 && c->side) {
+        std::vector<int> wfirst(1, 0);
+        for (int q = 0, used = 0; q < ncl; q++) {
+            if (used + cz[q] > 32) {
+                wfirst.push_back(q);
+                used = 0;
+            }
+            used += cz[q];
+        }
+        wfirst.push_back(ncl);
+        const int nwarps = (int)wfirst.size() - 1;
+        const size_t W32 = (size_t)n * 32;
+        if ((size_t)nwarps * (21 * W32) <= ((size_t)256 << 20)) {
+            side_clusters = true;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&sdcs, ncl * sizeof(int), c->stream), "clusters"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&sdcz, ncl * sizeof(int), c->stream), "clusters"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&sdco, 2 * ncl * sizeof(int), c->stream), "clusters"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&sdwf, wfirst.size() * sizeof(int), c->stream), "clusters"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&sw0, n * sizeof(double), c->stream), "cluster shifts"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&sscr, (size_t)nwarps * 5 * W32 * sizeof(float), c->stream), "cluster scratch"))) return st;
+            if ((st = cuda_check(c, cudaMallocAsync((void**)&spiv, (size_t)nwarps * W32, c->stream), "cluster pivots"))) return st;
+            cudaMemcpyAsync(sdcs, cs.data(), ncl * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+            cudaMemcpyAsync(sdcz, cz.data(), ncl * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+            cudaMemcpyAsync(sdco, co.data(), 2 * ncl * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+            cudaMemcpyAsync(sdwf, wfirst.data(), wfirst.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+            cudaMemcpyAsync(sw0, dW, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+            if ((st = cuda_check(c, cudaEventRecord(c->ev_fork, c->stream), "fork"))) return st;
+            if ((st = cuda_check(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork"))) return st;
+            if (!c->stage_mute) cudaEventRecord(c->ev[2 * 12], c->side);
+            cluster_kernel<R><<<nwarps, 32 * kClusterWarps, kStageSmem, c->side>>>(n, df, ef, sw0, dW, sdcs, sdcz, sdco, sdwf, 0, tnorm,
+                                                                                 y ? (const float2*)y : nullptr, f_out, (R*)(w + o_z), n,
+                                                                                 n_vec, sscr, spiv);
+            c->launches++;
+            if (!c->stage_mute) {
+                cudaEventRecord(c->ev[2 * 12 + 1], c->side);
+                c->stage_ms[12] = -1.0;
+            }
+            if ((st = cuda_check(c, cudaEventRecord(c->ev_join, c->side), "join"))) return st;
+        }
+    }
     stage_begin(c, 10);
     double2* y64 = nullptr;
     if (y) {
@@ -1823,7 +1871,11 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
         }
     }
     stage_end(c, 10);
-    if (ncl > 0) {
+    if (side_clusters) {
+        if ((st = cuda_check(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join"))) return st;
+        for (void* p : {(void*)sdcs, (void*)sdcz, (void*)sdco, (void*)sdwf, (void*)sw0, (void*)sscr, (void*)spiv})
+            cudaFreeAsync(p, c->stream);
+    } else if (ncl > 0) {
         // the inverse-iteration scratch is free again (same stream)
         int* dcs = nullptr;
         int* dcz = nullptr;
