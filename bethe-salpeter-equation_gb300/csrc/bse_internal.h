@@ -58,7 +58,10 @@ struct bse_ctx {
     int device;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;           // concurrent work of the own solver (joined before use)
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t side2 = nullptr;          // the refinement's FP64 build, concurrent with the same phase
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_h64 = nullptr;
+    bool h64_pending = false;              // FP64 copy for the refinement still to be built
+    bool h64_side = false;                 // built on the side stream: wait for ev_h64 first
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
     cudaEvent_t ev[2 * bse::kStages] = {};
@@ -130,6 +133,10 @@ int run_tables(bse_ctx* c);
 int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out);
 int run_eig(bse_ctx* c, bool want_vectors);
 int run_refine(bse_ctx* c);
+// FP64 copy of the solved block(s) for the refinement, launched on c->stream (kernel_build.cu)
+int build_h64(bse_ctx* c);
+// launch a pending FP64 build on the side stream (after the work already on c->stream)
+int fork_h64(bse_ctx* c);
 int run_oscillators(bse_ctx* c);
 int run_eps(bse_ctx* c, const double* omega, int n_omega, double gamma, double* eps2, double* eps1);
 

@@ -201,6 +201,7 @@ void destroy_ctx(bse_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->side) cudaStreamSynchronize(c->side);
+    if (c->side2) cudaStreamSynchronize(c->side2);
     void* ptrs[] = {c->d_rcart, c->d_weights, c->d_hr, c->d_centres, c->d_k, c->d_bmat, c->d_kidx, c->d_g, c->d_status,
                     c->d_ec, c->d_ev, c->d_cc, c->d_cv, c->d_phi, c->d_phi32, c->d_X, c->d_qx, c->d_qx32, c->d_rho,
                     c->d_H, c->d_H64, c->d_blk, c->d_E, c->d_f, c->d_work};
@@ -212,7 +213,9 @@ void destroy_ctx(bse_ctx* c) {
     if (c->cusolver) cusolverDnDestroy(c->cusolver);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_h64) cudaEventDestroy(c->ev_h64);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->side2) cudaStreamDestroy(c->side2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -312,8 +315,10 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     } while (0)
     CK(cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"));
     CK(cuda_check(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "side stream"));
+    CK(cuda_check(c, cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking), "side stream"));
     CK(cuda_check(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event"));
     CK(cuda_check(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event"));
+    CK(cuda_check(c, cudaEventCreateWithFlags(&c->ev_h64, cudaEventDisableTiming), "event"));
     for (auto& e : c->ev) CK(cuda_check(c, cudaEventCreate(&e), "event"));
     if (cublasCreate(&c->cublas) != CUBLAS_STATUS_SUCCESS) CK(fail(c, BSE_ERR_CUDA, "cublasCreate"));
     if (cusolverDnCreate(&c->cusolver) != CUSOLVER_STATUS_SUCCESS) CK(fail(c, BSE_ERR_CUDA, "cusolverDnCreate"));

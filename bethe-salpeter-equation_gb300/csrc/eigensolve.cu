@@ -669,7 +669,13 @@ int run_refine(bse_ctx* c) {
     const int64_t n = c->n_opt;
     const int64_t m = std::min<int64_t>(n, (int64_t)c->p.n_refine + kGuard);
     const int64_t nref = std::min<int64_t>(n, c->p.n_refine);
-    // FP64 matrix of the solved block, lower triangle
+    // FP64 matrix of the solved block, lower triangle: built here, or waited for on the side stream
+    if (c->h64_pending) {
+        if ((st = build_h64(c))) return st;
+    } else if (c->h64_side) {
+        if ((st = cuda_check(c, cudaStreamWaitEvent(c->stream, c->ev_h64, 0), "FP64 build wait"))) return st;
+        c->h64_side = false;
+    }
     double2* H64 = c->d_H64;
     size_t off = 0;
     auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };

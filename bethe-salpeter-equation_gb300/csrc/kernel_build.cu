@@ -507,6 +507,44 @@ int run_tables(bse_ctx* c) {
     return BSE_OK;
 }
 
+int build_h64(bse_ctx* c) {
+    int st;
+    const bool coll = c->S != 0;
+    const int64_t n64 = coll ? 4 * c->N : c->N;
+    const int dd = c->p.ipa ? 0 : 1, de = c->p.ipa ? 0 : 1;
+    int pairs[6][2] = {{0, 0}, {1, 1}, {2, 2}, {3, 3}, {0, 3}, {3, 0}};
+    const int npairs = coll ? 6 : 1;
+    if ((st = cuda_check(c, cudaMemsetAsync(c->d_H64, 0, (size_t)n64 * n64 * sizeof(double2), c->stream), "H64 clear"))) return st;
+    for (int pi = 0; pi < npairs; pi++) {
+        const int br = pairs[pi][0], bc = pairs[pi][1];
+        const int direct = (br == bc) ? dd : 0;
+        const int exch = ((br == 0 || br == 3) && (bc == 0 || bc == 3)) ? de : 0;
+        if ((st = launch_build<double>(c, c->d_H64, n64, !coll, c->d_phi, c->d_qx, br, bc, direct, exch, br == bc))) return st;
+    }
+    if (coll) {
+        const int64_t nn = c->N * c->N;
+        spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, c->d_H64);
+        c->launches++;
+    }
+    c->h64_pending = false;
+    return cuda_check(c, cudaGetLastError(), "FP64 build");
+}
+
+int fork_h64(bse_ctx* c) {
+    if (!c->h64_pending || !c->side2) return BSE_OK;
+    int st;
+    if ((st = cuda_check(c, cudaEventRecord(c->ev_h64, c->stream), "fork"))) return st;
+    if ((st = cuda_check(c, cudaStreamWaitEvent(c->side2, c->ev_h64, 0), "fork"))) return st;
+    cudaStream_t main_stream = c->stream;
+    c->stream = c->side2;            // the build's launches go to the second side stream
+    st = build_h64(c);
+    c->stream = main_stream;
+    if (st) return st;
+    if ((st = cuda_check(c, cudaEventRecord(c->ev_h64, c->side2), "FP64 build done"))) return st;
+    c->h64_side = true;
+    return BSE_OK;
+}
+
 int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     int st;
     if (!c->bands_valid) return fail(c, BSE_ERR_STATE, "bands not computed");
@@ -543,22 +581,10 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     }
     stage_end(c, 2);
     if ((st = cuda_check(c, cudaGetLastError(), "build"))) return st;
-    if (mixed && !c->p.ipa && c->p.n_refine > 0) {
-        // FP64 copy of the optically active block for the Rayleigh-Ritz refinement
-        const int64_t n64 = coll ? 4 * c->N : c->N;
-        if ((st = cuda_check(c, cudaMemsetAsync(c->d_H64, 0, (size_t)n64 * n64 * sizeof(double2), c->stream), "H64 clear"))) return st;
-        for (int pi = 0; pi < npairs; pi++) {
-            const int br = pairs[pi][0], bc = pairs[pi][1];
-            const int direct = (br == bc) ? dd : 0;
-            const int exch = ((br == 0 || br == 3) && (bc == 0 || bc == 3)) ? de : 0;
-            if ((st = launch_build<double>(c, c->d_H64, n64, !coll, c->d_phi, c->d_qx, br, bc, direct, exch, br == bc))) return st;
-        }
-        if (coll) {
-            const int64_t nn = c->N * c->N;
-            spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, c->d_H64);
-            c->launches++;
-        }
-    }
+    // the FP64 copy of the optically active block for the refinement is built later (on the side
+    // stream while the FP32 eigensolve runs, or by the refinement itself)
+    c->h64_pending = mixed && !c->p.ipa && c->p.n_refine > 0;
+    c->h64_side = false;
     if (coll) {
         const int64_t n2 = 2 * c->N;
         const size_t bb = (size_t)n2 * n2 * c->h_elem;

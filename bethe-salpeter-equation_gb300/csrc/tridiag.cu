@@ -1849,6 +1849,9 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             if ((st = cuda_check(c, cudaEventRecord(c->ev_join, c->side), "join"))) return st;
         }
     }
+    // the refinement's FP64 matrix builds on a second side stream during inverse iteration and the
+    // clusters, which leave most SMs idle
+    if (!nested && (st = fork_h64(c))) return st;
     stage_begin(c, 10);
     double2* y64 = nullptr;
     if (y) {
