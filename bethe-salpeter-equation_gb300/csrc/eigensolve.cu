@@ -9,7 +9,9 @@
 // iteration (tridiag.cu); BSE_EIG_CUSOLVER calls cuSOLVER's heevd (the plain library path,
 // used as the FP64 GPU baseline).  In BSE_MIXED the solve runs on the complex64 matrix
 // and the lowest n_refine eigenpairs are then refined in FP64 by one Rayleigh-Ritz step
-// on the FP64 matrix (Cholesky-QR orthonormalisation, H*X, projected m x m solve).
+// on the FP64 matrix: the pencil (X^H H X, X^H X) of the FP32 Ritz vectors X, its products in
+// compensated FP32, solved by Ogita-Aishima iterative refinement (a dense FP64 solve of the
+// Cholesky-transformed pencil as the fallback).
 #include <cstdlib>
 #include <string>
 

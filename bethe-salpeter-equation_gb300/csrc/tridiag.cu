@@ -3,14 +3,14 @@
 // Replaces the eig_sym (LAPACK zheevd) call of common_diagonalization
 // (bse.version13.cpp:3195, 3330) with a solver shaped for what the BSE path needs:
 //
-//  1. tridiag_kernel: Householder reduction Q^H A Q = T (T real symmetric tridiagonal, the
-//     zhetd2 algorithm, lower reflectors).  One cooperative persistent kernel: for every
-//     reflector k, each block recomputes column k with the pending rank-2 update and the
-//     reflector (redundantly, no barrier), then one fused pass over the trailing matrix
-//     applies the pending update A -= v w^H + w v^H and accumulates p = tau A v for the new
-//     reflector; two grid barriers per reflector finish p and the scalar of w.  The same
-//     pass applies Q^H to the optical pair-density vector (y = Q^H rho), so oscillator
-//     strengths never need the eigenvectors of A: f_l = y^H z_l with z_l real.
+//  1. tridiag_fused_kernel (tridiag_kernel where its vectors do not fit in shared memory):
+//     Householder reduction Q^H A Q = T (T real symmetric tridiagonal, the zhetd2 algorithm,
+//     lower reflectors).  One cooperative persistent kernel: for every reflector k, each block
+//     recomputes column k with the pending rank-2 update and the reflector (redundantly, no
+//     barrier), then one fused pass over the trailing matrix applies the pending update
+//     A -= v w^H + w v^H and accumulates p = tau A v for the new reflector; one barrier per
+//     reflector.  The same steps apply Q^H to the optical pair-density vector (y = Q^H rho), so
+//     oscillator strengths never need the eigenvectors of A: f_l = y^H z_l with z_l real.
 //  2. bisect32_kernel: eigenvalues of T by FP32 Sturm-count multisection (several lanes per
 //     eigenvalue when the problem is small); runs of eigenvalues FP32 cannot separate form
 //     clusters (FP64 division is slow on this part, so no FP64 bisection).
