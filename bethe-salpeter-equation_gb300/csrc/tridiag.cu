@@ -1604,10 +1604,10 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     if ((st = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_kernel<T2>, threads, smem), "occupancy"))) return st;
     if (per_sm < 1) return fail(c, BSE_ERR_CUDA, "tridiagonal kernel does not fit on an SM");
     // one block per SM (16 warps of loads in flight each) once the matrix is large enough; small
-    // matrices (batched runs) use ~n/16 blocks so several models' reductions can share the GPU;
+    // matrices (batched runs) use ~n/15 blocks so several models' reductions can share the GPU;
     // a nested FP64 solve runs alone and is bound by FP64 arithmetic (slow on this part), so it
     // spreads the trailing columns over up to one block per SM
-    int B = std::max(4, std::min(nsm, n / 16));
+    int B = std::max(4, std::min(nsm, (n + 14) / 15));
     if (nested) B = std::max(4, std::min(nsm, n / 2));
     if (const char* v = std::getenv("BSE_TRIDIAG_BLOCKS")) B = std::max(1, std::min(nsm * per_sm, std::atoi(v)));
     const int nt_max = (n + TR - 1) / TR;
