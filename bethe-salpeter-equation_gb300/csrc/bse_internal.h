@@ -133,6 +133,10 @@ int run_tables(bse_ctx* c);
 int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out);
 int run_eig(bse_ctx* c, bool want_vectors);
 int run_refine(bse_ctx* c);
+// C = op(A) B for FP64 operands in compensated FP32 arithmetic (eigensolve.cu); C packed (ldc = M)
+// when the product is split over K (small products), P: scratch of pcap elements for the splits
+int df_gemm(bse_ctx* c, bool conj_a, int M, int N, int K, const double2* A, int64_t lda, const double2* B, int64_t ldb,
+            double2* C, int64_t ldc, double2* P, int64_t pcap);
 // FP64 copy of the solved block(s) for the refinement, launched on c->stream (kernel_build.cu)
 int build_h64(bse_ctx* c);
 // launch a pending FP64 build on the side stream (after the work already on c->stream)

@@ -632,6 +632,11 @@ int solve_one(bse_ctx* c, int64_t n, void* A, int64_t lda, bool fp64, double* dW
 
 }  // namespace
 
+int df_gemm(bse_ctx* c, bool conj_a, int M, int N, int K, const double2* A, int64_t lda, const double2* B, int64_t ldb,
+            double2* C, int64_t ldc, double2* P, int64_t pcap) {
+    return gemm_df(c, conj_a, M, N, K, A, lda, B, ldb, C, ldc, P, pcap);
+}
+
 int run_eig(bse_ctx* c, bool want_vectors) {
     int st;
     if (!c->h_valid) return fail(c, BSE_ERR_STATE, "BSE matrix not built (diagonalize consumes it; rebuild first)");

@@ -29,6 +29,7 @@
 #include <cstdlib>
 #include <mutex>
 #include <string>
+#include <type_traits>
 
 #include "blas_ops.h"
 #include "bse_internal.h"
@@ -1529,6 +1530,17 @@ __global__ void ut_diag_kernel(int n, int npanel, const T2* __restrict__ tau, T2
     }
 }
 
+// X[r + j ldx] -= D[r + j m] for the m x ncol block (FP64 back-transformation)
+__global__ void sub_block_kernel(int m, int ncol, const double2* __restrict__ D, double2* __restrict__ X, int64_t ldx) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)m * ncol) return;
+    const int r = (int)(t % m), j = (int)(t / m);
+    double2 x = X[r + (int64_t)j * ldx];
+    x.x -= D[t].x;
+    x.y -= D[t].y;
+    X[r + (int64_t)j * ldx] = x;
+}
+
 template <typename T2>
 __global__ void real_to_complex_kernel(int64_t n, const typename Real<T2>::t* __restrict__ in, T2* __restrict__ out) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -1985,15 +1997,39 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
             }
             T2 one, zero, mone;
             one.x = 1; one.y = 0; zero.x = 0; zero.y = 0; mone.x = -1; mone.y = 0;
-            for (int p = npanel - 1; p >= 0 && !st; p--) {
-                const int k0 = kWY * p, m = n - 1 - k0, nb = std::min(kWY, m);
-                const T2* Vp = Vall + vpanel_offset(n, p);
-                const T2* Up = Tf + (size_t)p * kWY * kWY;
-                cublasStatus_t bs = xgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nb, n_vec, m, &one, Vp, m, X + k0 + 1, n, &zero, W1, kWY);
-                if (bs == CUBLAS_STATUS_SUCCESS) bs = xtrsm_lu(c->cublas, nb, n_vec, Up, kWY, W1, kWY);
-                if (bs == CUBLAS_STATUS_SUCCESS)
-                    bs = xgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m, n_vec, nb, &mone, Vp, m, W1, kWY, &one, X + k0 + 1, n);
-                if (bs != CUBLAS_STATUS_SUCCESS) st = fail(c, BSE_ERR_CUDA, "cuBLAS failed in the back-transformation");
+            if constexpr (std::is_same<T2, double2>::value) {
+                // FP64: the two products in compensated FP32 (FP64 GEMMs are slow on this part),
+                // the triangular solve in cuBLAS
+                const int64_t pcap = (int64_t)1 << 22;
+                double2 *D = nullptr, *P = nullptr;
+                if ((st = cuda_check(c, cudaMallocAsync((void**)&D, (size_t)(n - 1) * n_vec * sizeof(double2), c->stream), "WY work"))) return st;
+                if ((st = cuda_check(c, cudaMallocAsync((void**)&P, (size_t)pcap * sizeof(double2), c->stream), "WY work"))) return st;
+                for (int p = npanel - 1; p >= 0 && !st; p--) {
+                    const int k0 = kWY * p, m = n - 1 - k0, nb = std::min(kWY, m);
+                    const double2* Vp = Vall + vpanel_offset(n, p);
+                    const double2* Up = Tf + (size_t)p * kWY * kWY;
+                    if ((st = df_gemm(c, true, nb, n_vec, m, Vp, m, X + k0 + 1, n, W1, nb, P, pcap))) break;      // V^H X
+                    if (xtrsm_lu(c->cublas, nb, n_vec, Up, kWY, W1, nb) != CUBLAS_STATUS_SUCCESS) {
+                        st = fail(c, BSE_ERR_CUDA, "cuBLAS failed in the back-transformation");
+                        break;
+                    }
+                    if ((st = df_gemm(c, false, m, n_vec, nb, Vp, m, W1, nb, D, m, P, pcap))) break;            // V W
+                    sub_block_kernel<<<(unsigned)(((int64_t)m * n_vec + 255) / 256), 256, 0, c->stream>>>(m, n_vec, D, X + k0 + 1, n);
+                    c->launches++;
+                }
+                cudaFreeAsync(D, c->stream);
+                cudaFreeAsync(P, c->stream);
+            } else {
+                for (int p = npanel - 1; p >= 0 && !st; p--) {
+                    const int k0 = kWY * p, m = n - 1 - k0, nb = std::min(kWY, m);
+                    const T2* Vp = Vall + vpanel_offset(n, p);
+                    const T2* Up = Tf + (size_t)p * kWY * kWY;
+                    cublasStatus_t bs = xgemm(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nb, n_vec, m, &one, Vp, m, X + k0 + 1, n, &zero, W1, kWY);
+                    if (bs == CUBLAS_STATUS_SUCCESS) bs = xtrsm_lu(c->cublas, nb, n_vec, Up, kWY, W1, kWY);
+                    if (bs == CUBLAS_STATUS_SUCCESS)
+                        bs = xgemm(c->cublas, CUBLAS_OP_N, CUBLAS_OP_N, m, n_vec, nb, &mone, Vp, m, W1, kWY, &one, X + k0 + 1, n);
+                    if (bs != CUBLAS_STATUS_SUCCESS) st = fail(c, BSE_ERR_CUDA, "cuBLAS failed in the back-transformation");
+                }
             }
             if (!st) st = cuda_check(c, cudaGetLastError(), "back-transformation");
             for (void* q : {(void*)Tf, (void*)Vall, (void*)W1}) cudaFreeAsync(q, c->stream);
