@@ -73,10 +73,13 @@ class Marshalled:
         self.nk, self.nc, self.nv, self.ng = prob.nk, p.nc, p.nv, prob.ng
         self.nb = m.nw * m.n_spin
         self.N = prob.nk * p.nc * p.nv
+        self.coupled = p.tamm_dancoff == 0 and not p.ipa
         self.n_h = (3 * S + 1) * self.N
         self.n_rho = (S + 1) * self.N
         self.n_exc = (3 * S + 1) * self.N
         self.n_opt = (S + 1) * self.N     # optically active block (spinless N, collinear 2N)
+        if self.coupled:                  # full BSE: resonant + anti-resonant exciton rows, all 2N pairs
+            self.n_h = self.n_rho = self.n_exc = self.n_opt = 2 * self.N
 
     def band_buffers(self):
         return (np.zeros((2, self.nk, self.nc)), np.zeros((2, self.nk, self.nv)),

@@ -51,6 +51,7 @@ struct bse_ctx {
     // sizes
     int nw, ns, nb, nk, ng, nv, nc, S, nr;
     int64_t N, n_h, n_rho, n_exc, n_opt;
+    bool coupled = false;        // full BSE with the coupling block (tamm_dancoff = 0, not IPA; spinless, FP64)
     bse_params p;
     bse::Geometry geo;
     bse::Interaction itx;
@@ -101,7 +102,8 @@ struct bse_ctx {
     void* d_H = nullptr;         // n_h x n_h, complex64 (MIXED) or complex128 (FP64)
     size_t h_elem = 0;
     double2* d_H64 = nullptr;    // MIXED refinement: FP64 lower triangle of the solved block(s)
-    void* d_blk = nullptr;       // collinear: the two 2N x 2N diagonal blocks (H0, H1)
+    void* d_blk = nullptr;       // collinear: the two 2N x 2N diagonal blocks (H0, H1); coupled: L^H J L
+    double2* d_aux = nullptr;    // coupled: L^{-1} rho(G0) (2N)
     bool h_valid = false;
     double* d_E = nullptr;       // n_exc eigenvalues
     void* d_A = nullptr;         // eigenvectors of the optically active block (n_opt x n_opt)
@@ -142,6 +144,8 @@ int build_h64(bse_ctx* c);
 // launch a pending FP64 build on the side stream (after the work already on c->stream)
 int fork_h64(bse_ctx* c);
 int run_oscillators(bse_ctx* c);
+// full BSE: structure-preserving solve of H = J M through M = L L^H (eigensolve.cu)
+int run_eig_coupled(bse_ctx* c, bool want_vectors);
 int run_eps(bse_ctx* c, const double* omega, int n_omega, double gamma, double* eps2, double* eps1);
 
 // own dense eigensolver (tridiag.cu)

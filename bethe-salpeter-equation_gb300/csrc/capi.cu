@@ -158,8 +158,14 @@ int validate(const bse_model* m, const bse_params* p) {
     if (p->nv < 1 || p->nc < 1 || p->nv + p->nc > m->nw)
         return fail(nullptr, BSE_ERR_BAD_INPUT, "need 1 <= nv, nc and nv + nc <= nw");
     if (p->nv > 8 || p->nc > 8) return fail(nullptr, BSE_ERR_BAD_INPUT, "nv, nc above 8 are not supported");
-    if (p->tamm_dancoff != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "only the Tamm-Dancoff BSE is implemented");
+    if (p->tamm_dancoff != 0 && p->tamm_dancoff != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "tamm_dancoff must be 0 or 1");
     if (p->precision != BSE_FP64 && p->precision != BSE_MIXED) return fail(nullptr, BSE_ERR_BAD_INPUT, "precision");
+    if (p->tamm_dancoff == 0 && !p->ipa) {
+        if (m->n_spin != 1)
+            return fail(nullptr, BSE_ERR_BAD_INPUT, "the full BSE (tamm_dancoff = 0) is implemented for n_spin = 1 only");
+        if (p->precision != BSE_FP64)
+            return fail(nullptr, BSE_ERR_BAD_INPUT, "the full BSE (tamm_dancoff = 0) runs in FP64: set precision = BSE_FP64");
+    }
     if (p->eig_solver != BSE_EIG_OWN && p->eig_solver != BSE_EIG_CUSOLVER) return fail(nullptr, BSE_ERR_BAD_INPUT, "eig_solver");
     if (p->coulomb_kind != BSE_V_BARE_3D && p->coulomb_kind != BSE_V_BARE_2D) return fail(nullptr, BSE_ERR_BAD_INPUT, "coulomb_kind");
     if (p->w_kind < BSE_W_EMPIRICAL || p->w_kind > BSE_W_BARE) return fail(nullptr, BSE_ERR_BAD_INPUT, "w_kind");
@@ -204,7 +210,7 @@ void destroy_ctx(bse_ctx* c) {
     if (c->side2) cudaStreamSynchronize(c->side2);
     void* ptrs[] = {c->d_rcart, c->d_weights, c->d_hr, c->d_centres, c->d_k, c->d_bmat, c->d_kidx, c->d_g, c->d_status,
                     c->d_ec, c->d_ev, c->d_cc, c->d_cv, c->d_phi, c->d_phi32, c->d_X, c->d_qx, c->d_qx32, c->d_rho,
-                    c->d_H, c->d_H64, c->d_blk, c->d_E, c->d_f, c->d_work};
+                    c->d_H, c->d_H64, c->d_blk, c->d_aux, c->d_E, c->d_f, c->d_work};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : c->ev)
@@ -245,10 +251,11 @@ int bse_sizes(const bse_model* m, const bse_params* p, int64_t* n_bse, int64_t* 
     if (!m || !p) return BSE_ERR_BAD_INPUT;
     const int64_t N = (int64_t)m->n_k * p->nc * p->nv;
     const int S = m->n_spin - 1;
+    const bool coupled = p->tamm_dancoff == 0 && !p->ipa;   // full BSE: 2N rows everywhere
     if (n_bse) *n_bse = N;
-    if (n_exc) *n_exc = (3 * S + 1) * N;
-    if (n_rho) *n_rho = (S + 1) * N;
-    if (n_h) *n_h = (3 * S + 1) * N;
+    if (n_exc) *n_exc = coupled ? 2 * N : (3 * S + 1) * N;
+    if (n_rho) *n_rho = coupled ? 2 * N : (S + 1) * N;
+    if (n_h) *n_h = coupled ? 2 * N : (3 * S + 1) * N;
     return BSE_OK;
 }
 
@@ -281,6 +288,8 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     c->n_rho = (c->S + 1) * c->N;
     c->n_exc = (3 * c->S + 1) * c->N;
     c->n_opt = (c->S + 1) * c->N;
+    c->coupled = p->tamm_dancoff == 0 && !p->ipa;
+    if (c->coupled) c->n_h = c->n_rho = c->n_exc = c->n_opt = 2 * c->N;
     // geometry (Crystal_Lattice, bse.version13.cpp:85-124)
     {
         const double* a = m->lattice;
@@ -351,6 +360,10 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     c->h_elem = mixed ? 8 : 16;
     CK(dmalloc(c, &c->d_H, (size_t)c->n_h * c->n_h * c->h_elem, "H"));
     if (c->S) CK(dmalloc(c, &c->d_blk, 2 * (size_t)(2 * c->N) * (2 * c->N) * c->h_elem, "spin blocks"));
+    if (c->coupled) {
+        CK(dmalloc(c, &c->d_blk, (size_t)c->n_h * c->n_h * sizeof(double2), "L^H J L"));
+        CK(dmalloc(c, &c->d_aux, (size_t)c->n_h * sizeof(double2), "L^-1 rho"));
+    }
     if (mixed && !p->ipa && p->n_refine > 0) {
         const size_t n64 = c->S ? 4 * c->N : c->N;
         CK(dmalloc(c, &c->d_H64, n64 * n64 * 16, "H64"));

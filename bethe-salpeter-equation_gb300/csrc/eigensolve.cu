@@ -637,10 +637,133 @@ int df_gemm(bse_ctx* c, bool conj_a, int M, int N, int K, const double2* A, int6
     return gemm_df(c, conj_a, M, N, K, A, lda, B, ldb, C, ldc, P, pcap);
 }
 
+namespace {
+
+// L (lower, from potrf) in place with its strict upper triangle cleared, and W = J L
+// (rows N..2N-1 negated), n = 2N.
+__global__ void jl_kernel(int64_t n, int64_t N, double2* __restrict__ L, double2* __restrict__ W) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    const int64_t i = t % n, j = t / n;
+    double2 l = L[t];
+    if (i < j) {
+        l = make_double2(0, 0);
+        L[t] = l;
+    }
+    W[t] = i >= N ? make_double2(-l.x, -l.y) : l;
+}
+
+// W <- (W + W^H) / 2 (the product L^H (J L) is Hermitian up to rounding)
+__global__ void hermitian_part_kernel(int64_t n, double2* __restrict__ W) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    const int64_t i = t % n, j = t / n;
+    if (i < j) return;
+    if (i == j) {
+        W[t].y = 0.0;
+        return;
+    }
+    const double2 a = W[t], b = W[j + n * i];
+    const double2 m = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+    W[t] = m;
+    W[j + n * i] = make_double2(m.x, -m.y);
+}
+
+// x_l *= |E_l|^(1/2) for the leading ncols columns of X (ld n), and f_l *= |E_l|^(1/2)
+__global__ void jnorm_scale_kernel(int64_t n, int64_t ncols, const double* __restrict__ E, double2* __restrict__ X,
+                                   double2* __restrict__ f) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (f && t < n) {
+        const double s = sqrt(fabs(E[t]));
+        f[t] = make_double2(f[t].x * s, f[t].y * s);
+    }
+    if (t >= n * ncols) return;
+    const double s = sqrt(fabs(E[t / n]));
+    X[t] = make_double2(X[t].x * s, X[t].y * s);
+}
+
+}  // namespace
+
+// Full BSE (tamm_dancoff = 0, spinless, FP64): common_diagonalization's eig_gen of the 2N x 2N
+// matrix (bse.version13.cpp:3326) replaced by a structure-preserving Hermitian solve.  The build
+// left M = [[A, B], [B^H, conj(A)]] (H = J M) in d_H.  With M = L L^H (potrf; M must be positive
+// definite, the stable-ground-state case), H = J L L^H is similar to the Hermitian W = L^H J L,
+// so W y = E y gives H x = E x for x = |E|^{1/2} L^{-H} y, normalised x^H J x = sign(E), and the
+// oscillator f = rho^H x = |E|^{1/2} (L^{-1} rho)^H y needs no eigenvector when the own solver
+// forms (L^{-1} rho)^H y itself.  Eigenvalues ascending: -E_max .. -E_min, E_min .. E_max.
+int run_eig_coupled(bse_ctx* c, bool want_vectors) {
+    int st;
+    const int64_t n = c->n_h, N = c->N;
+    double2* M = (double2*)c->d_H;
+    double2* W = (double2*)c->d_blk;
+    cublasSetStream(c->cublas, c->stream);
+    cusolverDnSetStream(c->cusolver, c->stream);
+    {
+        cusolverDnParams_t prm;
+        if ((st = cusolver_check(c, cusolverDnCreateParams(&prm), "params"))) return st;
+        size_t dws = 0, hws = 0;
+        st = cusolver_check(c, cusolverDnXpotrf_bufferSize(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F, M, n,
+                                                           CUDA_C_64F, &dws, &hws), "potrf size");
+        if (!st) st = ensure_work(c, dws + 256);
+        if (st) { cusolverDnDestroyParams(prm); return st; }
+        int* dinfo = (int*)c->d_work;
+        std::vector<char> hbuf(std::max<size_t>(hws, 1));
+        st = cusolver_check(c, cusolverDnXpotrf(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F, M, n, CUDA_C_64F,
+                                                (char*)c->d_work + 256, dws, hbuf.data(), hws, dinfo), "potrf");
+        cusolverDnDestroyParams(prm);
+        if (st) return st;
+        int info = 0;
+        if ((st = cuda_check(c, cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "potrf info"))) return st;
+        if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "potrf sync"))) return st;
+        if (info != 0) {
+            c->h_valid = false;
+            return fail(c, BSE_ERR_BAD_INPUT, "full BSE: [[A, B], [B*, A*]] is not positive definite (leading minor " +
+                                                  std::to_string(info) + "); the structure-preserving solve needs a stable ground state");
+        }
+    }
+    const unsigned gb = (unsigned)((n * n + 255) / 256);
+    jl_kernel<<<gb, 256, 0, c->stream>>>(n, N, M, W);
+    c->launches++;
+    const cuDoubleComplex one = make_cuDoubleComplex(1, 0);
+    if ((st = cublas_check(c, cublasZtrmm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
+                                          n, n, &one, (const cuDoubleComplex*)M, n, (const cuDoubleComplex*)W, n,
+                                          (cuDoubleComplex*)W, n), "L^H J L"))) return st;
+    hermitian_part_kernel<<<gb, 256, 0, c->stream>>>(n, W);
+    c->launches++;
+    // L^{-1} rho(G0)
+    const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
+    if ((st = cuda_check(c, cudaMemcpyAsync(c->d_aux, rho0, n * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream), "rho copy"))) return st;
+    if ((st = cublas_check(c, cublasZtrsv(c->cublas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n,
+                                          (const cuDoubleComplex*)M, n, (cuDoubleComplex*)c->d_aux, 1), "L^-1 rho"))) return st;
+    if ((st = cuda_check(c, cudaGetLastError(), "coupled setup"))) return st;
+    if ((st = solve_one(c, n, W, n, true, c->d_E, want_vectors ? n : 0, c->d_aux, c->d_f))) return st;
+    // eigenvectors of H: X = L^{-H} Y, then the J-normalisation of X and of the oscillators
+    const int64_t nvec = c->n_vec_valid;
+    if (nvec > 0 &&
+        (st = cublas_check(c, cublasZtrsm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
+                                          n, nvec, &one, (const cuDoubleComplex*)M, n, (cuDoubleComplex*)W, n), "L^-H Y")))
+        return st;
+    jnorm_scale_kernel<<<(unsigned)((n * std::max<int64_t>(nvec, 1) + 255) / 256), 256, 0, c->stream>>>(
+        n, nvec, c->d_E, W, c->f_from_eig ? c->d_f : nullptr);
+    c->launches++;
+    c->d_A = W;
+    return cuda_check(c, cudaGetLastError(), "coupled eigenvectors");
+}
+
 int run_eig(bse_ctx* c, bool want_vectors) {
     int st;
     if (!c->h_valid) return fail(c, BSE_ERR_STATE, "BSE matrix not built (diagonalize consumes it; rebuild first)");
     stage_begin(c, 3);
+    if (c->coupled) {
+        c->n_refined = 0;
+        st = run_eig_coupled(c, want_vectors);
+        c->h_valid = false;
+        if (st) return st;
+        stage_end(c, 3);
+        c->eig_valid = true;
+        c->osc_valid = false;
+        return BSE_OK;
+    }
     const bool fp64 = c->p.precision == BSE_FP64;
     const bool refine = !fp64 && !c->p.ipa && c->p.n_refine > 0;
     const int64_t n_opt = c->n_opt;

@@ -13,7 +13,11 @@
 //   H_x[r1,r2] = sf/(V nk) sum_ab P[r1,(aa)] X_ab conj(P[r2,(bb)]),
 //                X_ab = sum_{G != G0} v(q+G) e^{i(G+q).(tau_a - tau_b)}
 // (same values as the reference's G-sums over stored all-pairs densities -- the oracle
-// keeps those loops).  Phi is tabulated once per distinct Delta k (on a k-grid there are
+// keeps those loops).  The coupling block of the full BSE (add_coupling_part, 2929-3040)
+// reuses both tables with the other pairing of the band coefficients:
+//   B_d[r1,r2] = -1/(V nk) sum_ab P[r1,(ba)] conj(Phi_ab(dk)) P[r2,(ab)],
+//   B_x[r1,r2] = sf/(V nk) sum_ab P[r1,(aa)] X_ab P[r2,(bb)].
+// Phi is tabulated once per distinct Delta k (on a k-grid there are
 // (2n-1)^d of them); the build kernel then writes each element of H exactly once, k1
 // fastest so that a warp stores 32 consecutive elements of one column: the kernel is
 // bound by the N^2 store of H, not by arithmetic (inner dimension nw <= 16).
@@ -145,18 +149,21 @@ __global__ void exchange_table_kernel(int ns, int nw, int ng, Interaction it, do
     X[t] = make_double2(re, im);
 }
 
-// rho_cv[s*N + r, g] (Dipole_Elements::pull_values, k-diagonal branch, 1951-2066; Q12/Q13)
-__global__ void rho_cv_kernel(int nk, int nc, int nv, int nw, int ns, int ng, int small_q,
+// rho_cv[s*N + r, g] (Dipole_Elements::pull_values, k-diagonal branch, 1951-2066; Q12/Q13).
+// coupled (spinless): rows N..2N-1 hold rho_vc[r, g] = sum_a conj(c_va) M_a c_ca of
+// add_coupling_part (2937, 2950), with the valence states of rho_cv and the dipole column (Q25).
+__global__ void rho_cv_kernel(int nk, int nc, int nv, int nw, int ns, int ng, int small_q, int coupled,
                               double q0, double q1, double q2,
                               const double* __restrict__ gcart, const double* __restrict__ centres,
                               const double2* __restrict__ cc, const double2* __restrict__ cv,
                               double2* __restrict__ rho) {
-    const int64_t N = (int64_t)nk * nc * nv, nrho = N * ns;
+    const int64_t N = (int64_t)nk * nc * nv, nrho = N * (coupled ? 2 : ns);
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= nrho * ng) return;
     const int64_t i = t % nrho;
     const int g = (int)(t / nrho);
-    const int s = (int)(i / N);
+    const bool vc = coupled && i >= N;
+    const int s = coupled ? 0 : (int)(i / N);
     const int64_t r = i % N;
     const int k = (int)(r % nk), v = (int)((r / nk) % nv), c = (int)(r / ((int64_t)nk * nv));
     const int nb = nw * ns;
@@ -175,8 +182,8 @@ __global__ void rho_cv_kernel(int nk, int nc, int nv, int nw, int ns, int ng, in
             sincos(ph, &sn, &cs);
             mel = make_double2(cs, sn);
         }
-        double2 x = cmul(cmul(cconj(cc[((size_t)k * nc + c) * nb + s * nw + a]), mel),
-                         cv[((size_t)k * nv + v) * nb + s * nw + a]);
+        const double2 ca = cc[((size_t)k * nc + c) * nb + s * nw + a], va = cv[((size_t)k * nv + v) * nb + s * nw + a];
+        const double2 x = vc ? cmul(cmul(cconj(va), mel), ca) : cmul(cmul(cconj(ca), mel), va);
         acc.x += x.x;
         acc.y += x.y;
     }
@@ -370,6 +377,94 @@ __global__ void __launch_bounds__(256) build_kernel(BuildArgs a, const typename 
     }
 }
 
+// Coupling block B = H[0:N, N:2N] of the full BSE, spinless, FP64 (add_coupling_part,
+// bse.version13.cpp:2929-3040).  Same launch shape as build_kernel (lane = k1, warp = k2):
+//   direct   (rho_kk_cv W conj(rho_kk_vc), 2975-3033; Q26): P[r1,(ba)] pairs the valence state of
+//            exciton r1 with the conduction state of r2 through conj(Phi_ab(k2 - k1)),
+//   exchange (rho_cv(r1) conj(rho_vc(r2)), 2940-2967): the row factors Qx times P[r2,(bb)].
+// Every element of B is written once.
+template <int NW>
+__global__ void __launch_bounds__(256) coupling_kernel(BuildArgs a, const double2* __restrict__ phi,
+                                                       const double2* __restrict__ qx, double2* __restrict__ H) {
+    extern __shared__ unsigned char smem_raw[];
+    const int lane = threadIdx.x, warp = threadIdx.y, KW = blockDim.y;
+    const int nb = a.nw;                                                        // spinless: nb == nw
+    double2* sC = reinterpret_cast<double2*>(smem_raw) + (size_t)warp * (a.nc + a.nv) * nb;   // [nc+nv][nb] of k2
+    const int k1 = blockIdx.x * 32 + lane;
+    const int k2 = blockIdx.y * KW + warp;
+    if (k2 < a.nk) {
+        for (int i = lane; i < a.nc * nb; i += 32) sC[i] = a.cc[(size_t)k2 * a.nc * nb + i];
+        for (int i = lane; i < a.nv * nb; i += 32) sC[a.nc * nb + i] = a.cv[(size_t)k2 * a.nv * nb + i];
+    }
+    __syncwarp();
+    if (k1 >= a.nk || k2 >= a.nk) return;
+    int64_t d;
+    if (a.on_grid) {
+        const int x1 = a.kidx[k1], x2 = a.kidx[k2];
+        const int i0 = (x2 & 1023) - (x1 & 1023), i1 = ((x2 >> 10) & 1023) - ((x1 >> 10) & 1023);
+        const int i2 = ((x2 >> 20) & 1023) - ((x1 >> 20) & 1023);
+        d = (int64_t)(i0 + a.m0 - 1) + (int64_t)(2 * a.m0 - 1) * ((i1 + a.m1 - 1) + (int64_t)(2 * a.m1 - 1) * (i2 + a.m2 - 1));
+    } else {
+        d = (int64_t)k2 * a.nk + k1;
+    }
+    const double2* ph = phi + (size_t)d * a.nblk * NW * NW;                    // exciton spin block 0
+    const double2* sCc2 = sC;
+    const double2* sCv2 = sC + (size_t)a.nc * nb;
+    for (int v1 = 0; v1 < a.nv; v1++) {
+        double2 va[NW];
+#pragma unroll
+        for (int al = 0; al < NW; al++)
+            va[al] = al < a.nw ? a.cv[((size_t)k1 * a.nv + v1) * nb + al] : make_double2(0, 0);   // c_v1(k1)
+        for (int c2 = 0; c2 < a.nc; c2++) {
+            double2 S[NW];   // S[b] = sum_a c_v1a(k1) conj(c_c2a(k2)) conj(Phi_ab)
+#pragma unroll
+            for (int b = 0; b < NW; b++) S[b] = make_double2(0, 0);
+            for (int al = 0; al < a.nw; al++) {
+                const double2 coef = tmul(va[al], cconj(sCc2[c2 * nb + al]));
+                const double2* prow = ph + al * NW;
+#pragma unroll
+                for (int b = 0; b < NW; b++)
+                    if (b < a.nw) cfma_conjb(S[b], coef, prow[b]);
+            }
+            for (int c1 = 0; c1 < a.nc; c1++) {
+                const int64_t r1 = (int64_t)c1 * a.nv * a.nk + (int64_t)v1 * a.nk + k1;
+                double2 tt[NW], qq[NW];
+#pragma unroll
+                for (int b = 0; b < NW; b++) {
+                    tt[b] = make_double2(0, 0);
+                    qq[b] = make_double2(0, 0);
+                    if (b < a.nw) {
+                        tt[b] = tmul(S[b], cconj(a.cc[((size_t)k1 * a.nc + c1) * nb + b]));   // conj(c_c1b(k1))
+                        qq[b] = qx[(size_t)b * a.N + r1];
+                    }
+                }
+                for (int v2 = 0; v2 < a.nv; v2++) {
+                    const int64_t r2 = (int64_t)c2 * a.nv * a.nk + (int64_t)v2 * a.nk + k2;
+                    double2 acc = make_double2(0, 0), accx = make_double2(0, 0);
+#pragma unroll
+                    for (int b = 0; b < NW; b++)
+                        if (b < a.nw) {
+                            const double2 cvb = sCv2[v2 * nb + b];
+                            cfma(acc, tt[b], cvb);                                       // ... c_v2b(k2)
+                            cfma(accx, qq[b], tmul(cconj(sCc2[c2 * nb + b]), cvb));     // Qx P[r2,(bb)]
+                        }
+                    H[r1 + a.ld * (a.N + r2)] = make_double2(a.fw * acc.x + accx.x, a.fw * acc.y + accx.y);
+                }
+            }
+        }
+    }
+}
+
+// M = [[A, B], [B^H, conj(A)]] from the top blocks (ld = 2N): the Hermitian matrix whose J-scaled
+// form J M is the full BSE matrix [[A, B], [-B^H, -conj(A)]] of 2917-2923 and 3035-3038.
+__global__ void coupled_lower_blocks_kernel(int64_t N, double2* __restrict__ M) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= N * N) return;
+    const int64_t i = t % N, j = t / N, ld = 2 * N;
+    M[(N + i) + ld * (N + j)] = cconj(M[i + ld * j]);
+    M[(N + i) + ld * j] = cconj(M[j + ld * (N + i)]);
+}
+
 // Collinear spin rotation U H U (spin_transformation, bse.version13.cpp:3048-3117), in place per
 // (row, col) position across the 4x4 spin blocks, so no block reads an already rotated one (Q24).
 template <typename T2>
@@ -447,6 +542,32 @@ int launch_build_nw(bse_ctx* c, void* H, int64_t ld, bool lower, const void* phi
     return cuda_check(c, cudaGetLastError(), "build kernel launch");
 }
 
+template <int NW>
+int launch_coupling_nw(bse_ctx* c) {
+    BuildArgs a = {};
+    a.nk = c->nk; a.nc = c->nc; a.nv = c->nv; a.nw = c->nw; a.ns = c->ns;
+    a.N = c->N; a.ld = 2 * c->N;
+    a.fw = -1.0 / (c->geo.vol * c->nk);   // bse.version13.cpp:2960
+    a.on_grid = c->dmap.on_grid;
+    a.m0 = c->dmap.m[0]; a.m1 = c->dmap.m[1]; a.m2 = c->dmap.m[2];
+    a.nblk = 1;
+    a.kidx = c->d_kidx;
+    a.cc = c->d_cc; a.cv = c->d_cv;
+    const int KW = 8;
+    dim3 block(32, KW), grid((c->nk + 31) / 32, (c->nk + KW - 1) / KW, 1);
+    const size_t smem = (size_t)KW * (c->nc + c->nv) * c->nb * sizeof(double2);   // <= 8 * 16 * 16 * 16 = 32 KB
+    coupling_kernel<NW><<<grid, block, smem, c->stream>>>(a, c->d_phi, c->d_qx, (double2*)c->d_H);
+    c->launches++;
+    return cuda_check(c, cudaGetLastError(), "coupling kernel launch");
+}
+
+int launch_coupling(bse_ctx* c) {
+    if (c->nw <= 2) return launch_coupling_nw<2>(c);
+    if (c->nw <= 4) return launch_coupling_nw<4>(c);
+    if (c->nw <= 8) return launch_coupling_nw<8>(c);
+    return launch_coupling_nw<16>(c);
+}
+
 template <typename T>
 int launch_build(bse_ctx* c, void* H, int64_t ld, bool lower, const void* phi, const void* qx,
                  int br, int bc, int dd, int de, int dg) {
@@ -470,7 +591,7 @@ int run_tables(bse_ctx* c) {
         const int64_t total = c->n_rho * ng;
         const int thr = 256;
         rho_cv_kernel<<<(unsigned)((total + thr - 1) / thr), thr, 0, c->stream>>>(
-            c->nk, c->nc, c->nv, nw, ns, ng, c->p.small_momentum, c->p.q[0], c->p.q[1], c->p.q[2],
+            c->nk, c->nc, c->nv, nw, ns, ng, c->p.small_momentum, c->coupled ? 1 : 0, c->p.q[0], c->p.q[1], c->p.q[2],
             c->d_g, c->d_centres, c->d_cc, c->d_cv, c->d_rho);
         c->launches++;
         if ((st = cuda_check(c, cudaGetLastError(), "rho kernel"))) return st;
@@ -553,7 +674,7 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     const bool mixed = c->p.precision == BSE_MIXED;
     const bool coll = c->S == 1;
     // the own eigensolver reads full Hermitian storage; cuSOLVER reads the lower triangle
-    const bool lower = !full && !coll && h_out == nullptr && c->p.eig_solver != BSE_EIG_OWN;
+    const bool lower = !full && !coll && !c->coupled && h_out == nullptr && c->p.eig_solver != BSE_EIG_OWN;
     const int64_t ld = c->n_h;
     // every element the solver reads is written by the build (lower triangle, or all of it);
     // only the collinear layout has blocks the build never touches
@@ -572,6 +693,12 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
         st = mixed ? launch_build<float>(c, c->d_H, ld, lower, phi, qx, br, bc, direct, exch, diag)
                    : launch_build<double>(c, c->d_H, ld, lower, phi, qx, br, bc, direct, exch, diag);
         if (st) return st;
+    }
+    if (c->coupled && !c->p.ipa) {
+        if ((st = launch_coupling(c))) return st;
+        const int64_t nn = c->N * c->N;
+        coupled_lower_blocks_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, (double2*)c->d_H);
+        c->launches++;
     }
     if (coll) {
         const int64_t nn = c->N * c->N;
@@ -606,6 +733,15 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
             for (size_t i = 0; i < n; i++) { h_out[2 * i] = tmp[i].x; h_out[2 * i + 1] = tmp[i].y; }
         } else {
             if ((st = cuda_check(c, cudaMemcpyAsync(h_out, c->d_H, n * sizeof(double2), cudaMemcpyDeviceToHost, c->stream), "H copy"))) return st;
+            if (c->coupled) {
+                // the device holds M; the caller gets the reference's matrix H = J M (rows N..2N-1 negated)
+                if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "H copy sync"))) return st;
+                for (int64_t j = 0; j < ld; j++)
+                    for (int64_t i = c->N; i < ld; i++) {
+                        h_out[2 * (i + ld * j)] = -h_out[2 * (i + ld * j)];
+                        h_out[2 * (i + ld * j) + 1] = -h_out[2 * (i + ld * j) + 1];
+                    }
+            }
         }
     }
     if (rho_out) {

@@ -5,6 +5,8 @@
 // (3621-3634):
 //   f_l   = sum_i conj(rho_i(G0)) A_il
 //   eps(w) = 1 - F sum_l |f_l|^2 / (w - E_l + i gamma),  F = conv / (V nk)  (small q, 3531-3532)
+// and, for the full BSE (3607-3620), eps(w) = 1 - F rho^H (w - H + i gamma)^{-1} J rho over all 2N
+// J-normalised pairs: 1 - F sum_l sign(E_l) |f_l|^2 / (w - E_l + i gamma), rho = (rho_cv; rho_vc).
 // The oscillator pass reads the eigenvector matrix once (HBM-bound, one warp per column,
 // lanes stride down the column so every load is coalesced; FP32 partial sums per lane for
 // complex64 vectors, combined in FP64 with warp shuffles).  The spectrum is one warp per
@@ -47,9 +49,11 @@ __global__ void __launch_bounds__(256) oscillator_kernel(int64_t n, int64_t lda,
     if (lane == 0) f[col] = make_double2(re, im);
 }
 
+// signed_w (full BSE): every pair enters with the sign of its J-norm x^H J x = sign(E_l), so the
+// anti-resonant pairs (E_l < 0) give -|f_l|^2 / (w - E_l + i gamma)
 __global__ void __launch_bounds__(256) eps_kernel(int64_t n, const double* __restrict__ E,
                                                   const double2* __restrict__ f, const double* __restrict__ omega,
-                                                  int n_omega, double gamma, double F,
+                                                  int n_omega, double gamma, double F, int signed_w,
                                                   double* __restrict__ eps2, double* __restrict__ eps1) {
     const int lane = threadIdx.x & 31;
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -58,8 +62,10 @@ __global__ void __launch_bounds__(256) eps_kernel(int64_t n, const double* __res
     double a2 = 0, a1 = 0;
     for (int64_t l = lane; l < n; l += 32) {
         const double2 fl = f[l];
-        const double s2 = fl.x * fl.x + fl.y * fl.y;     // conj(f_l) f_l
-        const double d = w - E[l];
+        const double el = E[l];
+        double s2 = fl.x * fl.x + fl.y * fl.y;           // conj(f_l) f_l
+        if (signed_w && el < 0.0) s2 = -s2;
+        const double d = w - el;
         const double inv = s2 / (d * d + g2);
         a2 += inv * gamma;                               // -Im 1/(w - E + i gamma) = gamma / (d^2 + gamma^2)
         a1 += inv * d;
@@ -101,7 +107,7 @@ int run_oscillators(bse_ctx* c) {
 // Launch of eps_kernel on caller-provided device buffers (used by the allocation-free entry point).
 cudaError_t launch_eps_raw(int64_t n, const double* E, const double2* f, const double* omega, int n_omega,
                            double gamma, double F, double* eps2, double* eps1, cudaStream_t stream) {
-    eps_kernel<<<(unsigned)(((int64_t)n_omega * 32 + 255) / 256), 256, 0, stream>>>(n, E, f, omega, n_omega, gamma, F,
+    eps_kernel<<<(unsigned)(((int64_t)n_omega * 32 + 255) / 256), 256, 0, stream>>>(n, E, f, omega, n_omega, gamma, F, 0,
                                                                                 eps2, eps1);
     return cudaGetLastError();
 }
@@ -124,7 +130,7 @@ int run_eps(bse_ctx* c, const double* omega, int n_omega, double gamma, double* 
     stage_begin(c, 6);
     const double* E = c->S ? c->d_E + 2 * c->N : c->d_E;
     eps_kernel<<<(unsigned)(((int64_t)n_omega * 32 + 255) / 256), 256, 0, c->stream>>>(
-        c->n_opt, E, c->d_f, d_om, n_omega, gamma, eps_prefactor(c), d_e2, d_e1);
+        c->n_opt, E, c->d_f, d_om, n_omega, gamma, eps_prefactor(c), c->coupled ? 1 : 0, d_e2, d_e1);
     c->launches++;
     stage_end(c, 6);
     if ((st = cuda_check(c, cudaGetLastError(), "eps kernel"))) return st;

@@ -1,5 +1,6 @@
 /*
- * bse_gpu.h -- C ABI of the GB300 Bethe-Salpeter solver (q->0, Tamm-Dancoff).
+ * bse_gpu.h -- C ABI of the GB300 Bethe-Salpeter solver (q->0; Tamm-Dancoff, or the full
+ * BSE with the coupling block).
  *
  * The entry points replace the kernel-build-and-diagonalize path of
  * bse.version13.cpp (marcomarino123/Bethe-Salpeter-equation):
@@ -8,7 +9,8 @@
  *                       (bse.version13.cpp:647-705, 706-777, 778-821), batched over k
  *   bse_build_kernel    Excitonic_Hamiltonian::extract_hbse_and_rcv (3041-3047):
  *                       pull_coulomb_potentials (2547-2766, model-W modes),
- *                       pull_resonant_part_and_rcv (2767-2928), spin_transformation (3048-3117)
+ *                       pull_resonant_part_and_rcv (2767-2928), spin_transformation (3048-3117),
+ *                       add_coupling_part (2929-3040) when tamm_dancoff = 0
  *   bse_diagonalize     Excitonic_Hamiltonian::common_diagonalization (3120-3368)
  *   bse_oscillators     Excitonic_Hamiltonian::pull_excitonic_oscillator_force (3486-3502)
  *   bse_eps             the omega loop of pull_macroscopic_bse_dielectric_function (3525-3657)
@@ -88,7 +90,9 @@ typedef struct bse_params {
     double fermi_energy;         /* valence = E <= E_F in every spin row (790-799) */
     double scissor;              /* added to conduction energies (815-816) */
     double q[3];                 /* excitonic momentum, q -> 0 (minval * x, 3590-3601) */
-    int32_t tamm_dancoff;        /* must be 1: the coupling block is out of scope */
+    int32_t tamm_dancoff;        /* 1: resonant block only; 0: full BSE with the coupling block B
+                                    (add_coupling_part 2929-3040), n_spin = 1 and BSE_FP64 only;
+                                    no effect with ipa = 1 */
     int32_t ipa;                 /* 1: no kernel, H = diag(E_c - E_v) (3346-3365) */
     int32_t small_momentum;      /* 1: G=0 pair density is the dipole i q.<c|r|v> (1535-1650) */
     int32_t coulomb_kind;        /* BSE_V_* */
@@ -111,7 +115,8 @@ const char* bse_last_error(const bse_ctx* ctx);
 int bse_version(void);
 
 /* Sizes derived from model+params: n_exc = (3*spin+1)*N eigenvalues, n_rho = (spin+1)*N
- * pair-density rows, n_h = dimension of the (full, before the spin split) BSE matrix. */
+ * pair-density rows, n_h = dimension of the (full, before the spin split) BSE matrix.
+ * Full BSE (tamm_dancoff = 0): n_exc = n_rho = n_h = 2N (resonant rows, then anti-resonant). */
 int bse_sizes(const bse_model* model, const bse_params* params,
               int64_t* n_bse, int64_t* n_exc, int64_t* n_rho, int64_t* n_h);
 
@@ -137,21 +142,30 @@ int bse_set_bands(bse_ctx* ctx, const double* e_c, const double* e_v,
 
 /* Stage b: kernel build == extract_hbse_and_rcv (3041-3047).  H stays on the device;
  * h_out (nullable) receives the full n_h x n_h complex128 matrix (spin-transformed when
- * n_spin == 2, 3048-3117), rho_out (nullable) the n_rho x n_g complex128 pair densities. */
+ * n_spin == 2, 3048-3117), rho_out (nullable) the n_rho x n_g complex128 pair densities.
+ * Full BSE: h_out = [[A, B], [-B^H, -conj(A)]] (2917-2923, 3035-3038), rho rows N..2N-1 hold
+ * rho_vc (2937, 2950). */
 int bse_build_kernel(bse_ctx* ctx, double* h_out, double* rho_out);
 
 /* Stage c: dense Hermitian eigensolve == common_diagonalization (3120-3368).
  * e_out (nullable): n_exc eigenvalues ascending (collinear: H0 block then H1 block).
  * a_out (nullable): eigenvectors (spinless n_bse x n_bse; collinear: the
- * spin-conserving block H1, 2N x 2N), complex128 column-major. */
+ * spin-conserving block H1, 2N x 2N), complex128 column-major.
+ * Full BSE (eig_gen of the 2N x 2N matrix, 3326): a structure-preserving solve through the
+ * Cholesky factor of [[A, B], [B^H, conj(A)]], which must be positive definite (a stable
+ * ground state; otherwise BSE_ERR_BAD_INPUT).  e_out: all 2N eigenvalues ascending, -E then +E;
+ * a_out: 2N x 2N eigenvectors of H in that order, J-normalised: x^H diag(1,-1) x = sign(E). */
 int bse_diagonalize(bse_ctx* ctx, double* e_out, double* a_out);
 
 /* Stage d: oscillator strengths f_l = sum_i conj(rho_i(G0)) A_il (3486-3502),
- * complex128, one per optically active exciton (spinless N, collinear 2N). */
+ * complex128, one per optically active exciton (spinless N, collinear 2N; full BSE 2N, from the
+ * J-normalised vectors and rho = (rho_cv; rho_vc)). */
 int bse_oscillators(bse_ctx* ctx, double* f_out);
 
 /* Stage d: eps(w) = 1 - F sum_l |f_l|^2 / (w - E_l + i gamma), F = conv / (V nk)
- * (3531-3532, 3621-3634).  eps2 = Im eps, eps1 = Re eps (either nullable). */
+ * (3531-3532, 3621-3634).  eps2 = Im eps, eps1 = Re eps (either nullable).  Full BSE
+ * (3607-3620): eps(w) = 1 - F rho^H (w - H + i gamma)^{-1} J rho
+ *                     = 1 - F sum_l sign(E_l) |f_l|^2 / (w - E_l + i gamma) over all 2N pairs. */
 int bse_eps(bse_ctx* ctx, const double* omega, int32_t n_omega, double gamma,
             double* eps2, double* eps1);
 

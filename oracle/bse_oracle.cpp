@@ -32,6 +32,14 @@
  *       contraction f = rho^H A (3492), which keeps H gauge-covariant.
  *   Q24 the collinear spin rotation U H U is applied out of place (3091-3097 update the
  *       blocks in place, so later blocks read already-rotated ones).
+ *   Q25 coupling block (tamm_dancoff = 0): rho_vc uses the valence states of rho_cv (k - q;
+ *       2937 evaluates them at k + q, in a separate gauge) and, in small-q mode, the dipole
+ *       i q.<v|r|c> in its G0 column (2937 passes small-momentum 0 there, which leaves an
+ *       unnormalised O(q) density next to the normalised rho_cv dipole).
+ *   Q26 coupling direct term: the q -> 0 limit of the all-pairs densities (states at k, phases
+ *       e^{i(G + k2 - k1).tau}) and of W (no -q shift of Delta k, 2549-2552); like Q23, the
+ *       accumulated row is used as it is, without the conjugation of the .t() assignment
+ *       (3031-3033), which makes B transform as the exciton basis requires (B' = D^H B D*).
  */
 #include "../include/bse_gpu.h"
 
@@ -272,6 +280,7 @@ int ks_subset(const bse_model* m, const bse_params* p, const double* k, int nvs,
 
 struct Dims {
     int nw, ns, nb, nk, ng, nv, nc, S;
+    bool coupled;   // full BSE with the coupling block (tamm_dancoff = 0, not IPA)
     int64_t N, n_h, n_rho;
 };
 
@@ -280,8 +289,9 @@ Dims dims(const bse_model* m, const bse_params* p) {
     d.nw = m->nw; d.ns = m->n_spin; d.nb = d.nw * d.ns; d.nk = m->n_k; d.ng = m->n_g;
     d.nv = p->nv; d.nc = p->nc; d.S = d.ns - 1;
     d.N = (int64_t)d.nk * d.nc * d.nv;
-    d.n_h = (int64_t)(3 * d.S + 1) * d.N;
-    d.n_rho = (int64_t)(d.S + 1) * d.N;
+    d.coupled = p->tamm_dancoff == 0 && !p->ipa;
+    d.n_h = d.coupled ? 2 * d.N : (int64_t)(3 * d.S + 1) * d.N;
+    d.n_rho = d.coupled ? 2 * d.N : (int64_t)(d.S + 1) * d.N;
     return d;
 }
 
@@ -322,6 +332,7 @@ double oracle_prefactor(const bse_model* m, const bse_params* p) {
 int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, const double* e_v,
                  const double* c_c_in, const double* c_v_in, double* h_out, double* rho_out) {
     Dims d = dims(m, p);
+    if (d.coupled && d.S) return BSE_ERR_BAD_INPUT;     // coupling block: spinless / spin-orbital basis only
     Geometry geo = make_geometry(m);
     const cd* Cc = (const cd*)c_c_in;
     const cd* Cv = (const cd*)c_v_in;
@@ -363,6 +374,31 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                         }
                         rho[(s * N + (int64_t)c * nv * nk + (int64_t)v * nk + k) + d.n_rho * g] = acc;
                     }
+
+    // rho_vc rows N..2N-1 of the coupled problem: pull_values(q, -q, 0, ..., left = v, right = c,
+    // reverse = 1) of add_coupling_part (2937, stored at 2950), same row layout c*nv*nk + v*nk + k; Q25
+    if (d.coupled) {
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int c = 0; c < nc; c++)
+            for (int v = 0; v < nv; v++)
+                for (int g = 0; g < ng; g++)
+                    for (int k = 0; k < nk; k++) {
+                        cd acc = 0;
+                        for (int a = 0; a < nw; a++) {
+                            const double* t = tau(0, a);
+                            cd mel;
+                            if (g == g0 && p->small_momentum) {
+                                mel = cd(0.0, qhat[0] * t[0] + qhat[1] * t[1] + qhat[2] * t[2]);
+                            } else {
+                                const double* G = Gv(g);
+                                double ph = t[0] * (G[0] + q[0]) + t[1] * (G[1] + q[1]) + t[2] * (G[2] + q[2]);
+                                mel = cd(std::cos(ph), std::sin(ph));
+                            }
+                            acc += std::conj(Cv[((size_t)k * nv + v) * nb + a]) * mel * Cc[((size_t)k * nc + c) * nb + a];
+                        }
+                        rho[(N + (int64_t)c * nv * nk + (int64_t)v * nk + k) + d.n_rho * g] = acc;
+                    }
+    }
 
     if (!p->ipa) {
         // exchange (2796-2829), Q9; spin blocks i*3, j*3 (2818-2824)
@@ -461,6 +497,70 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                 }
             }
         }
+
+        if (d.coupled) {
+            // coupling block B = H[0:N, N:2N] (add_coupling_part 2929-3040, spinless).
+            // exchange as written (2940-2967): B[r, s] += fx sum_{G != G0} v_G rho_cv[r, G] conj(rho_vc[s, G])
+#pragma omp parallel for schedule(static)
+            for (int64_t s2 = 0; s2 < N; s2++)
+                for (int64_t r = 0; r < N; r++) {
+                    cd acc = 0;
+                    for (int g = 0; g < ng; g++) {
+                        if (g == g0) continue;
+                        acc += (fx * vg[g]) * std::conj(rho[(N + s2) + d.n_rho * g]) * rho[r + d.n_rho * g];
+                    }
+                    H[r + NH * (N + s2)] += acc;
+                }
+            // direct (2971-3033): rho_kk_cv[c2][v1][k2][k1] (2975, left c at k2, right v at k1) and
+            // rho_kk_vc[v2][c1][k2][k1] (2976, left v at k2, right c at k1); Q26
+#pragma omp parallel
+            {
+                std::vector<cd> rcv((size_t)nc * nv * nk * ng), rvc((size_t)nv * nc * nk * ng);
+                std::vector<cd> T((size_t)nk * ng);
+                std::vector<double> W((size_t)nk * ng);
+#pragma omp for schedule(dynamic)
+                for (int k1 = 0; k1 < nk; k1++) {
+                    for (int k2 = 0; k2 < nk; k2++) {
+                        double dk[3] = {Kv(k2)[0] - Kv(k1)[0], Kv(k2)[1] - Kv(k1)[1], Kv(k2)[2] - Kv(k1)[2]};
+                        for (int g = 0; g < ng; g++) W[(size_t)k2 * ng + g] = w_diag(p, geo, nk, dk, Gv(g), g == g0);
+                    }
+                    for (int c2 = 0; c2 < nc; c2++)
+                        for (int v1 = 0; v1 < nv; v1++)
+                            for (int k2 = 0; k2 < nk; k2++)
+                                for (int g = 0; g < ng; g++) {
+                                    cd acc = 0, acc2 = 0;
+                                    for (int a = 0; a < nw; a++) {
+                                        const double* t = tau(0, a);
+                                        double ph = 0;
+                                        for (int x = 0; x < 3; x++) ph += t[x] * (Gv(g)[x] + Kv(k2)[x] - Kv(k1)[x]);
+                                        const cd e(std::cos(ph), std::sin(ph));
+                                        acc += std::conj(Cc[((size_t)k2 * nc + c2) * nb + a]) * e * Cv[((size_t)k1 * nv + v1) * nb + a];
+                                        // the same loop fills rho_kk_vc[v1][c2] (left v1 at k2, right c2 at k1)
+                                        acc2 += std::conj(Cv[((size_t)k2 * nv + v1) * nb + a]) * e * Cc[((size_t)k1 * nc + c2) * nb + a];
+                                    }
+                                    rcv[(((size_t)c2 * nv + v1) * nk + k2) * ng + g] = acc;
+                                    rvc[(((size_t)v1 * nc + c2) * nk + k2) * ng + g] = acc2;
+                                }
+                    for (int c1 = 0; c1 < nc; c1++)
+                        for (int v1 = 0; v1 < nv; v1++) {
+                            const int64_t r1 = (int64_t)c1 * nv * nk + (int64_t)v1 * nk + k1;
+                            for (int c2 = 0; c2 < nc; c2++) {
+                                for (int k2 = 0; k2 < nk; k2++)
+                                    for (int g = 0; g < ng; g++)   // W diagonal in G: T(k2, s) = rho_kk_cv W(s, s)
+                                        T[(size_t)k2 * ng + g] = rcv[(((size_t)c2 * nv + v1) * nk + k2) * ng + g] * W[(size_t)k2 * ng + g];
+                                for (int v2 = 0; v2 < nv; v2++)
+                                    for (int k2 = 0; k2 < nk; k2++) {
+                                        cd acc = 0;
+                                        for (int g = 0; g < ng; g++)
+                                            acc += fw * T[(size_t)k2 * ng + g] * std::conj(rvc[(((size_t)v2 * nc + c1) * nk + k2) * ng + g]);
+                                        const int64_t r2 = (int64_t)c2 * nv * nk + (int64_t)v2 * nk + k2;
+                                        H[r1 + NH * (N + r2)] += acc;
+                                    }
+                            }
+                        }
+                }
+            }
+        }
     }
 
     // transition energies on the diagonal (2893-2897) and collinear spin-flip blocks (2898-2915, Q18)
@@ -476,6 +576,15 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                         H[((i + 1) * N + r) * (1 + NH)] += ecf - ev;
                     }
                 }
+
+    if (d.coupled) {
+        // anti-resonant block -conj(A) (2917-2923) and H[N:2N, 0:N] = -conj(B)^T (3035-3038)
+        for (int64_t j = 0; j < N; j++)
+            for (int64_t i = 0; i < N; i++) {
+                H[(N + i) + NH * (N + j)] = -std::conj(H[i + NH * j]);
+                H[(N + i) + NH * j] = -std::conj(H[j + NH * (N + i)]);
+            }
+    }
 
     if (S) {
         // spin_transformation (3048-3117), out of place (Q24): U = diag(1, [[1,1],[1,-1]]/sqrt2, 1)

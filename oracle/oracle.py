@@ -135,6 +135,36 @@ def eps(E, f, F, omega, gamma):
     return e2, e1
 
 
+def solve_coupled(H, rho_g0, F, omega, gamma):
+    """Full (non-Tamm-Dancoff) BSE on the CPU, the reference's route: eig_gen of the 2N x 2N
+    matrix (LAPACK zgeev, common_diagonalization 3326), eigenpairs sorted by real part (3335),
+    and the spectrum through the inverse overlap ("augmentation") matrix of the eigenvectors
+    (pull_augmentation_matrix 3504-3522, omega loop 3607-3620), here over all 2N eigenpairs:
+      eps(w) = 1 - F rho^H V diag(1 / (w - E + i gamma)) S^{-1} V^H J rho,  S = V^H V,
+    i.e. 1 - F rho^H (w - H + i gamma)^{-1} J rho with J = diag(1, -1) over the two exciton
+    blocks (the reference's N x N truncation of S and its pairing of rows are not reproduced).
+    Also returns the J-normalised eigenvectors (x^H J x = sign(E)) and f = rho^H x."""
+    n = H.shape[0]
+    N = n // 2
+    w, V = np.linalg.eig(H)
+    order = np.argsort(w.real, kind="stable")
+    w, V = w[order], V[:, order]
+    V = V / np.linalg.norm(V, axis=0)                         # unit columns (3337-3343)
+    J = np.r_[np.ones(N), -np.ones(N)]
+    rho = np.asarray(rho_g0, dtype=np.complex128)
+    S = V.conj().T @ V
+    b = np.linalg.solve(S, V.conj().T @ (J * rho))            # S^{-1} V^H J rho
+    a = V.conj().T @ rho                                      # V^H rho
+    om = np.asarray(omega, dtype=np.float64)
+    chi = (np.conj(a)[None, :] * b[None, :] / (om[:, None] - w[None, :] + 1j * gamma)).sum(axis=1)
+    eps = 1.0 - F * chi
+    jn = np.einsum("il,i,il->l", V.conj(), J, V).real         # x^H J x of the unit vectors
+    X = V / np.sqrt(np.abs(jn))
+    f = X.T @ np.conj(rho)
+    return {"E": w.real, "E_imag": w.imag, "X": X, "f": f, "jnorm_sign": np.sign(jn),
+            "eps2": eps.imag, "eps1": eps.real}
+
+
 def solve(prob, omega, gamma, band_states=None, want_vectors=True, timings=None, **overrides):
     """Whole reference path on the CPU: bands -> build -> zheevd -> oscillators -> eps."""
     t0 = time.perf_counter()
@@ -146,6 +176,16 @@ def solve(prob, omega, gamma, band_states=None, want_vectors=True, timings=None,
     N = prob.n_bse
     ng0 = prob.ng // 2
     out = {"bands": band_states, "H": H, "rho": rho}
+    p = prob.params.replace(**overrides) if overrides else prob.params
+    if p.tamm_dancoff == 0 and not p.ipa:
+        F = prefactor(prob, **overrides)
+        res = solve_coupled(H, rho[:, ng0], F, omega, gamma)
+        t3 = time.perf_counter()
+        out.update(E=res["E"], E_opt=res["E"], A=res["X"], f=res["f"], F=F, eps2=res["eps2"], eps1=res["eps1"],
+                   E_imag=res["E_imag"])
+        if timings is not None:
+            timings.update(bands=t1 - t0, build=t2 - t1, eig=t3 - t2, eps=0.0)
+        return out
     if prob.model.n_spin == 2:
         H0, H1 = split_blocks(H, N)
         E0 = eigh(H0, eigvals_only=True)

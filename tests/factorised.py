@@ -123,3 +123,48 @@ def build_factorised(prob, bands):
         B = H.reshape(4, N, 4, N)
         H = np.einsum("il,lakb,kj->iajb", U, B, U).reshape(NH, NH)
     return H, rho_rows
+
+
+def coupling_factorised(prob, bands):
+    """Coupling block B (N x N) of the full BSE, spinless, in the factorised form the CUDA
+    coupling kernel evaluates:
+      B_d[r1,r2] = -1/(V nk) sum_ab P[r1,(ba)] conj(Phi_ab(k2-k1)) P[r2,(ab)]
+      B_x[r1,r2] =  sf/(V nk) sum_ab P[r1,(aa)] X_ab P[r2,(bb)],
+      X_ab = sum_{G != G0} v(q+G) e^{i(G+q).(tau_a - tau_b)},
+    against the oracle's loops over stored densities (add_coupling_part,
+    bse.version13.cpp:2929-3040)."""
+    ec, ev, cc, cv = bands
+    m, p = prob.model, prob.params
+    nk, nc, nv, nw, ng = prob.nk, p.nc, p.nv, m.nw, prob.ng
+    N = nk * nc * nv
+    vol, area, normal, lz = _geometry(m.lattice)
+    q = np.asarray(p.q, dtype=float)
+    G = prob.g_cart
+    K = prob.k_cart
+    g0 = ng // 2
+    tau = m.centres[0]                                                     # (nw, 3)
+    A1 = np.conj(cc[:, :, None, :, None]) * cv[:, None, :, None, :]       # P[k,c,v,a,b]
+    # exchange
+    sf = p.spin_factor if p.spin_factor >= 0 else 2
+    vg = _coulomb(p, G + q, normal, lz)
+    vg[g0] = 0.0
+    d = tau[:, None, :] - tau[None, :, :]                                  # [a,b,3]
+    X = np.einsum("g,gab->ab", vg, np.exp(1j * np.einsum("gi,abi->gab", G + q, d)))
+    Pd = np.einsum("kcvaa->cvka", A1).reshape(N, nw)                       # P[r,(aa)]
+    B = sf / (nk * vol) * (Pd @ X @ Pd.T)
+    # direct
+    fw = -1.0 / (vol * nk)
+    dk = K[None, :, :] - K[:, None, :]
+    ndk = np.linalg.norm(dk, axis=-1)
+    x = dk[:, :, None, :] + G[None, None, :, :]
+    if p.w_kind == 2:
+        W = _coulomb(p, x, normal, lz)
+    else:
+        W = (p.inv_eps * _coulomb(p, x, normal, lz)) if p.w_kind == 0 else _rk(p, x, normal, lz)
+        avg = _cell_avg(p, vol, area, lz, nk)
+        avg = p.inv_eps * avg if p.w_kind == 0 else avg
+        W[:, :, g0] = np.where(ndk > MINVAL, W[:, :, g0], avg)
+    phase = np.exp(-1j * np.einsum("xygi,abi->xygab", x, d))
+    Phi = np.einsum("xyg,xygab->xyab", W, phase)
+    Bd = fw * np.einsum("xcvba,xyab,yCVab->cvxCVy", A1, np.conj(Phi), A1)
+    return B + Bd.reshape(N, N)

@@ -63,9 +63,31 @@ def test_rejects_nan(synth, gpu):
     assert st == -1 and "NaN" in msg
 
 
-def test_rejects_coupling_block(synth, gpu):
-    st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0)
-    assert st == -1 and "Tamm" in msg
+def test_full_bse_validation(synth, gpu):
+    """tamm_dancoff = 0 (coupling block): FP64, n_spin = 1; other values are rejected."""
+    st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=2)
+    assert st == -1 and "tamm_dancoff" in msg
+    st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0, precision=1)
+    assert st == -1 and "FP64" in msg
+    st, msg = _create(gpu, synth.collinear_problem(grid=2), tamm_dancoff=0)
+    assert st == -1 and "n_spin" in msg
+    st, _ = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0)
+    assert st in (0, -2)
+    st, _ = _create(gpu, synth.collinear_problem(grid=2), tamm_dancoff=0, ipa=1, precision=1)
+    assert st in (0, -2)                      # no kernel: the coupling flag has no effect
+
+
+def test_full_bse_sizes(synth, gpu):
+    from bse_gb300.capi import Marshalled
+    lib = gpu.load()
+    prob = synth.hbn_problem(grid=3)
+    out = [C.c_int64() for _ in range(4)]
+    for tda, factor in ((1, 1), (0, 2)):
+        m = Marshalled(prob, tamm_dancoff=tda)
+        assert lib.bse_sizes(C.byref(m.model), C.byref(m.params), *[C.byref(x) for x in out]) == 0
+        N = prob.n_bse
+        assert [x.value for x in out] == [N, factor * N, factor * N, factor * N]
+        assert (m.n_exc, m.n_rho, m.n_h, m.n_opt) == (factor * N,) * 4
 
 
 def test_rejects_zero_q(synth, gpu):

@@ -1,0 +1,131 @@
+"""CPU tests of the oracle's full BSE (tamm_dancoff = 0: the coupling block of
+add_coupling_part, bse.version13.cpp:2929-3040, and the non-TDA spectrum, 3504-3522 and
+3607-3620).  They pin the restatement the GPU path is checked against:
+  - the resonant block and rho_cv are the Tamm-Dancoff ones, the anti-resonant blocks are
+    -conj(A) (2917-2923) and -conj(B)^T (3035-3038), B is symmetric up to the O(q) shift of
+    the exchange phases;
+  - the coupling block equals the factorised lattice-sum form the CUDA kernel evaluates;
+  - the three routes to the spectrum agree: the reference's eig_gen + inverse overlap matrix,
+    the J-normalised sum over pairs, and direct linear solves of (w - H + i gamma) x = J rho;
+  - eigenvalues come in +-E pairs, the J-norm of each eigenvector has the sign of E;
+  - gauge invariance of the spectrum and of eps2 (decisions Q25, Q26);
+  - with B = 0 the positive half of the spectrum is the Tamm-Dancoff one.
+"""
+import numpy as np
+import pytest
+
+from factorised import coupling_factorised
+
+OMEGA = np.arange(400) * 8.0 / 400
+GAMMA = 0.05
+
+
+def _prob(synth, name):
+    return {"hbn6": lambda: synth.hbn_problem(grid=6), "hbn8": lambda: synth.hbn_problem(grid=8),
+            "cubic3": lambda: synth.cubic3d_problem(grid=3), "orb8_3": lambda: synth.orb8_problem(grid=3),
+            "mag4_4": lambda: synth.magnetic4_problem(grid=4)}[name]()
+
+
+def _random_phases(bands, seed):
+    ec, ev, cc, cv = bands
+    rng = np.random.default_rng(seed)
+    pc = np.exp(1j * rng.uniform(0, 2 * np.pi, cc.shape[:2]))[..., None]
+    pv = np.exp(1j * rng.uniform(0, 2 * np.pi, cv.shape[:2]))[..., None]
+    return ec, ev, cc * pc, cv * pv
+
+
+@pytest.mark.parametrize("name", ["hbn6", "cubic3", "mag4_4"])
+def test_block_structure(synth, oracle, name):
+    prob = _prob(synth, name)
+    bands = oracle.bands(prob)
+    H, rho = oracle.build(prob, bands, tamm_dancoff=0)
+    Ht, rhot = oracle.build(prob, bands)
+    N = prob.n_bse
+    g0 = prob.ng // 2
+    assert H.shape == (2 * N, 2 * N) and rho.shape == (2 * N, prob.ng)
+    A, B = H[:N, :N], H[:N, N:]
+    assert np.array_equal(A, Ht) and np.array_equal(rho[:N], rhot)
+    assert np.array_equal(H[N:, N:], -A.conj())
+    assert np.array_equal(H[N:, :N], -B.conj().T)
+    # B^T = B up to the q-shift of the exchange phases e^{i(G+q).tau} (q = 1e-5 x)
+    assert np.abs(B - B.T).max() < 1e-8 * np.abs(B).max()
+    # dipole column of rho_vc: i q.<v|r|c> = -conj(i q.<c|r|v>)  (Q25)
+    assert np.abs(rho[N:, g0] + rho[:N, g0].conj()).max() < 1e-14
+
+
+@pytest.mark.parametrize("name", ["hbn6", "cubic3", "orb8_3", "mag4_4"])
+def test_coupling_factorised_agrees(synth, oracle, name):
+    """The oracle's loops over stored all-pairs densities and the factorised form (what the
+    CUDA coupling kernel evaluates) give the same B."""
+    prob = _prob(synth, name)
+    bands = oracle.bands(prob)
+    H, _ = oracle.build(prob, bands, tamm_dancoff=0)
+    N = prob.n_bse
+    B = coupling_factorised(prob, bands)
+    assert np.abs(B - H[:N, N:]).max() < 1e-12 * np.abs(B).max()
+
+
+@pytest.mark.parametrize("name", ["hbn6", "cubic3", "mag4_4"])
+def test_spectrum_routes_agree(synth, oracle, name):
+    prob = _prob(synth, name)
+    H, rho = oracle.build(prob, tamm_dancoff=0)
+    N = prob.n_bse
+    F = oracle.prefactor(prob)
+    r = rho[:, prob.ng // 2]
+    res = oracle.solve_coupled(H, r, F, OMEGA, GAMMA)
+    E = res["E"]
+    # M = J H positive definite here: real spectrum in +-E pairs, J-norm sign = sign(E)
+    J = np.r_[np.ones(N), -np.ones(N)]
+    assert np.linalg.eigvalsh(J[:, None] * H).min() > 0
+    assert np.abs(res["E_imag"]).max() < 1e-10 * np.abs(E).max()
+    assert np.abs(E[:N][::-1] + E[N:]).max() < 1e-9 * np.abs(E).max()
+    assert np.array_equal(res["jnorm_sign"], np.sign(E))
+    # J-normalised pair sum == augmentation-matrix route
+    chi = (np.sign(E) * np.abs(res["f"]) ** 2 / (OMEGA[:, None] - E[None, :] + 1j * GAMMA)).sum(axis=1)
+    e2 = (1 - F * chi).imag
+    assert np.linalg.norm(e2 - res["eps2"]) < 1e-10 * np.linalg.norm(res["eps2"])
+    # == direct resolvent rho^H (w - H + i gamma)^{-1} J rho
+    for w in OMEGA[::40]:
+        x = np.linalg.solve((w + 1j * GAMMA) * np.eye(2 * N) - H, J * r)
+        ref = (1 - F * (r.conj() @ x)).imag
+        s = np.searchsorted(OMEGA, w)
+        assert abs(ref - res["eps2"][s]) < 1e-10 * np.abs(res["eps2"]).max()
+
+
+@pytest.mark.parametrize("name", ["hbn6", "cubic3"])
+def test_gauge_invariance(synth, oracle, name):
+    prob = _prob(synth, name)
+    bands = oracle.bands(prob)
+    r0 = oracle.solve(prob, OMEGA, GAMMA, band_states=bands, tamm_dancoff=0)
+    r1 = oracle.solve(prob, OMEGA, GAMMA, band_states=_random_phases(bands, 5), tamm_dancoff=0)
+    assert np.abs(r0["E"] - r1["E"]).max() < 1e-10
+    assert np.linalg.norm(r0["eps2"] - r1["eps2"]) < 1e-9 * np.linalg.norm(r0["eps2"])
+
+
+def test_no_coupling_limit(synth, oracle):
+    """B = 0: the positive eigenvalues are the Tamm-Dancoff ones and eps2 is the TDA spectrum
+    plus the anti-resonant term -F sum |f|^2 gamma / ((w + E)^2 + gamma^2)."""
+    prob = _prob(synth, "hbn6")
+    H, rho = oracle.build(prob, tamm_dancoff=0)
+    N = prob.n_bse
+    H[:N, N:] = 0
+    H[N:, :N] = 0
+    F = oracle.prefactor(prob)
+    res = oracle.solve_coupled(H, rho[:, prob.ng // 2], F, OMEGA, GAMMA)
+    tda = oracle.solve(prob, OMEGA, GAMMA)
+    assert np.abs(res["E"][N:] - tda["E"]).max() < 1e-10
+    anti = F * (np.abs(tda["f"]) ** 2 * GAMMA / ((OMEGA[:, None] + tda["E"][None, :]) ** 2 + GAMMA ** 2)).sum(axis=1)
+    assert np.abs(res["eps2"] - (tda["eps2"] - anti)).max() < 1e-10 * np.abs(tda["eps2"]).max()
+
+
+def test_ipa_ignores_coupling(synth, oracle):
+    """ipa = 1 has no kernel: tamm_dancoff = 0 changes nothing (3346-3365, 3490-3493)."""
+    prob = _prob(synth, "hbn6")
+    a = oracle.solve(prob, OMEGA, GAMMA, ipa=1)
+    b = oracle.solve(prob, OMEGA, GAMMA, ipa=1, tamm_dancoff=0)
+    assert np.array_equal(a["E"], b["E"]) and np.array_equal(a["eps2"], b["eps2"])
+
+
+def test_collinear_coupling_rejected(synth, oracle):
+    with pytest.raises(oracle.OracleError):
+        oracle.build(synth.collinear_problem(grid=3), tamm_dancoff=0)
