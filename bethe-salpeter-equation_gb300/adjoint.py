@@ -230,10 +230,18 @@ def reference_loss(pm: ParamModel, prob_template: Problem, theta, r0, omega, wei
 # ---------------------------------------------------------------------------- hand-written backward
 
 
+def _require_tda(prob: Problem):
+    """The adjoint differentiates the Tamm-Dancoff spectrum (Hermitian H, one exciton block)."""
+    p = prob.params
+    if p.tamm_dancoff == 0 and not p.ipa:
+        raise ValueError("the eps2 adjoint covers the Tamm-Dancoff BSE only (tamm_dancoff = 1)")
+
+
 def backward(pm: ParamModel, prob: Problem, fwd: Dict[str, np.ndarray], omega, weights, gamma,
              device=None):
     """dL/dtheta (n_params) and dL/dr0 for L = sum_s weights_s eps2(omega_s), from the forward
     intermediates: E (N), A (N x N), f (N), bands (e_c, e_v, c_c, c_v as from bse_get_bands)."""
+    _require_tda(prob)
     dev = device or (torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu"))
     p = prob.params
     nv, nc, nk = p.nv, p.nc, prob.nk
@@ -350,6 +358,7 @@ def backward(pm: ParamModel, prob: Problem, fwd: Dict[str, np.ndarray], omega, w
 def gpu_forward(pm: ParamModel, prob_template: Problem, theta, r0, omega, gamma, want_vectors=True):
     """FP64 forward through the CUDA library: E, A, f, bands, eps2."""
     from . import gpu
+    _require_tda(prob_template)
     prob = Problem(model=pm.model(theta), k_cart=prob_template.k_cart, g_cart=prob_template.g_cart,
                    params=prob_template.params.replace(rk_r0=float(r0)), k_cryst=prob_template.k_cryst,
                    grid=prob_template.grid)

@@ -112,3 +112,16 @@ def test_autograd_function_wrapper(synth):
     assert abs(float(L) - L_ref) <= 1e-9 * abs(L_ref)
     assert np.abs(th.grad.numpy() - g_th).max() <= 1e-6 * np.abs(g_th).max()
     assert abs(float(rr.grad) - g_r0) <= 1e-6 * abs(g_r0)
+
+
+def test_adjoint_rejects_full_bse(synth):
+    """The adjoint differentiates the Tamm-Dancoff spectrum; a full-BSE problem is refused
+    before any device work."""
+    from bse_gb300.adjoint import backward, gpu_forward
+    pm, prob, theta, r0, w = _setup(synth, 3)
+    full = prob.__class__(model=prob.model, k_cart=prob.k_cart, g_cart=prob.g_cart,
+                          params=prob.params.replace(tamm_dancoff=0), k_cryst=prob.k_cryst, grid=prob.grid)
+    with pytest.raises(ValueError, match="Tamm-Dancoff"):
+        gpu_forward(pm, full, theta, r0, OMEGA, GAMMA)
+    with pytest.raises(ValueError, match="Tamm-Dancoff"):
+        backward(pm, full, {}, OMEGA, w, GAMMA, device=torch.device("cpu"))
