@@ -5,6 +5,8 @@ the oracle's FP64 results on two small seeded workloads (regression vectors for 
 restatement; the GPU parity tests compare against the live oracle):
   hbn4_golden.npz   hBN-like 2-band model, 4x4 grid, RK W + bare 2-D V, N = 16
   coll3_golden.npz  collinear two-channel model, 3x3 grid, N = 9 (H is 36 x 36)
+  hbn4_full_golden.npz  the hbn4 workload as a full BSE (tamm_dancoff = 0: coupling block,
+                    2N = 32 eigenvalues, non-TDA spectrum)
 Run: python tests/golden/make_golden.py
 """
 import os
@@ -31,6 +33,9 @@ def main():
     r = orc.solve(synth.collinear_problem(grid=3), omega, gamma)
     np.savez(os.path.join(HERE, "coll3_golden.npz"), omega=omega, gamma=gamma, E=r["E"], eps2=r["eps2"],
              eps1=r["eps1"])
+    r = orc.solve(synth.hbn_problem(grid=4), omega, gamma, tamm_dancoff=0)
+    np.savez(os.path.join(HERE, "hbn4_full_golden.npz"), omega=omega, gamma=gamma, E=r["E"], eps2=r["eps2"],
+             eps1=r["eps1"], absH=np.abs(r["H"]), absf=np.abs(r["f"]))
     print("wrote golden vectors")
 
 

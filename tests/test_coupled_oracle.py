@@ -11,6 +11,8 @@ add_coupling_part, bse.version13.cpp:2929-3040, and the non-TDA spectrum, 3504-3
   - gauge invariance of the spectrum and of eps2 (decisions Q25, Q26);
   - with B = 0 the positive half of the spectrum is the Tamm-Dancoff one.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -129,3 +131,11 @@ def test_ipa_ignores_coupling(synth, oracle):
 def test_collinear_coupling_rejected(synth, oracle):
     with pytest.raises(oracle.OracleError):
         oracle.build(synth.collinear_problem(grid=3), tamm_dancoff=0)
+
+
+def test_golden_vectors(synth, oracle):
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hbn4_full_golden.npz"))
+    r = oracle.solve(synth.hbn_problem(grid=4), g["omega"], float(g["gamma"]), tamm_dancoff=0)
+    assert np.abs(r["E"] - g["E"]).max() < 1e-12
+    assert np.abs(r["eps2"] - g["eps2"]).max() < 1e-12 * np.abs(g["eps2"]).max()
+    assert np.abs(np.abs(r["H"]) - g["absH"]).max() < 1e-12 * g["absH"].max()
