@@ -198,7 +198,8 @@ int bse_stage_times(const bse_ctx* ctx, double* ms, int32_t n);
  * exit.  Limits below; larger sizes return BSE_ERR_BAD_INPUT.  The first call on a device
  * resolves the array's address: make it before any stream capture.  Calls share the array:
  * calls that overlap on the GPU race.  stream: a cudaStream_t, or NULL for the default stream.
- * prefactor is F = conv / (V nk) of bse_eps. */
+ * prefactor is F = conv / (V nk) of bse_eps.  The Tamm-Dancoff form: a full-BSE spectrum (signed
+ * anti-resonant pairs) goes through bse_eps. */
 #define BSE_EPS_NOALLOC_MAX_EXCITONS 131072
 #define BSE_EPS_NOALLOC_MAX_OMEGA 16384
 int bse_eps_noalloc(int64_t n_exc, const double* e, const double* f, double prefactor,

@@ -109,3 +109,34 @@ def test_sizes(synth, gpu):
     assert lib.bse_sizes(C.byref(m.model), C.byref(m.params), *[C.byref(v) for v in vals]) == 0
     N = 9
     assert [v.value for v in vals] == [N, 4 * N, 2 * N, 4 * N]
+
+
+def test_null_context_is_an_error_not_a_crash(gpu):
+    """Every entry point taking a context returns BSE_ERR_BAD_INPUT for NULL (checked before any
+    device call), the destructors accept NULL, and the allocation-free spectrum validates its
+    sizes first."""
+    lib = gpu.load()
+    null = C.c_void_p()
+    dp = C.POINTER(C.c_double)()
+    assert lib.bse_compute_bands(null) == -1
+    assert lib.bse_get_bands(null, dp, dp, dp, dp) == -1
+    assert lib.bse_set_bands(null, dp, dp, dp, dp) == -1
+    assert lib.bse_build_kernel(null, dp, dp) == -1
+    assert lib.bse_diagonalize(null, dp, dp) == -1
+    assert lib.bse_oscillators(null, dp) == -1
+    assert lib.bse_eps(null, dp, 0, 0.05, dp, dp) == -1
+    assert lib.bse_solve(null, dp, 0, 0.05, dp, dp, dp) == -1
+    assert lib.bse_stage_times(null, dp, 0) == -1
+    assert lib.bse_diagnostics(null, dp, 0) == -1
+    assert lib.bse_kernel_launches(null) == 0
+    lib.bse_reset_kernel_launches(null)
+    lib.bse_destroy(null)
+    assert lib.bse_solve_many(C.POINTER(C.c_void_p)(), 1, dp, 0, 0.05, dp, dp, 1) == -1
+    assert lib.bse_sizes(None, None, None, None, None, None) == -1
+    assert isinstance(lib.bse_last_error(None), bytes)
+    one = np.ones(4)
+    assert lib.bse_eps_noalloc(0, one.ctypes.data_as(C.POINTER(C.c_double)), one.ctypes.data_as(C.POINTER(C.c_double)),
+                               1.0, one.ctypes.data_as(C.POINTER(C.c_double)), 4, 0.05,
+                               one.ctypes.data_as(C.POINTER(C.c_double)), dp, None) == -1
+    assert b"n_exc" in lib.bse_last_error(None)
+    assert lib.bse_eps_noalloc(4, dp, dp, 1.0, dp, 4, 0.05, dp, dp, None) == -1
