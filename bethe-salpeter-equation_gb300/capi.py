@@ -78,8 +78,8 @@ class Marshalled:
         self.n_rho = (S + 1) * self.N
         self.n_exc = (3 * S + 1) * self.N
         self.n_opt = (S + 1) * self.N     # optically active block (spinless N, collinear 2N)
-        if self.coupled:                  # full BSE: resonant + anti-resonant exciton rows, all 2N pairs
-            self.n_h = self.n_rho = self.n_exc = self.n_opt = 2 * self.N
+        if self.coupled:                  # full BSE: resonant + anti-resonant exciton rows, every size doubles
+            self.n_h, self.n_rho, self.n_exc, self.n_opt = 2 * self.n_h, 2 * self.n_rho, 2 * self.n_exc, 2 * self.n_opt
 
     def band_buffers(self):
         return (np.zeros((2, self.nk, self.nc)), np.zeros((2, self.nk, self.nv)),

@@ -251,11 +251,11 @@ int bse_sizes(const bse_model* m, const bse_params* p, int64_t* n_bse, int64_t* 
     if (!m || !p) return BSE_ERR_BAD_INPUT;
     const int64_t N = (int64_t)m->n_k * p->nc * p->nv;
     const int S = m->n_spin - 1;
-    const bool coupled = p->tamm_dancoff == 0 && !p->ipa;   // full BSE: 2N rows everywhere
+    const int64_t x = (p->tamm_dancoff == 0 && !p->ipa) ? 2 : 1;   // full BSE: every size doubles
     if (n_bse) *n_bse = N;
-    if (n_exc) *n_exc = coupled ? 2 * N : (3 * S + 1) * N;
-    if (n_rho) *n_rho = coupled ? 2 * N : (S + 1) * N;
-    if (n_h) *n_h = coupled ? 2 * N : (3 * S + 1) * N;
+    if (n_exc) *n_exc = x * (3 * S + 1) * N;
+    if (n_rho) *n_rho = x * (S + 1) * N;
+    if (n_h) *n_h = x * (3 * S + 1) * N;
     return BSE_OK;
 }
 

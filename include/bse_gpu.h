@@ -116,7 +116,8 @@ int bse_version(void);
 
 /* Sizes derived from model+params: n_exc = (3*spin+1)*N eigenvalues, n_rho = (spin+1)*N
  * pair-density rows, n_h = dimension of the (full, before the spin split) BSE matrix.
- * Full BSE (tamm_dancoff = 0): n_exc = n_rho = n_h = 2N (resonant rows, then anti-resonant). */
+ * Full BSE (tamm_dancoff = 0): each doubles (resonant rows, then anti-resonant; the sizes of the
+ * reference's collinear full BSE are reported although bse_create accepts n_spin = 1 only). */
 int bse_sizes(const bse_model* model, const bse_params* params,
               int64_t* n_bse, int64_t* n_exc, int64_t* n_rho, int64_t* n_h);
 

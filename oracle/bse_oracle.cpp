@@ -290,8 +290,8 @@ Dims dims(const bse_model* m, const bse_params* p) {
     d.nv = p->nv; d.nc = p->nc; d.S = d.ns - 1;
     d.N = (int64_t)d.nk * d.nc * d.nv;
     d.coupled = p->tamm_dancoff == 0 && !p->ipa;
-    d.n_h = d.coupled ? 2 * d.N : (int64_t)(3 * d.S + 1) * d.N;
-    d.n_rho = d.coupled ? 2 * d.N : (int64_t)(d.S + 1) * d.N;
+    d.n_h = (int64_t)(d.coupled ? 2 : 1) * (3 * d.S + 1) * d.N;
+    d.n_rho = (int64_t)(d.coupled ? 2 : 1) * (d.S + 1) * d.N;
     return d;
 }
 
@@ -332,12 +332,13 @@ double oracle_prefactor(const bse_model* m, const bse_params* p) {
 int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, const double* e_v,
                  const double* c_c_in, const double* c_v_in, double* h_out, double* rho_out) {
     Dims d = dims(m, p);
-    if (d.coupled && d.S) return BSE_ERR_BAD_INPUT;     // coupling block: spinless / spin-orbital basis only
     Geometry geo = make_geometry(m);
     const cd* Cc = (const cd*)c_c_in;
     const cd* Cv = (const cd*)c_v_in;
     const int nk = d.nk, nc = d.nc, nv = d.nv, ng = d.ng, nw = d.nw, nb = d.nb, S = d.S;
     const int64_t N = d.N, NH = d.n_h;
+    const int64_t NA = (int64_t)(3 * S + 1) * N;   // resonant block (the whole matrix without coupling)
+    const int64_t NR = (int64_t)(S + 1) * N;       // rho_cv rows
     const int g0 = ng / 2;
     cd* H = (cd*)h_out;
     cd* rho = (cd*)rho_out;
@@ -375,17 +376,18 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                         rho[(s * N + (int64_t)c * nv * nk + (int64_t)v * nk + k) + d.n_rho * g] = acc;
                     }
 
-    // rho_vc rows N..2N-1 of the coupled problem: pull_values(q, -q, 0, ..., left = v, right = c,
-    // reverse = 1) of add_coupling_part (2937, stored at 2950), same row layout c*nv*nk + v*nk + k; Q25
+    // rho_vc rows NR + s*N + r of the coupled problem: pull_values(q, -q, 0, ..., left = v, right = c,
+    // reverse = 1) of add_coupling_part (2937, stored at 2950), same row layout s*N + c*nv*nk + v*nk + k; Q25
     if (d.coupled) {
-#pragma omp parallel for collapse(2) schedule(static)
+#pragma omp parallel for collapse(3) schedule(static)
+        for (int s = 0; s <= S; s++)
         for (int c = 0; c < nc; c++)
             for (int v = 0; v < nv; v++)
                 for (int g = 0; g < ng; g++)
                     for (int k = 0; k < nk; k++) {
                         cd acc = 0;
                         for (int a = 0; a < nw; a++) {
-                            const double* t = tau(0, a);
+                            const double* t = tau(s, a);
                             cd mel;
                             if (g == g0 && p->small_momentum) {
                                 mel = cd(0.0, qhat[0] * t[0] + qhat[1] * t[1] + qhat[2] * t[2]);
@@ -394,9 +396,9 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                                 double ph = t[0] * (G[0] + q[0]) + t[1] * (G[1] + q[1]) + t[2] * (G[2] + q[2]);
                                 mel = cd(std::cos(ph), std::sin(ph));
                             }
-                            acc += std::conj(Cv[((size_t)k * nv + v) * nb + a]) * mel * Cc[((size_t)k * nc + c) * nb + a];
+                            acc += std::conj(Cv[((size_t)k * nv + v) * nb + s * nw + a]) * mel * Cc[((size_t)k * nc + c) * nb + s * nw + a];
                         }
-                        rho[(N + (int64_t)c * nv * nk + (int64_t)v * nk + k) + d.n_rho * g] = acc;
+                        rho[(NR + s * N + (int64_t)c * nv * nk + (int64_t)v * nk + k) + d.n_rho * g] = acc;
                     }
     }
 
@@ -499,27 +501,36 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
         }
 
         if (d.coupled) {
-            // coupling block B = H[0:N, N:2N] (add_coupling_part 2929-3040, spinless).
-            // exchange as written (2940-2967): B[r, s] += fx sum_{G != G0} v_G rho_cv[r, G] conj(rho_vc[s, G])
-#pragma omp parallel for schedule(static)
-            for (int64_t s2 = 0; s2 < N; s2++)
-                for (int64_t r = 0; r < N; r++) {
-                    cd acc = 0;
-                    for (int g = 0; g < ng; g++) {
-                        if (g == g0) continue;
-                        acc += (fx * vg[g]) * std::conj(rho[(N + s2) + d.n_rho * g]) * rho[r + d.n_rho * g];
-                    }
-                    H[r + NH * (N + s2)] += acc;
-                }
-            // direct (2971-3033): rho_kk_cv[c2][v1][k2][k1] (2975, left c at k2, right v at k1) and
-            // rho_kk_vc[v2][c1][k2][k1] (2976, left v at k2, right c at k1); Q26
+            // coupling block B = H[0:NA, NA:2NA] (add_coupling_part 2929-3040).  Exchange as written
+            // (2940-2967), spin blocks i*3, j*3 as the resonant exchange:
+            //   B[i*3N + r, j*3N + s] += fx sum_{G != G0} v_G rho_cv[i*N + r, G] conj(rho_vc[j*N + s, G])
+#pragma omp parallel for collapse(2) schedule(static)
+            for (int j = 0; j <= S; j++)
+                for (int64_t s2 = 0; s2 < N; s2++)
+                    for (int i = 0; i <= S; i++)
+                        for (int64_t r = 0; r < N; r++) {
+                            cd acc = 0;
+                            for (int g = 0; g < ng; g++) {
+                                if (g == g0) continue;
+                                acc += (fx * vg[g]) * std::conj(rho[(NR + j * N + s2) + d.n_rho * g]) * rho[(i * N + r) + d.n_rho * g];
+                            }
+                            H[(i * 3 * N + r) + NH * (NA + j * 3 * N + s2)] += acc;
+                        }
+            // direct (2971-3033): exciton spin block sp (v-spin sv1, c-spin sc1) couples to block sp2 = sp
+            // for 0 and 3, 3 - sp for the spin-flip blocks (2986-2989), through
+            // rho_kk_cv[sv1][c2][v1][k2][k1] (2975, left c at k2, right v at k1) and
+            // rho_kk_vc[sc1][v2][c1][k2][k1] (2976, left v at k2, right c at k1); Q26
+            const int exc_spin_b[4][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}};   // (v-spin, c-spin) 2522-2526
 #pragma omp parallel
             {
                 std::vector<cd> rcv((size_t)nc * nv * nk * ng), rvc((size_t)nv * nc * nk * ng);
                 std::vector<cd> T((size_t)nk * ng);
                 std::vector<double> W((size_t)nk * ng);
-#pragma omp for schedule(dynamic)
+#pragma omp for collapse(2) schedule(dynamic)
+                for (int sp = 0; sp < 3 * S + 1; sp++)
                 for (int k1 = 0; k1 < nk; k1++) {
+                    const int sv1 = exc_spin_b[sp][0], sc1 = exc_spin_b[sp][1];
+                    const int sp2 = (sp == 0 || sp == 3 * S) ? sp : 3 - sp;
                     for (int k2 = 0; k2 < nk; k2++) {
                         double dk[3] = {Kv(k2)[0] - Kv(k1)[0], Kv(k2)[1] - Kv(k1)[1], Kv(k2)[2] - Kv(k1)[2]};
                         for (int g = 0; g < ng; g++) W[(size_t)k2 * ng + g] = w_diag(p, geo, nk, dk, Gv(g), g == g0);
@@ -530,13 +541,17 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                                 for (int g = 0; g < ng; g++) {
                                     cd acc = 0, acc2 = 0;
                                     for (int a = 0; a < nw; a++) {
-                                        const double* t = tau(0, a);
+                                        const double* t = tau(sv1, a);
                                         double ph = 0;
                                         for (int x = 0; x < 3; x++) ph += t[x] * (Gv(g)[x] + Kv(k2)[x] - Kv(k1)[x]);
-                                        const cd e(std::cos(ph), std::sin(ph));
-                                        acc += std::conj(Cc[((size_t)k2 * nc + c2) * nb + a]) * e * Cv[((size_t)k1 * nv + v1) * nb + a];
-                                        // the same loop fills rho_kk_vc[v1][c2] (left v1 at k2, right c2 at k1)
-                                        acc2 += std::conj(Cv[((size_t)k2 * nv + v1) * nb + a]) * e * Cc[((size_t)k1 * nc + c2) * nb + a];
+                                        acc += std::conj(Cc[((size_t)k2 * nc + c2) * nb + sv1 * nw + a]) * cd(std::cos(ph), std::sin(ph)) *
+                                               Cv[((size_t)k1 * nv + v1) * nb + sv1 * nw + a];
+                                        // the same loop fills rho_kk_vc[v1][c2] (left v1 at k2, right c2 at k1), channel sc1
+                                        const double* t2 = tau(sc1, a);
+                                        double ph2 = 0;
+                                        for (int x = 0; x < 3; x++) ph2 += t2[x] * (Gv(g)[x] + Kv(k2)[x] - Kv(k1)[x]);
+                                        acc2 += std::conj(Cv[((size_t)k2 * nv + v1) * nb + sc1 * nw + a]) * cd(std::cos(ph2), std::sin(ph2)) *
+                                                Cc[((size_t)k1 * nc + c2) * nb + sc1 * nw + a];
                                     }
                                     rcv[(((size_t)c2 * nv + v1) * nk + k2) * ng + g] = acc;
                                     rvc[(((size_t)v1 * nc + c2) * nk + k2) * ng + g] = acc2;
@@ -554,7 +569,7 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                                         for (int g = 0; g < ng; g++)
                                             acc += fw * T[(size_t)k2 * ng + g] * std::conj(rvc[(((size_t)v2 * nc + c1) * nk + k2) * ng + g]);
                                         const int64_t r2 = (int64_t)c2 * nv * nk + (int64_t)v2 * nk + k2;
-                                        H[r1 + NH * (N + r2)] += acc;
+                                        H[(sp * N + r1) + NH * (NA + sp2 * N + r2)] += acc;
                                     }
                             }
                         }
@@ -577,15 +592,6 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                     }
                 }
 
-    if (d.coupled) {
-        // anti-resonant block -conj(A) (2917-2923) and H[N:2N, 0:N] = -conj(B)^T (3035-3038)
-        for (int64_t j = 0; j < N; j++)
-            for (int64_t i = 0; i < N; i++) {
-                H[(N + i) + NH * (N + j)] = -std::conj(H[i + NH * j]);
-                H[(N + i) + NH * j] = -std::conj(H[j + NH * (N + i)]);
-            }
-    }
-
     if (S) {
         // spin_transformation (3048-3117), out of place (Q24): U = diag(1, [[1,1],[1,-1]]/sqrt2, 1)
         const double h = 1.0 / std::sqrt(2.0);
@@ -598,11 +604,23 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                     for (int kb = 0; kb < 4; kb++) {
                         double w = U[bi][l] * U[kb][bj];
                         if (w == 0.0) continue;
-                        for (int64_t cc = 0; cc < N; cc++)
-                            for (int64_t rr = 0; rr < N; rr++)
-                                Ht[(bi * N + rr) + NH * (bj * N + cc)] += w * H[(l * N + rr) + NH * (kb * N + cc)];
+                        for (int off = 0; off < (d.coupled ? 2 : 1); off++)   // resonant, then coupling (3096-3105)
+                            for (int64_t cc = 0; cc < N; cc++)
+                                for (int64_t rr = 0; rr < N; rr++)
+                                    Ht[(bi * N + rr) + NH * (off * NA + bj * N + cc)] +=
+                                        w * H[(l * N + rr) + NH * (off * NA + kb * N + cc)];
                     }
         std::memcpy(H, Ht.data(), sizeof(cd) * NH * NH);
+    }
+
+    if (d.coupled) {
+        // anti-resonant block -conj(A) (2917-2923, again after the rotation 3111-3114) and
+        // H[NA:2NA, 0:NA] = -conj(B)^T (3035-3038, 3107-3110)
+        for (int64_t j = 0; j < NA; j++)
+            for (int64_t i = 0; i < NA; i++) {
+                H[(NA + i) + NH * (NA + j)] = -std::conj(H[i + NH * j]);
+                H[(NA + i) + NH * j] = -std::conj(H[j + NH * (NA + i)]);
+            }
     }
     return BSE_OK;
 }

@@ -108,6 +108,17 @@ def split_blocks(H, n_bse):
     return H[np.ix_(idx0, idx0)], H[np.ix_(idx1, idx1)]
 
 
+def split_blocks_coupled(H, n_bse):
+    """Collinear full BSE (8N x 8N): H0 = blocks {1,2} and H1 = blocks {0,3} of every quadrant,
+    each 4N x 4N with its own coupling part (common_diagonalization, bse.version13.cpp:3151-3172)."""
+    N = n_bse
+    b0 = np.r_[N:3 * N]
+    b1 = np.r_[0:N, 3 * N:4 * N]
+    idx0 = np.r_[b0, 4 * N + b0]
+    idx1 = np.r_[b1, 4 * N + b1]
+    return H[np.ix_(idx0, idx0)], H[np.ix_(idx1, idx1)]
+
+
 def eigh(H, eigvals_only=False):
     """LAPACK zheevd (or cheevd for complex64), ascending."""
     if eigvals_only:
@@ -181,9 +192,18 @@ def solve(prob, omega, gamma, band_states=None, want_vectors=True, timings=None,
     p = prob.params.replace(**overrides) if overrides else prob.params
     if p.tamm_dancoff == 0 and not p.ipa:
         F = prefactor(prob, **overrides)
-        res = solve_coupled(H, rho[:, ng0], F, omega, gamma)
+        if prob.model.n_spin == 2:
+            # both spin blocks diagonalised (3195, 3204); the spectrum from the spin-conserving H1 (Q17)
+            H0, H1 = split_blocks_coupled(H, N)
+            w0 = np.linalg.eigvals(H0)
+            E0 = np.sort_complex(w0[np.lexsort((w0.imag, w0.real))]).real
+            res = solve_coupled(H1, rho[:, ng0], F, omega, gamma)
+            E_all = np.concatenate([E0, res["E"]])
+        else:
+            res = solve_coupled(H, rho[:, ng0], F, omega, gamma)
+            E_all = res["E"]
         t3 = time.perf_counter()
-        out.update(E=res["E"], E_opt=res["E"], A=res["X"], f=res["f"], F=F, eps2=res["eps2"], eps1=res["eps1"],
+        out.update(E=E_all, E_opt=res["E"], A=res["X"], f=res["f"], F=F, eps2=res["eps2"], eps1=res["eps1"],
                    E_imag=res["E_imag"])
         if timings is not None:
             timings.update(bands=t1 - t0, build=t2 - t1, eig=t3 - t2, eps=0.0)

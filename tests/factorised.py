@@ -126,32 +126,41 @@ def build_factorised(prob, bands):
 
 
 def coupling_factorised(prob, bands):
-    """Coupling block B (N x N) of the full BSE, spinless, in the factorised form the CUDA
-    coupling kernel evaluates:
-      B_d[r1,r2] = -1/(V nk) sum_ab P[r1,(ba)] conj(Phi_ab(k2-k1)) P[r2,(ab)]
-      B_x[r1,r2] =  sf/(V nk) sum_ab P[r1,(aa)] X_ab P[r2,(bb)],
-      X_ab = sum_{G != G0} v(q+G) e^{i(G+q).(tau_a - tau_b)},
-    against the oracle's loops over stored densities (add_coupling_part,
-    bse.version13.cpp:2929-3040)."""
+    """Coupling block B (NA x NA, NA = N spinless or 4N collinear) of the full BSE in factorised
+    form, against the oracle's loops over stored densities (add_coupling_part,
+    bse.version13.cpp:2929-3040):
+      B_d[sp r1, sp2 r2] = -1/(V nk) sum_ab Q[r1,(ab)] conj(Phi^{sv1 sc1}_ab(k2-k1)) R[r2,(ab)],
+          Q[r1,(ab)] = c_v1a(k1)^{sv1} conj(c_c1b(k1))^{sc1},  R[r2,(ab)] = conj(c_c2a(k2))^{sv1} c_v2b(k2)^{sc1},
+          Phi^{st}_ab = sum_G W_G e^{-i(G+dk).(tau^s_a - tau^t_b)}, (sv1, sc1) the spins of block sp,
+          sp2 = sp for blocks 0 and 3, 3 - sp for the spin-flip blocks;
+      B_x[i*3N + r, j*3N + s] = sf/(V nk) sum_ab P_i[r,(aa)] X^{ij}_ab P_j[s,(bb)],
+          X^{ij}_ab = sum_{G != G0} v(q+G) e^{i(G+q).(tau^i_a - tau^j_b)};
+    collinear models then rotate U B U over the four exciton spin blocks."""
     ec, ev, cc, cv = bands
     m, p = prob.model, prob.params
     nk, nc, nv, nw, ng = prob.nk, p.nc, p.nv, m.nw, prob.ng
+    ns = m.n_spin
+    S = ns - 1
     N = nk * nc * nv
+    NA = (3 * S + 1) * N
     vol, area, normal, lz = _geometry(m.lattice)
     q = np.asarray(p.q, dtype=float)
     G = prob.g_cart
     K = prob.k_cart
     g0 = ng // 2
-    tau = m.centres[0]                                                     # (nw, 3)
-    A1 = np.conj(cc[:, :, None, :, None]) * cv[:, None, :, None, :]       # P[k,c,v,a,b]
+    tau = m.centres                                                        # (ns, nw, 3)
+    blk = lambda x, s: x[..., s * nw:(s + 1) * nw]
+    B = np.zeros((NA, NA), np.complex128)
     # exchange
-    sf = p.spin_factor if p.spin_factor >= 0 else 2
+    sf = p.spin_factor if p.spin_factor >= 0 else 2 - S
     vg = _coulomb(p, G + q, normal, lz)
     vg[g0] = 0.0
-    d = tau[:, None, :] - tau[None, :, :]                                  # [a,b,3]
-    X = np.einsum("g,gab->ab", vg, np.exp(1j * np.einsum("gi,abi->gab", G + q, d)))
-    Pd = np.einsum("kcvaa->cvka", A1).reshape(N, nw)                       # P[r,(aa)]
-    B = sf / (nk * vol) * (Pd @ X @ Pd.T)
+    Pd = [np.einsum("kca,kva->cvka", np.conj(blk(cc, s)), blk(cv, s)).reshape(N, nw) for s in range(ns)]
+    for i in range(ns):
+        for j in range(ns):
+            d = tau[i][:, None, :] - tau[j][None, :, :]
+            X = np.einsum("g,gab->ab", vg, np.exp(1j * np.einsum("gi,abi->gab", G + q, d)))
+            B[i * 3 * N:i * 3 * N + N, j * 3 * N:j * 3 * N + N] += sf / (nk * vol) * (Pd[i] @ X @ Pd[j].T)
     # direct
     fw = -1.0 / (vol * nk)
     dk = K[None, :, :] - K[:, None, :]
@@ -164,7 +173,18 @@ def coupling_factorised(prob, bands):
         avg = _cell_avg(p, vol, area, lz, nk)
         avg = p.inv_eps * avg if p.w_kind == 0 else avg
         W[:, :, g0] = np.where(ndk > MINVAL, W[:, :, g0], avg)
-    phase = np.exp(-1j * np.einsum("xygi,abi->xygab", x, d))
-    Phi = np.einsum("xyg,xygab->xyab", W, phase)
-    Bd = fw * np.einsum("xcvba,xyab,yCVab->cvxCVy", A1, np.conj(Phi), A1)
-    return B + Bd.reshape(N, N)
+    exc = [(0, 0), (0, 1), (1, 0), (1, 1)]
+    for sp in range(3 * S + 1):
+        sv1, sc1 = exc[sp]
+        sp2 = sp if sp in (0, 3 * S) else 3 - sp
+        d = tau[sv1][:, None, :] - tau[sc1][None, :, :]
+        Phi = np.einsum("xyg,xygab->xyab", W, np.exp(-1j * np.einsum("xygi,abi->xygab", x, d)))
+        Q = blk(cv, sv1)[:, None, :, :, None] * np.conj(blk(cc, sc1))[:, :, None, None, :]   # [k,c1,v1,a,b]
+        R = np.conj(blk(cc, sv1))[:, :, None, :, None] * blk(cv, sc1)[:, None, :, None, :]   # [k,c2,v2,a,b]
+        Bd = fw * np.einsum("xcvab,xyab,yCVab->cvxCVy", Q, np.conj(Phi), R)
+        B[sp * N:(sp + 1) * N, sp2 * N:(sp2 + 1) * N] += Bd.reshape(N, N)
+    if S:
+        h = 1 / math.sqrt(2)
+        U = np.array([[1, 0, 0, 0], [0, h, h, 0], [0, h, -h, 0], [0, 0, 0, 1]])
+        B = np.einsum("il,lakb,kj->iajb", U, B.reshape(4, N, 4, N), U).reshape(NA, NA)
+    return B

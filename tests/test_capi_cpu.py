@@ -88,6 +88,12 @@ def test_full_bse_sizes(synth, gpu):
         N = prob.n_bse
         assert [x.value for x in out] == [N, factor * N, factor * N, factor * N]
         assert (m.n_exc, m.n_rho, m.n_h, m.n_opt) == (factor * N,) * 4
+    prob = synth.collinear_problem(grid=3)
+    N = prob.n_bse
+    m = Marshalled(prob, tamm_dancoff=0)
+    assert lib.bse_sizes(C.byref(m.model), C.byref(m.params), *[C.byref(x) for x in out]) == 0
+    assert [x.value for x in out] == [N, 8 * N, 4 * N, 8 * N]
+    assert (m.n_exc, m.n_rho, m.n_h, m.n_opt) == (8 * N, 4 * N, 8 * N, 4 * N)
 
 
 def test_rejects_zero_q(synth, gpu):

@@ -25,7 +25,8 @@ GAMMA = 0.05
 def _prob(synth, name):
     return {"hbn6": lambda: synth.hbn_problem(grid=6), "hbn8": lambda: synth.hbn_problem(grid=8),
             "cubic3": lambda: synth.cubic3d_problem(grid=3), "orb8_3": lambda: synth.orb8_problem(grid=3),
-            "mag4_4": lambda: synth.magnetic4_problem(grid=4)}[name]()
+            "mag4_4": lambda: synth.magnetic4_problem(grid=4), "coll3": lambda: synth.collinear_problem(grid=3),
+            "coll4": lambda: synth.collinear_problem(grid=4)}[name]()
 
 
 def _random_phases(bands, seed):
@@ -36,35 +37,37 @@ def _random_phases(bands, seed):
     return ec, ev, cc * pc, cv * pv
 
 
-@pytest.mark.parametrize("name", ["hbn6", "cubic3", "mag4_4"])
+@pytest.mark.parametrize("name", ["hbn6", "cubic3", "mag4_4", "coll3"])
 def test_block_structure(synth, oracle, name):
+    """Collinear models: the resonant part is the spin-rotated 4N x 4N Tamm-Dancoff matrix and
+    the coupling part is rotated the same way (spin_transformation 3096-3105)."""
     prob = _prob(synth, name)
     bands = oracle.bands(prob)
     H, rho = oracle.build(prob, bands, tamm_dancoff=0)
     Ht, rhot = oracle.build(prob, bands)
-    N = prob.n_bse
+    NA, NR = Ht.shape[0], rhot.shape[0]
     g0 = prob.ng // 2
-    assert H.shape == (2 * N, 2 * N) and rho.shape == (2 * N, prob.ng)
-    A, B = H[:N, :N], H[:N, N:]
-    assert np.array_equal(A, Ht) and np.array_equal(rho[:N], rhot)
-    assert np.array_equal(H[N:, N:], -A.conj())
-    assert np.array_equal(H[N:, :N], -B.conj().T)
+    assert H.shape == (2 * NA, 2 * NA) and rho.shape == (2 * NR, prob.ng)
+    A, B = H[:NA, :NA], H[:NA, NA:]
+    assert np.array_equal(A, Ht) and np.array_equal(rho[:NR], rhot)
+    assert np.array_equal(H[NA:, NA:], -A.conj())
+    assert np.array_equal(H[NA:, :NA], -B.conj().T)
     # B^T = B up to the q-shift of the exchange phases e^{i(G+q).tau} (q = 1e-5 x)
     assert np.abs(B - B.T).max() < 1e-8 * np.abs(B).max()
     # dipole column of rho_vc: i q.<v|r|c> = -conj(i q.<c|r|v>)  (Q25)
-    assert np.abs(rho[N:, g0] + rho[:N, g0].conj()).max() < 1e-14
+    assert np.abs(rho[NR:, g0] + rho[:NR, g0].conj()).max() < 1e-14
 
 
-@pytest.mark.parametrize("name", ["hbn6", "cubic3", "orb8_3", "mag4_4"])
+@pytest.mark.parametrize("name", ["hbn6", "cubic3", "orb8_3", "mag4_4", "coll3", "coll4"])
 def test_coupling_factorised_agrees(synth, oracle, name):
     """The oracle's loops over stored all-pairs densities and the factorised form (what the
     CUDA coupling kernel evaluates) give the same B."""
     prob = _prob(synth, name)
     bands = oracle.bands(prob)
     H, _ = oracle.build(prob, bands, tamm_dancoff=0)
-    N = prob.n_bse
+    NA = H.shape[0] // 2
     B = coupling_factorised(prob, bands)
-    assert np.abs(B - H[:N, N:]).max() < 1e-12 * np.abs(B).max()
+    assert np.abs(B - H[:NA, NA:]).max() < 1e-12 * np.abs(B).max()
 
 
 @pytest.mark.parametrize("name", ["hbn6", "cubic3", "mag4_4"])
@@ -128,9 +131,30 @@ def test_ipa_ignores_coupling(synth, oracle):
     assert np.array_equal(a["E"], b["E"]) and np.array_equal(a["eps2"], b["eps2"])
 
 
-def test_collinear_coupling_rejected(synth, oracle):
-    with pytest.raises(oracle.OracleError):
-        oracle.build(synth.collinear_problem(grid=3), tamm_dancoff=0)
+def test_collinear_blocks(synth, oracle):
+    """Collinear full BSE: both 4N x 4N spin blocks (H0 = {1,2}, H1 = {0,3} of every quadrant,
+    3151-3172) keep the full-BSE structure; at 4x4 both are positive definite, the eigenvalues
+    are the union of the blocks' and the spectrum comes from H1 with rho = (rho_cv; rho_vc)."""
+    prob = _prob(synth, "coll4")
+    H, rho = oracle.build(prob, tamm_dancoff=0)
+    N = prob.n_bse
+    H0, H1 = oracle.split_blocks_coupled(H, N)
+    for Hb in (H0, H1):
+        n2 = Hb.shape[0] // 2
+        M = np.r_[np.ones(n2), -np.ones(n2)][:, None] * Hb
+        assert np.abs(M - M.conj().T).max() < 1e-12 * np.abs(M).max()
+        assert np.linalg.eigvalsh(M).min() > 0
+    r = oracle.solve(prob, OMEGA, GAMMA, tamm_dancoff=0)
+    assert r["E"].shape == (8 * N,) and r["f"].shape == (4 * N,)
+    E0 = np.sort(np.linalg.eigvals(H0).real)
+    assert np.abs(r["E"][:4 * N] - E0).max() < 1e-10
+    res = oracle.solve_coupled(H1, rho[:, prob.ng // 2], oracle.prefactor(prob), OMEGA, GAMMA)
+    assert np.array_equal(r["eps2"], res["eps2"])
+    # spin-rotation invariance of the spectrum of the spin-conserving block: the coupled H1
+    # equals the un-rotated blocks {0,3}
+    Ht, _ = oracle.build(prob)
+    b1 = np.r_[0:N, 3 * N:4 * N]
+    assert np.array_equal(H1[:2 * N, :2 * N], Ht[np.ix_(b1, b1)])
 
 
 def test_golden_vectors(synth, oracle):
