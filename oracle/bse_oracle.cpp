@@ -40,6 +40,18 @@
  *       e^{i(G + k2 - k1).tau}) and of W (no -q shift of Delta k, 2549-2552); like Q23, the
  *       accumulated row is used as it is, without the conjugation of the .t() assignment
  *       (3031-3033), which makes B transform as the exciton basis requires (B' = D^H B D*).
+ *   RPA screening (adding_screening = 1, insulator branch of pull_coulomb_potentials 2597-2690,
+ *   Dielectric_Function::pull_values 2214-2315; oracle_rpa_w, passed to oracle_build as a W table):
+ *   Q28 Delta k = 0: the Monte-Carlo sphere average (seeded points, Q19) of W(q) itself, except
+ *       the head G = G' = G0, which is the average of eps^-1_00 times the cell average of v (the
+ *       reference multiplies the average of every eps^-1 entry by that cell average, the analogue
+ *       of Q8, which makes W at Delta k = 0 non-Hermitian); the points come in +-q pairs;
+ *   Q29 W_GG'(q) = eps^-1_GG'(q) v(q + G') (2677: eps^-1_GG' sqrt(v(q+G)) sqrt(v(q+G')), which
+ *       with eps^-1 = 1 + v chi is not Hermitian); the densities of chi0 use the point-like M at
+ *       momentum q (Q13) and the band states at k and k - q of the model;
+ *   Q30 the anti-resonant term of chi0 uses the densities at -q (2232 reuses the +q densities,
+ *       equal for a time-reversal symmetric model), so the static chi0 and W keep
+ *       W_{-G,-G'}(-q) = W_GG'(q)^* and the BSE matrix stays Hermitian for magnetic models too.
  */
 #include "../include/bse_gpu.h"
 
@@ -48,6 +60,7 @@
 #include <complex>
 #include <cstdint>
 #include <cstring>
+#include <random>
 #include <vector>
 
 #ifdef _OPENMP
@@ -284,6 +297,114 @@ struct Dims {
     int64_t N, n_h, n_rho;
 };
 
+// Small dense complex solve A X = B (n x n, nrhs columns, column-major, partial pivoting).
+int csolve(int n, int nrhs, std::vector<cd>& A, std::vector<cd>& B) {
+    for (int k = 0; k < n; k++) {
+        int piv = k;
+        for (int i = k + 1; i < n; i++)
+            if (std::abs(A[i + (size_t)n * k]) > std::abs(A[piv + (size_t)n * k])) piv = i;
+        if (std::abs(A[piv + (size_t)n * k]) == 0.0) return BSE_ERR_BAD_INPUT;
+        if (piv != k) {
+            for (int j = 0; j < n; j++) std::swap(A[k + (size_t)n * j], A[piv + (size_t)n * j]);
+            for (int j = 0; j < nrhs; j++) std::swap(B[k + (size_t)n * j], B[piv + (size_t)n * j]);
+        }
+        const cd d = A[k + (size_t)n * k];
+        for (int i = k + 1; i < n; i++) {
+            const cd l = A[i + (size_t)n * k] / d;
+            if (l == 0.0) continue;
+            for (int j = k; j < n; j++) A[i + (size_t)n * j] -= l * A[k + (size_t)n * j];
+            for (int j = 0; j < nrhs; j++) B[i + (size_t)n * j] -= l * B[k + (size_t)n * j];
+        }
+    }
+    for (int j = 0; j < nrhs; j++)
+        for (int i = n - 1; i >= 0; i--) {
+            cd x = B[i + (size_t)n * j];
+            for (int l = i + 1; l < n; l++) x -= A[i + (size_t)n * l] * B[l + (size_t)n * j];
+            B[i + (size_t)n * j] = x / A[i + (size_t)n * i];
+        }
+    return BSE_OK;
+}
+
+/* chi0 and eps^-1 at momentum q, omega = 0 (Dielectric_Function::pull_values 2214-2315):
+ *   rho_r(G) = sum_a conj(c_ca(k)) e^{i(G+q).tau_a} c_va(k - q)   (point-like M, Q13; both spins)
+ *   chi0_GG' = 1/(V nk) sum_r [conj(rho_r(G)) rho_r(G') / (-E_r + i eta)
+ *                              - rho'_r(G) conj(rho'_r(G')) / (E'_r - i eta)]   (2232, 2255; Q30)
+ *   with rho'_r(G) = sum_a conj(c_ca(k)) e^{-i(G+q).tau_a} c_va(k + q), E' = E_c(k) - E_v(k + q): the
+ *   anti-resonant term at -q (the reference reuses rho_r there, the same thing for a time-reversal
+ *   symmetric model)
+ *   order 0: eps^-1 = 1 + diag(v) chi0 (2261-2268); otherwise the Dyson form
+ *   eps^-1 = 1 + diag(v) (1 - chi0 diag(v))^-1 chi0 (2270-2306), v_G = v(q + G).
+ * chi0 / einv: ng x ng column-major. */
+int rpa_eps_inv(const bse_model* m, const bse_params* p, const Geometry& geo, const double* q, double eta,
+                int order, cd* chi0, cd* einv) {
+    const int nk = m->n_k, ng = m->n_g, nw = m->nw, ns = m->n_spin, nb = nw * ns, nc = p->nc, nv = p->nv;
+    const int64_t R = (int64_t)ns * nk * nc * nv;
+    std::vector<cd> rho((size_t)R * ng), mult(R), rho2((size_t)R * ng), mult2(R);
+    int err = 0;
+#pragma omp parallel for schedule(dynamic) reduction(min : err)
+    for (int k = 0; k < nk; k++) {
+        std::vector<double> ec(2 * nc), ev(2 * nv), ev2(2 * nv);
+        std::vector<cd> Cc((size_t)nc * nb), Cv((size_t)nv * nb), Cv2((size_t)nv * nb);
+        const double* kk = m->k_cart + 3 * k;
+        const double kq[3] = {kk[0] - q[0], kk[1] - q[1], kk[2] - q[2]};
+        const double kp[3] = {kk[0] + q[0], kk[1] + q[1], kk[2] + q[2]};
+        int st = ks_subset(m, p, kk, 0, nc, ec.data(), Cc.data());
+        if (!st) st = ks_subset(m, p, kq, nv, 0, ev.data(), Cv.data());
+        if (!st) st = ks_subset(m, p, kp, nv, 0, ev2.data(), Cv2.data());
+        if (st) { err = std::min(err, st); continue; }
+        for (int s = 0; s < ns; s++)
+            for (int c = 0; c < nc; c++)
+                for (int v = 0; v < nv; v++) {
+                    const int64_t r = (((int64_t)s * nc + c) * nv + v) * nk + k;
+                    const double E = ec[s * nc + c] - ev[s * nv + v], E2 = ec[s * nc + c] - ev2[s * nv + v];
+                    mult[r] = 1.0 / cd(-E, eta);
+                    mult2[r] = -1.0 / cd(E2, -eta);
+                    for (int g = 0; g < ng; g++) {
+                        const double* G = m->g_cart + 3 * (size_t)g;
+                        cd acc = 0, acc2 = 0;
+                        for (int a = 0; a < nw; a++) {
+                            const double* t = m->centres + 3 * ((size_t)s * nw + a);
+                            const double ph = t[0] * (G[0] + q[0]) + t[1] * (G[1] + q[1]) + t[2] * (G[2] + q[2]);
+                            const cd cca = std::conj(Cc[(size_t)c * nb + s * nw + a]);
+                            acc += cca * cd(std::cos(ph), std::sin(ph)) * Cv[(size_t)v * nb + s * nw + a];
+                            acc2 += cca * cd(std::cos(ph), -std::sin(ph)) * Cv2[(size_t)v * nb + s * nw + a];
+                        }
+                        rho[(size_t)r * ng + g] = acc;
+                        rho2[(size_t)r * ng + g] = acc2;
+                    }
+                }
+    }
+    if (err) return err;
+    const double fchi = 1.0 / (geo.vol * nk);                                  // 2252
+    for (int j = 0; j < ng; j++)
+        for (int i = 0; i < ng; i++) {
+            cd acc = 0;
+            for (int64_t r = 0; r < R; r++)
+                acc += std::conj(rho[(size_t)r * ng + i]) * rho[(size_t)r * ng + j] * mult[r] +
+                       rho2[(size_t)r * ng + i] * std::conj(rho2[(size_t)r * ng + j]) * mult2[r];
+            chi0[i + (size_t)ng * j] = fchi * acc;
+        }
+    std::vector<double> vq(ng);
+    for (int g = 0; g < ng; g++) {
+        const double* G = m->g_cart + 3 * (size_t)g;
+        const double x[3] = {q[0] + G[0], q[1] + G[1], q[2] + G[2]};
+        vq[g] = coulomb(p, geo, x);                                            // 2244-2247
+    }
+    if (order == 0) {
+        for (int j = 0; j < ng; j++)
+            for (int i = 0; i < ng; i++) einv[i + (size_t)ng * j] = vq[i] * chi0[i + (size_t)ng * j] + (i == j ? 1.0 : 0.0);
+        return BSE_OK;
+    }
+    std::vector<cd> A((size_t)ng * ng), X(chi0, chi0 + (size_t)ng * ng);
+    for (int j = 0; j < ng; j++)
+        for (int i = 0; i < ng; i++) A[i + (size_t)ng * j] = (i == j ? 1.0 : 0.0) - chi0[i + (size_t)ng * j] * vq[j];
+    int st = csolve(ng, ng, A, X);
+    if (st) return st;
+    for (int j = 0; j < ng; j++)
+        for (int i = 0; i < ng; i++) einv[i + (size_t)ng * j] = vq[i] * X[i + (size_t)ng * j] + (i == j ? 1.0 : 0.0);
+    return BSE_OK;
+}
+
 Dims dims(const bse_model* m, const bse_params* p) {
     Dims d;
     d.nw = m->nw; d.ns = m->n_spin; d.nb = d.nw * d.ns; d.nk = m->n_k; d.ng = m->n_g;
@@ -330,7 +451,8 @@ double oracle_prefactor(const bse_model* m, const bse_params* p) {
  * point-like M of 1480-1498) and the kernel build (pull_resonant_part_and_rcv 2767-2928,
  * spin_transformation 3048-3117).  h_out: n_h x n_h, rho_out: n_rho x ng (complex128). */
 int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, const double* e_v,
-                 const double* c_c_in, const double* c_v_in, double* h_out, double* rho_out) {
+                 const double* c_c_in, const double* c_v_in, double* h_out, double* rho_out,
+                 const double* w_table /* nullable: W(g, s) per k pair from oracle_rpa_w */) {
     Dims d = dims(m, p);
     Geometry geo = make_geometry(m);
     const cd* Cc = (const cd*)c_c_in;
@@ -434,16 +556,17 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
             {
                 std::vector<cd> rcc((size_t)nc * nc * nk * ng), rvv((size_t)nv * nv * nk * ng);
                 std::vector<cd> T((size_t)nk * ng);
-                std::vector<double> W((size_t)nk * ng * ng);
+                std::vector<cd> W((size_t)nk * ng * ng);
 #pragma omp for schedule(dynamic)
                 for (int k1 = 0; k1 < nk; k1++) {
-                    // W(g, s', k2 - k1): model W is diagonal in G (2697-2728)
+                    // W(g, s', k2 - k1): model W is diagonal in G (2697-2728); an RPA table is not
                     for (int k2 = 0; k2 < nk; k2++) {
                         double dk[3] = {Kv(k2)[0] - Kv(k1)[0], Kv(k2)[1] - Kv(k1)[1], Kv(k2)[2] - Kv(k1)[2]};
+                        const cd* wt = w_table ? (const cd*)w_table + ((size_t)k2 * nk + k1) * ng * ng : nullptr;
                         for (int g = 0; g < ng; g++)
                             for (int s2 = 0; s2 < ng; s2++)
                                 W[((size_t)k2 * ng + g) * ng + s2] =
-                                    g == s2 ? w_diag(p, geo, nk, dk, Gv(g), g == g0) : 0.0;
+                                    wt ? wt[g + (size_t)ng * s2] : cd(g == s2 ? w_diag(p, geo, nk, dk, Gv(g), g == g0) : 0.0);
                     }
                     // rho_cc[c2][c1][k2][g] = sum_a conj(c_c2a(k2)) e^{i(G+k2-k1).tau} c_c1a(k1)  (2105-2117)
                     for (int a2 = 0; a2 < nc; a2++)
@@ -525,7 +648,7 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
             {
                 std::vector<cd> rcv((size_t)nc * nv * nk * ng), rvc((size_t)nv * nc * nk * ng);
                 std::vector<cd> T((size_t)nk * ng);
-                std::vector<double> W((size_t)nk * ng);
+                std::vector<cd> W((size_t)nk * ng * ng);
 #pragma omp for collapse(2) schedule(dynamic)
                 for (int sp = 0; sp < 3 * S + 1; sp++)
                 for (int k1 = 0; k1 < nk; k1++) {
@@ -533,7 +656,11 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                     const int sp2 = (sp == 0 || sp == 3 * S) ? sp : 3 - sp;
                     for (int k2 = 0; k2 < nk; k2++) {
                         double dk[3] = {Kv(k2)[0] - Kv(k1)[0], Kv(k2)[1] - Kv(k1)[1], Kv(k2)[2] - Kv(k1)[2]};
-                        for (int g = 0; g < ng; g++) W[(size_t)k2 * ng + g] = w_diag(p, geo, nk, dk, Gv(g), g == g0);
+                        const cd* wt = w_table ? (const cd*)w_table + ((size_t)k2 * nk + k1) * ng * ng : nullptr;
+                        for (int g = 0; g < ng; g++)
+                            for (int s2 = 0; s2 < ng; s2++)
+                                W[((size_t)k2 * ng + g) * ng + s2] =
+                                    wt ? wt[g + (size_t)ng * s2] : cd(g == s2 ? w_diag(p, geo, nk, dk, Gv(g), g == g0) : 0.0);
                     }
                     for (int c2 = 0; c2 < nc; c2++)
                         for (int v1 = 0; v1 < nv; v1++)
@@ -561,8 +688,12 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                             const int64_t r1 = (int64_t)c1 * nv * nk + (int64_t)v1 * nk + k1;
                             for (int c2 = 0; c2 < nc; c2++) {
                                 for (int k2 = 0; k2 < nk; k2++)
-                                    for (int g = 0; g < ng; g++)   // W diagonal in G: T(k2, s) = rho_kk_cv W(s, s)
-                                        T[(size_t)k2 * ng + g] = rcv[(((size_t)c2 * nv + v1) * nk + k2) * ng + g] * W[(size_t)k2 * ng + g];
+                                    for (int s2 = 0; s2 < ng; s2++) {   // T(k2, s) = sum_g rho_kk_cv(g) W(g, s)
+                                        cd acc = 0;
+                                        for (int g = 0; g < ng; g++)
+                                            acc += rcv[(((size_t)c2 * nv + v1) * nk + k2) * ng + g] * W[((size_t)k2 * ng + g) * ng + s2];
+                                        T[(size_t)k2 * ng + s2] = acc;
+                                    }
                                 for (int v2 = 0; v2 < nv; v2++)
                                     for (int k2 = 0; k2 < nk; k2++) {
                                         cd acc = 0;
@@ -622,6 +753,83 @@ int oracle_build(const bse_model* m, const bse_params* p, const double* e_c, con
                 H[(NA + i) + NH * j] = -std::conj(H[j + NH * (NA + i)]);
             }
     }
+    return BSE_OK;
+}
+
+/* chi0 and eps^-1 at one momentum q (cartesian), ng x ng column-major complex each. */
+int oracle_rpa_eps_inv(const bse_model* m, const bse_params* p, const double* q, double eta, int order,
+                       double* chi0, double* einv) {
+    Geometry geo = make_geometry(m);
+    return rpa_eps_inv(m, p, geo, q, eta, order, (cd*)chi0, (cd*)einv);
+}
+
+/* RPA W table for every k pair (pull_coulomb_potentials 2597-2690, adding_screening = 1):
+ * w_out[(i*nk + j)*ng*ng + g + ng*s] = W_{G_g G_s}(k_i - k_j).  |k_i - k_j| > minval: eps^-1(dk)
+ * times v(dk + G_s) (Q29); otherwise the average of W(q) over n_points seeded points q of the
+ * sphere of radius 2 pi (3 / (4 pi nk V))^(1/3) (2597-2650, Q7, Q19), with the head
+ * <eps^-1_00> times the cell average of v (Q28). */
+int oracle_rpa_w(const bse_model* m, const bse_params* p, double eta, int order, int n_points, uint64_t seed,
+                 double* w_out) {
+    Geometry geo = make_geometry(m);
+    const int nk = m->n_k, ng = m->n_g, g0 = ng / 2;
+    cd* W = (cd*)w_out;
+    const size_t gg = (size_t)ng * ng;
+    std::vector<cd> chi0(gg), einv(gg), avg(gg, cd(0));   // avg: <W(q)> over the sphere points
+    // Delta k = 0: sphere average of eps^-1 (2614-2650), points drawn as the reference draws them
+    const double radius = 2.0 * kPi * std::pow(3.0 / (4.0 * kPi * nk * geo.vol), 1.0 / 3.0);
+    std::mt19937_64 gen(seed);
+    std::uniform_real_distribution<double> dis(0.0, 1.0);
+    double xprev[3] = {0, 0, 0};
+    for (int n = 0; n < n_points;) {
+        double x[3];
+        if (n % 2 == 0) {
+            double y[3];
+            for (int i = 0; i < 3; i++) y[i] = dis(gen) > 0.5 ? -dis(gen) * radius : dis(gen) * radius;
+            const double ny = std::sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+            if (!(ny <= radius && ny > kMinval * kMinval)) continue;
+            for (int i = 0; i < 3; i++) x[i] = y[i];
+            for (int i = 0; i < 3; i++) xprev[i] = y[i];
+        } else {
+            for (int i = 0; i < 3; i++) x[i] = -xprev[i];   // antithetic partner: the average keeps W(-q) = W(q)^*
+        }
+        int st = rpa_eps_inv(m, p, geo, x, eta, order, chi0.data(), einv.data());
+        if (st) return st;
+        for (int s2 = 0; s2 < ng; s2++) {
+            const double* G = m->g_cart + 3 * (size_t)s2;
+            const double y[3] = {x[0] + G[0], x[1] + G[1], x[2] + G[2]};
+            const double v = s2 == g0 ? 1.0 : coulomb(p, geo, y);   // the head keeps <eps^-1_00>
+            for (int g = 0; g < ng; g++) {
+                const size_t t = g + (size_t)ng * s2;
+                avg[t] += (s2 == g0 && g != g0) ? einv[t] * coulomb(p, geo, y) : einv[t] * v;
+            }
+        }
+        n++;
+    }
+    for (size_t t = 0; t < gg; t++) avg[t] /= (double)std::max(n_points, 1);
+    bse_params pb = *p;
+    pb.w_kind = BSE_W_BARE;                  // the bare-Coulomb cell average, whatever model W p names
+    const double vbar = cell_average(&pb, geo, nk);
+    for (int i = 0; i < nk; i++)
+        for (int j = 0; j < nk; j++) {
+            const double* ki = m->k_cart + 3 * (size_t)i;
+            const double* kj = m->k_cart + 3 * (size_t)j;
+            const double dk[3] = {ki[0] - kj[0], ki[1] - kj[1], ki[2] - kj[2]};
+            cd* w = W + ((size_t)i * nk + j) * gg;
+            const bool zero = !(std::sqrt(dk[0] * dk[0] + dk[1] * dk[1] + dk[2] * dk[2]) > kMinval);   // 2606
+            if (zero) {
+                for (size_t t = 0; t < gg; t++) w[t] = avg[t];
+                w[g0 + (size_t)ng * g0] = avg[g0 + (size_t)ng * g0] * vbar;
+                continue;
+            }
+            int st = rpa_eps_inv(m, p, geo, dk, eta, order, chi0.data(), einv.data());
+            if (st) return st;
+            for (int s2 = 0; s2 < ng; s2++) {
+                const double* G = m->g_cart + 3 * (size_t)s2;
+                const double x[3] = {dk[0] + G[0], dk[1] + G[1], dk[2] + G[2]};
+                const double v = coulomb(p, geo, x);
+                for (int g = 0; g < ng; g++) w[g + (size_t)ng * s2] = einv[g + (size_t)ng * s2] * v;
+            }
+        }
     return BSE_OK;
 }
 

@@ -50,7 +50,11 @@ def lib():
         dp = C.POINTER(C.c_double)
         capi = _pkg().capi
         L.oracle_bands.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams), dp, dp, dp, dp]
-        L.oracle_build.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams), dp, dp, dp, dp, dp, dp]
+        L.oracle_build.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams), dp, dp, dp, dp, dp, dp, dp]
+        L.oracle_rpa_eps_inv.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams), dp, C.c_double, C.c_int,
+                                         dp, dp]
+        L.oracle_rpa_w.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams), C.c_double, C.c_int, C.c_int,
+                                   C.c_uint64, dp]
         L.oracle_prefactor.argtypes = [C.POINTER(capi.BseModel), C.POINTER(capi.BseParams)]
         L.oracle_prefactor.restype = C.c_double
         L.oracle_oscillators.argtypes = [C.c_int64, C.c_int64, dp, dp, dp]
@@ -78,8 +82,31 @@ def bands(prob, **overrides):
     return ec, ev, cc, cv
 
 
-def build(prob, band_states=None, **overrides):
-    """Full BSE matrix (n_h x n_h, spin-rotated for collinear models) and rho_cv (n_rho x ng)."""
+def rpa_eps_inv(prob, q, eta=0.0, order=1, **overrides):
+    """chi0 and eps^-1 (ng x ng) at momentum q (Dielectric_Function::pull_values 2214-2315)."""
+    M = _pkg().capi.Marshalled(prob, **overrides)
+    chi0 = np.zeros((prob.ng, prob.ng), np.complex128)      # C order (col, row) == column-major (row, col)
+    einv = np.zeros((prob.ng, prob.ng), np.complex128)
+    qq = np.ascontiguousarray(q, dtype=np.float64)
+    p = _pkg().capi.ptr
+    _check(lib().oracle_rpa_eps_inv(C.byref(M.model), C.byref(M.params), p(qq), eta, order, p(chi0), p(einv)))
+    return chi0.T, einv.T
+
+
+def rpa_w(prob, eta=0.0, order=1, n_points=64, seed=1, **overrides):
+    """RPA screened interaction for every k pair: array [nk, nk, ng, ng] (numpy (row, col) per pair),
+    W[i, j] = W(k_i - k_j) (pull_coulomb_potentials 2597-2690, decisions Q28/Q29)."""
+    M = _pkg().capi.Marshalled(prob, **overrides)
+    nk, ng = prob.nk, prob.ng
+    w = np.zeros((nk, nk, ng, ng), np.complex128)            # per pair: C order (s, g) == column-major (g, s)
+    p = _pkg().capi.ptr
+    _check(lib().oracle_rpa_w(C.byref(M.model), C.byref(M.params), eta, order, n_points, seed, p(w)))
+    return np.swapaxes(w, -1, -2)
+
+
+def build(prob, band_states=None, w_table=None, **overrides):
+    """Full BSE matrix (n_h x n_h, spin-rotated for collinear models) and rho_cv (n_rho x ng).
+    w_table: an RPA W from rpa_w() replacing the model W of the direct terms."""
     M = _pkg().capi.Marshalled(prob, **overrides)
     if band_states is None:
         band_states = bands(prob, **overrides)
@@ -88,8 +115,9 @@ def build(prob, band_states=None, **overrides):
     rho = np.zeros((M.ng, M.n_rho), np.complex128)      # C order (ng, n_rho) == column-major n_rho x ng
     p = _pkg().capi.ptr
     Hc = np.zeros((M.n_h, M.n_h), np.complex128)         # C buffer, filled column-major
+    wt = None if w_table is None else np.ascontiguousarray(np.swapaxes(w_table, -1, -2), dtype=np.complex128)
     _check(lib().oracle_build(C.byref(M.model), C.byref(M.params), p(ec), p(ev), p(cc), p(cv),
-                              p(Hc), p(rho)))
+                              p(Hc), p(rho), p(wt)))
     H = Hc.T                                             # column-major -> numpy (row, col)
     return H, rho.T
 
@@ -178,13 +206,13 @@ def solve_coupled(H, rho_g0, F, omega, gamma):
             "eps2": eps.imag, "eps1": eps.real}
 
 
-def solve(prob, omega, gamma, band_states=None, want_vectors=True, timings=None, **overrides):
+def solve(prob, omega, gamma, band_states=None, want_vectors=True, timings=None, w_table=None, **overrides):
     """Whole reference path on the CPU: bands -> build -> zheevd -> oscillators -> eps."""
     t0 = time.perf_counter()
     if band_states is None:
         band_states = bands(prob, **overrides)
     t1 = time.perf_counter()
-    H, rho = build(prob, band_states, **overrides)
+    H, rho = build(prob, band_states, w_table=w_table, **overrides)
     t2 = time.perf_counter()
     N = prob.n_bse
     ng0 = prob.ng // 2
