@@ -1,5 +1,6 @@
 /*
- * bse_oracle.cpp -- CPU FP64 restatement of the reference's q->0 Tamm-Dancoff BSE path.
+ * bse_oracle.cpp -- CPU FP64 restatement of the reference's q->0 BSE path (Tamm-Dancoff and the
+ * full BSE with the coupling block; model or RPA screened interaction).
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the checker: only tests/, the smoke() of
  * __graft_entry__ and the cpu_baseline / reference arm of bench.py load it.  The product

@@ -7,7 +7,8 @@ scipy.linalg.eigh(driver="evd") for the dense solve -- the routine Armadillo's
 eig_sym dispatches to in Excitonic_Hamiltonian::common_diagonalization
 (bse.version13.cpp:3330); for the full BSE (tamm_dancoff = 0) numpy's zgeev, as the
 reference's eig_gen (3326), with the spectrum through the inverse overlap matrix of the
-eigenvectors (solve_coupled).  Parity against the reference binary is UNPINNED (the
+eigenvectors (solve_coupled); rpa_w builds the RPA screened interaction table that build() can
+use in place of the model W.  Parity against the reference binary is UNPINNED (the
 reference cannot be built here); see the header of bse_oracle.cpp.
 """
 from __future__ import annotations
