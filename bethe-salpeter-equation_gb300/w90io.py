@@ -201,3 +201,39 @@ def read_spectrum(path):
             om.append(w.real)
             eps.append(e)
     return np.asarray(om), np.asarray(eps)
+
+
+def read_band_path(path, n_segments: int, crystal: bool = False, reciprocal=None):
+    """Segments of a band-structure path, the file of Hamiltonian_TB::pull_bands
+    (bse.version13.cpp:823-875): per segment "kx ky kz  kx ky kz  n" (start, end, points).
+    crystal: coordinates in units of the reciprocal vectors (columns of `reciprocal`), converted
+    to cartesian as 841-851 do.  Returns [(k_start, k_end, n), ...] in cartesian coordinates."""
+    vals = np.loadtxt(path).reshape(-1, 7)[:n_segments]
+    segs = []
+    for row in vals:
+        a, b, n = row[:3].copy(), row[3:6].copy(), int(row[6])
+        if crystal:
+            a, b = np.asarray(reciprocal) @ a, np.asarray(reciprocal) @ b
+        segs.append((a, b, n))
+    return segs
+
+
+def band_path_points(segments) -> np.ndarray:
+    """k points of the path: n points per segment from start to end inclusive (853-857)."""
+    pts = []
+    for a, b, n in segments:
+        for j in range(n):
+            t = j / (n - 1) if n > 1 else 0.0
+            pts.append(a * (1.0 - t) + b * t)
+    return np.asarray(pts).reshape(-1, 3)
+
+
+def write_bands(path, e_v, e_c, n_spin: int):
+    """The bands file of pull_bands (858-864): per k, for each spin row the selected valence
+    bands (top-down from E_F) then the conduction bands (bottom-up, with the scissor)."""
+    with open(path, "w") as fh:
+        for k in range(e_v.shape[1]):
+            row = []
+            for s in range(n_spin):
+                row += [f"{x:.10g}" for x in e_v[s, k]] + [f"{x:.10g}" for x in e_c[s, k]]
+            fh.write(" ".join(row) + " \n")
