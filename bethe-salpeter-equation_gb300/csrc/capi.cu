@@ -161,8 +161,6 @@ int validate(const bse_model* m, const bse_params* p) {
     if (p->tamm_dancoff != 0 && p->tamm_dancoff != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "tamm_dancoff must be 0 or 1");
     if (p->precision != BSE_FP64 && p->precision != BSE_MIXED) return fail(nullptr, BSE_ERR_BAD_INPUT, "precision");
     if (p->tamm_dancoff == 0 && !p->ipa) {
-        if (m->n_spin != 1)
-            return fail(nullptr, BSE_ERR_BAD_INPUT, "the full BSE (tamm_dancoff = 0) is implemented for n_spin = 1 only");
         if (p->precision != BSE_FP64)
             return fail(nullptr, BSE_ERR_BAD_INPUT, "the full BSE (tamm_dancoff = 0) runs in FP64: set precision = BSE_FP64");
     }
@@ -289,7 +287,12 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     c->n_exc = (3 * c->S + 1) * c->N;
     c->n_opt = (c->S + 1) * c->N;
     c->coupled = p->tamm_dancoff == 0 && !p->ipa;
-    if (c->coupled) c->n_h = c->n_rho = c->n_exc = c->n_opt = 2 * c->N;
+    if (c->coupled) {   // resonant + anti-resonant rows: every size doubles (collinear: two 4N blocks)
+        c->n_h *= 2;
+        c->n_rho *= 2;
+        c->n_exc *= 2;
+        c->n_opt *= 2;
+    }
     // geometry (Crystal_Lattice, bse.version13.cpp:85-124)
     {
         const double* a = m->lattice;
@@ -359,10 +362,13 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     }
     c->h_elem = mixed ? 8 : 16;
     CK(dmalloc(c, &c->d_H, (size_t)c->n_h * c->n_h * c->h_elem, "H"));
-    if (c->S) CK(dmalloc(c, &c->d_blk, 2 * (size_t)(2 * c->N) * (2 * c->N) * c->h_elem, "spin blocks"));
     if (c->coupled) {
-        CK(dmalloc(c, &c->d_blk, (size_t)c->n_h * c->n_h * sizeof(double2), "L^H J L"));
-        CK(dmalloc(c, &c->d_aux, (size_t)c->n_h * sizeof(double2), "L^-1 rho"));
+        // spinless: L^H J L (2N); collinear: the two 4N blocks M0, M1 and L^H J L (4N)
+        const size_t nb = c->S ? (size_t)c->n_opt : (size_t)c->n_h;
+        CK(dmalloc(c, &c->d_blk, (c->S ? 3 : 1) * nb * nb * sizeof(double2), "full-BSE blocks"));
+        CK(dmalloc(c, &c->d_aux, nb * sizeof(double2), "L^-1 rho"));
+    } else if (c->S) {
+        CK(dmalloc(c, &c->d_blk, 2 * (size_t)(2 * c->N) * (2 * c->N) * c->h_elem, "spin blocks"));
     }
     if (mixed && !p->ipa && p->n_refine > 0) {
         const size_t n64 = c->S ? 4 * c->N : c->N;

@@ -691,11 +691,12 @@ __global__ void jnorm_scale_kernel(int64_t n, int64_t ncols, const double* __res
 // so W y = E y gives H x = E x for x = |E|^{1/2} L^{-H} y, normalised x^H J x = sign(E), and the
 // oscillator f = rho^H x = |E|^{1/2} (L^{-1} rho)^H y needs no eigenvector when the own solver
 // forms (L^{-1} rho)^H y itself.  Eigenvalues ascending: -E_max .. -E_min, E_min .. E_max.
-int run_eig_coupled(bse_ctx* c, bool want_vectors) {
+// One n x n block (n = 2N spinless; 4N for each collinear spin block): M consumed, W the workspace
+// (left holding the eigenvectors), rho0 / f null for a values-only block.
+int solve_coupled_block(bse_ctx* c, int64_t n, double2* M, double2* W, const double2* rho0, double* E, double2* f,
+                        bool want_vectors) {
     int st;
-    const int64_t n = c->n_h, N = c->N;
-    double2* M = (double2*)c->d_H;
-    double2* W = (double2*)c->d_blk;
+    const int64_t N = n / 2;
     cublasSetStream(c->cublas, c->stream);
     cusolverDnSetStream(c->cusolver, c->stream);
     {
@@ -731,12 +732,14 @@ int run_eig_coupled(bse_ctx* c, bool want_vectors) {
     hermitian_part_kernel<<<gb, 256, 0, c->stream>>>(n, W);
     c->launches++;
     // L^{-1} rho(G0)
-    const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
-    if ((st = cuda_check(c, cudaMemcpyAsync(c->d_aux, rho0, n * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream), "rho copy"))) return st;
-    if ((st = cublas_check(c, cublasZtrsv(c->cublas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n,
-                                          (const cuDoubleComplex*)M, n, (cuDoubleComplex*)c->d_aux, 1), "L^-1 rho"))) return st;
+    if (rho0) {
+        if ((st = cuda_check(c, cudaMemcpyAsync(c->d_aux, rho0, n * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream), "rho copy"))) return st;
+        if ((st = cublas_check(c, cublasZtrsv(c->cublas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n,
+                                              (const cuDoubleComplex*)M, n, (cuDoubleComplex*)c->d_aux, 1), "L^-1 rho"))) return st;
+    }
     if ((st = cuda_check(c, cudaGetLastError(), "coupled setup"))) return st;
-    if ((st = solve_one(c, n, W, n, true, c->d_E, want_vectors ? n : 0, c->d_aux, c->d_f))) return st;
+    if ((st = solve_one(c, n, W, n, true, E, want_vectors ? n : 0, rho0 ? c->d_aux : nullptr, rho0 ? f : nullptr))) return st;
+    if (!rho0) return BSE_OK;
     // eigenvectors of H: X = L^{-H} Y, then the J-normalisation of X and of the oscillators
     const int64_t nvec = c->n_vec_valid;
     if (nvec > 0 &&
@@ -744,10 +747,30 @@ int run_eig_coupled(bse_ctx* c, bool want_vectors) {
                                           n, nvec, &one, (const cuDoubleComplex*)M, n, (cuDoubleComplex*)W, n), "L^-H Y")))
         return st;
     jnorm_scale_kernel<<<(unsigned)((n * std::max<int64_t>(nvec, 1) + 255) / 256), 256, 0, c->stream>>>(
-        n, nvec, c->d_E, W, c->f_from_eig ? c->d_f : nullptr);
+        n, nvec, E, W, c->f_from_eig ? f : nullptr);
     c->launches++;
-    c->d_A = W;
     return cuda_check(c, cudaGetLastError(), "coupled eigenvectors");
+}
+
+int run_eig_coupled(bse_ctx* c, bool want_vectors) {
+    int st;
+    const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
+    if (c->S == 0) {
+        double2* W = (double2*)c->d_blk;
+        if ((st = solve_coupled_block(c, c->n_h, (double2*)c->d_H, W, rho0, c->d_E, c->d_f, want_vectors))) return st;
+        c->d_A = W;
+        return BSE_OK;
+    }
+    // collinear: M0 = spin blocks {1,2} (values only, 3195, 3317) and M1 = {0,3}, the optically
+    // active block (Q17), each 4N x 4N with its coupling part
+    const int64_t n4 = c->n_opt;
+    double2* M0 = (double2*)c->d_blk;
+    double2* M1 = M0 + n4 * n4;
+    double2* W = M1 + n4 * n4;
+    if ((st = solve_coupled_block(c, n4, M0, W, nullptr, c->d_E, nullptr, false))) return st;
+    if ((st = solve_coupled_block(c, n4, M1, W, rho0, c->d_E + n4, c->d_f, want_vectors))) return st;
+    c->d_A = W;
+    return BSE_OK;
 }
 
 int run_eig(bse_ctx* c, bool want_vectors) {

@@ -150,21 +150,22 @@ __global__ void exchange_table_kernel(int ns, int nw, int ng, Interaction it, do
 }
 
 // rho_cv[s*N + r, g] (Dipole_Elements::pull_values, k-diagonal branch, 1951-2066; Q12/Q13).
-// coupled (spinless): rows N..2N-1 hold rho_vc[r, g] = sum_a conj(c_va) M_a c_ca of
-// add_coupling_part (2937, 2950), with the valence states of rho_cv and the dipole column (Q25).
+// coupled: rows ns*N + s*N + r hold rho_vc[r, g] = sum_a conj(c_va) M_a c_ca of add_coupling_part
+// (2937, 2950), with the valence states of rho_cv and the dipole column (Q25).
 __global__ void rho_cv_kernel(int nk, int nc, int nv, int nw, int ns, int ng, int small_q, int coupled,
                               double q0, double q1, double q2,
                               const double* __restrict__ gcart, const double* __restrict__ centres,
                               const double2* __restrict__ cc, const double2* __restrict__ cv,
                               double2* __restrict__ rho) {
-    const int64_t N = (int64_t)nk * nc * nv, nrho = N * (coupled ? 2 : ns);
+    const int64_t N = (int64_t)nk * nc * nv, NR = N * ns, nrho = NR * (coupled ? 2 : 1);
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= nrho * ng) return;
     const int64_t i = t % nrho;
     const int g = (int)(t / nrho);
-    const bool vc = coupled && i >= N;
-    const int s = coupled ? 0 : (int)(i / N);
-    const int64_t r = i % N;
+    const bool vc = coupled && i >= NR;
+    const int64_t ii = vc ? i - NR : i;
+    const int s = (int)(ii / N);
+    const int64_t r = ii % N;
     const int k = (int)(r % nk), v = (int)((r / nk) % nv), c = (int)(r / ((int64_t)nk * nv));
     const int nb = nw * ns;
     const double qn = sqrt(q0 * q0 + q1 * q1 + q2 * q2);
@@ -377,18 +378,21 @@ __global__ void __launch_bounds__(256) build_kernel(BuildArgs a, const typename 
     }
 }
 
-// Coupling block B = H[0:N, N:2N] of the full BSE, spinless, FP64 (add_coupling_part,
-// bse.version13.cpp:2929-3040).  Same launch shape as build_kernel (lane = k1, warp = k2):
-//   direct   (rho_kk_cv W conj(rho_kk_vc), 2975-3033; Q26): P[r1,(ba)] pairs the valence state of
-//            exciton r1 with the conduction state of r2 through conj(Phi_ab(k2 - k1)),
-//   exchange (rho_cv(r1) conj(rho_vc(r2)), 2940-2967): the row factors Qx times P[r2,(bb)].
-// Every element of B is written once.
+// One block (row spin block br, column spin block bc) of the coupling part B = H[0:NA, NA:2NA] of the
+// full BSE, FP64 (add_coupling_part, bse.version13.cpp:2929-3040).  Same launch shape as
+// build_kernel (lane = k1, warp = k2):
+//   direct   (rho_kk_cv W conj(rho_kk_vc), 2975-3033; Q26; only bc = the partner block of br): the
+//            valence state of exciton r1 (spin sv1) pairs with the conduction state of r2, the
+//            valence state of r2 with the conduction state of r1 (spin sc1), through
+//            conj(Phi^{bc}_ab(k2 - k1)) -- the table of block bc has c-spin sv1 and v-spin sc1;
+//   exchange (rho_cv(r1) conj(rho_vc(r2)), 2940-2967; blocks 0|3 x 0|3): Qx[s1][s2] times P[r2,(bb)].
+// Every element of the block is written once.
 template <int NW>
 __global__ void __launch_bounds__(256) coupling_kernel(BuildArgs a, const double2* __restrict__ phi,
                                                        const double2* __restrict__ qx, double2* __restrict__ H) {
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x, warp = threadIdx.y, KW = blockDim.y;
-    const int nb = a.nw;                                                        // spinless: nb == nw
+    const int nb = a.nw * a.ns;
     double2* sC = reinterpret_cast<double2*>(smem_raw) + (size_t)warp * (a.nc + a.nv) * nb;   // [nc+nv][nb] of k2
     const int k1 = blockIdx.x * 32 + lane;
     const int k2 = blockIdx.y * KW + warp;
@@ -407,24 +411,29 @@ __global__ void __launch_bounds__(256) coupling_kernel(BuildArgs a, const double
     } else {
         d = (int64_t)k2 * a.nk + k1;
     }
-    const double2* ph = phi + (size_t)d * a.nblk * NW * NW;                    // exciton spin block 0
+    const double2* ph = phi + ((size_t)d * a.nblk + a.bc) * NW * NW;          // table of the column block
     const double2* sCc2 = sC;
     const double2* sCv2 = sC + (size_t)a.nc * nb;
+    const int sv1 = c_exc_spin[a.br].v, sc1 = c_exc_spin[a.br].c;            // direct: spins of row block br
+    const int s1 = a.br / 3, s2 = a.bc / 3;                                    // exchange: blocks 0 / 3
+    const int64_t NA = (int64_t)a.nblk * a.N;                                  // resonant block size
     for (int v1 = 0; v1 < a.nv; v1++) {
         double2 va[NW];
 #pragma unroll
         for (int al = 0; al < NW; al++)
-            va[al] = al < a.nw ? a.cv[((size_t)k1 * a.nv + v1) * nb + al] : make_double2(0, 0);   // c_v1(k1)
+            va[al] = al < a.nw ? a.cv[((size_t)k1 * a.nv + v1) * nb + sv1 * a.nw + al] : make_double2(0, 0);   // c_v1(k1)
         for (int c2 = 0; c2 < a.nc; c2++) {
             double2 S[NW];   // S[b] = sum_a c_v1a(k1) conj(c_c2a(k2)) conj(Phi_ab)
 #pragma unroll
             for (int b = 0; b < NW; b++) S[b] = make_double2(0, 0);
-            for (int al = 0; al < a.nw; al++) {
-                const double2 coef = tmul(va[al], cconj(sCc2[c2 * nb + al]));
-                const double2* prow = ph + al * NW;
+            if (a.do_direct) {
+                for (int al = 0; al < a.nw; al++) {
+                    const double2 coef = tmul(va[al], cconj(sCc2[c2 * nb + sv1 * a.nw + al]));
+                    const double2* prow = ph + al * NW;
 #pragma unroll
-                for (int b = 0; b < NW; b++)
-                    if (b < a.nw) cfma_conjb(S[b], coef, prow[b]);
+                    for (int b = 0; b < NW; b++)
+                        if (b < a.nw) cfma_conjb(S[b], coef, prow[b]);
+                }
             }
             for (int c1 = 0; c1 < a.nc; c1++) {
                 const int64_t r1 = (int64_t)c1 * a.nv * a.nk + (int64_t)v1 * a.nk + k1;
@@ -434,8 +443,8 @@ __global__ void __launch_bounds__(256) coupling_kernel(BuildArgs a, const double
                     tt[b] = make_double2(0, 0);
                     qq[b] = make_double2(0, 0);
                     if (b < a.nw) {
-                        tt[b] = tmul(S[b], cconj(a.cc[((size_t)k1 * a.nc + c1) * nb + b]));   // conj(c_c1b(k1))
-                        qq[b] = qx[(size_t)b * a.N + r1];
+                        if (a.do_direct) tt[b] = tmul(S[b], cconj(a.cc[((size_t)k1 * a.nc + c1) * nb + sc1 * a.nw + b]));   // conj(c_c1b(k1))
+                        if (a.do_exch) qq[b] = qx[((size_t)(s1 * a.ns + s2) * a.nw + b) * a.N + r1];
                     }
                 }
                 for (int v2 = 0; v2 < a.nv; v2++) {
@@ -444,34 +453,50 @@ __global__ void __launch_bounds__(256) coupling_kernel(BuildArgs a, const double
 #pragma unroll
                     for (int b = 0; b < NW; b++)
                         if (b < a.nw) {
-                            const double2 cvb = sCv2[v2 * nb + b];
-                            cfma(acc, tt[b], cvb);                                       // ... c_v2b(k2)
-                            cfma(accx, qq[b], tmul(cconj(sCc2[c2 * nb + b]), cvb));     // Qx P[r2,(bb)]
+                            if (a.do_direct) cfma(acc, tt[b], sCv2[v2 * nb + sc1 * a.nw + b]);   // ... c_v2b(k2)
+                            if (a.do_exch)                                                      // Qx P[r2,(bb)]
+                                cfma(accx, qq[b], tmul(cconj(sCc2[c2 * nb + s2 * a.nw + b]), sCv2[v2 * nb + s2 * a.nw + b]));
                         }
-                    H[r1 + a.ld * (a.N + r2)] = make_double2(a.fw * acc.x + accx.x, a.fw * acc.y + accx.y);
+                    H[(a.br * a.N + r1) + a.ld * (NA + a.bc * a.N + r2)] = make_double2(a.fw * acc.x + accx.x, a.fw * acc.y + accx.y);
                 }
             }
         }
     }
 }
 
-// M = [[A, B], [B^H, conj(A)]] from the top blocks (ld = 2N): the Hermitian matrix whose J-scaled
-// form J M is the full BSE matrix [[A, B], [-B^H, -conj(A)]] of 2917-2923 and 3035-3038.
-__global__ void coupled_lower_blocks_kernel(int64_t N, double2* __restrict__ M) {
+// M = [[A, B], [B^H, conj(A)]] from the top blocks (NA = resonant size, ld = 2 NA): the Hermitian
+// matrix whose J-scaled form J M is the full BSE matrix [[A, B], [-B^H, -conj(A)]] of 2917-2923 and
+// 3035-3038 (3107-3114 after the collinear rotation).
+__global__ void coupled_lower_blocks_kernel(int64_t NA, double2* __restrict__ M) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= N * N) return;
-    const int64_t i = t % N, j = t / N, ld = 2 * N;
-    M[(N + i) + ld * (N + j)] = cconj(M[i + ld * j]);
-    M[(N + i) + ld * j] = cconj(M[j + ld * (N + i)]);
+    if (t >= NA * NA) return;
+    const int64_t i = t % NA, j = t / NA, ld = 2 * NA;
+    M[(NA + i) + ld * (NA + j)] = cconj(M[i + ld * j]);
+    M[(NA + i) + ld * j] = cconj(M[j + ld * (NA + i)]);
+}
+
+// Collinear full BSE: the two 4N x 4N Hermitian blocks of M, M0 = spin blocks {1,2} and M1 = {0,3}
+// of every quadrant (common_diagonalization 3151-3172), from M (8N x 8N).
+__global__ void gather_coupled_blocks_kernel(int64_t N, const double2* __restrict__ M, double2* __restrict__ M0,
+                                             double2* __restrict__ M1) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t n4 = 4 * N, ld = 8 * N;
+    if (t >= n4 * n4) return;
+    const int64_t i = t % n4, j = t / n4;
+    // index within the 4N block: quadrant (i / 2N) and position p within the 2N half
+    auto map0 = [&](int64_t x) { const int64_t q = x / (2 * N), p = x % (2 * N); return q * 4 * N + N + p; };
+    auto map1 = [&](int64_t x) { const int64_t q = x / (2 * N), p = x % (2 * N); return q * 4 * N + (p < N ? p : p + 2 * N); };
+    M0[t] = M[map0(i) + ld * map0(j)];
+    M1[t] = M[map1(i) + ld * map1(j)];
 }
 
 // Collinear spin rotation U H U (spin_transformation, bse.version13.cpp:3048-3117), in place per
 // (row, col) position across the 4x4 spin blocks, so no block reads an already rotated one (Q24).
 template <typename T2>
-__global__ void spin_rotate_kernel(int64_t N, T2* __restrict__ H) {
+__global__ void spin_rotate_kernel(int64_t N, T2* __restrict__ H, int64_t ld) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= N * N) return;
-    const int64_t rr = t % N, cc = t / N, ld = 4 * N;
+    const int64_t rr = t % N, cc = t / N;
     const double h = 0.70710678118654752440;
     const double U[4][4] = {{1, 0, 0, 0}, {0, h, h, 0}, {0, h, -h, 0}, {0, 0, 0, 1}};
     double xr[4][4], xi[4][4];
@@ -543,29 +568,36 @@ int launch_build_nw(bse_ctx* c, void* H, int64_t ld, bool lower, const void* phi
 }
 
 template <int NW>
-int launch_coupling_nw(bse_ctx* c) {
+int launch_coupling_nw(bse_ctx* c, int br, int bc, int direct, int exch) {
     BuildArgs a = {};
     a.nk = c->nk; a.nc = c->nc; a.nv = c->nv; a.nw = c->nw; a.ns = c->ns;
-    a.N = c->N; a.ld = 2 * c->N;
+    a.N = c->N; a.ld = c->n_h;
+    a.br = br; a.bc = bc; a.do_direct = direct; a.do_exch = exch;
     a.fw = -1.0 / (c->geo.vol * c->nk);   // bse.version13.cpp:2960
     a.on_grid = c->dmap.on_grid;
     a.m0 = c->dmap.m[0]; a.m1 = c->dmap.m[1]; a.m2 = c->dmap.m[2];
-    a.nblk = 1;
+    a.nblk = 3 * c->S + 1;
     a.kidx = c->d_kidx;
     a.cc = c->d_cc; a.cv = c->d_cv;
     const int KW = 8;
     dim3 block(32, KW), grid((c->nk + 31) / 32, (c->nk + KW - 1) / KW, 1);
-    const size_t smem = (size_t)KW * (c->nc + c->nv) * c->nb * sizeof(double2);   // <= 8 * 16 * 16 * 16 = 32 KB
+    const size_t smem = (size_t)KW * (c->nc + c->nv) * c->nb * sizeof(double2);   // <= 8 * 16 * 32 * 16 = 64 KB
+    static std::once_flag smem_once;
+    static cudaError_t smem_err = cudaSuccess;
+    std::call_once(smem_once, [] {
+        smem_err = cudaFuncSetAttribute(coupling_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * 16 * 32 * 16);
+    });
+    if (smem_err != cudaSuccess) return cuda_check(c, smem_err, "coupling smem attribute");
     coupling_kernel<NW><<<grid, block, smem, c->stream>>>(a, c->d_phi, c->d_qx, (double2*)c->d_H);
     c->launches++;
     return cuda_check(c, cudaGetLastError(), "coupling kernel launch");
 }
 
-int launch_coupling(bse_ctx* c) {
-    if (c->nw <= 2) return launch_coupling_nw<2>(c);
-    if (c->nw <= 4) return launch_coupling_nw<4>(c);
-    if (c->nw <= 8) return launch_coupling_nw<8>(c);
-    return launch_coupling_nw<16>(c);
+int launch_coupling(bse_ctx* c, int br, int bc, int direct, int exch) {
+    if (c->nw <= 2) return launch_coupling_nw<2>(c, br, bc, direct, exch);
+    if (c->nw <= 4) return launch_coupling_nw<4>(c, br, bc, direct, exch);
+    if (c->nw <= 8) return launch_coupling_nw<8>(c, br, bc, direct, exch);
+    return launch_coupling_nw<16>(c, br, bc, direct, exch);
 }
 
 template <typename T>
@@ -644,7 +676,7 @@ int build_h64(bse_ctx* c) {
     }
     if (coll) {
         const int64_t nn = c->N * c->N;
-        spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, c->d_H64);
+        spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, c->d_H64, n64);
         c->launches++;
     }
     c->h64_pending = false;
@@ -694,16 +726,31 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
                    : launch_build<double>(c, c->d_H, ld, lower, phi, qx, br, bc, direct, exch, diag);
         if (st) return st;
     }
-    if (c->coupled && !c->p.ipa) {
-        if ((st = launch_coupling(c))) return st;
-        const int64_t nn = c->N * c->N;
-        coupled_lower_blocks_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, (double2*)c->d_H);
-        c->launches++;
+    if (c->coupled) {
+        // coupling part, spin-block pairs: exchange on (0|3, 0|3), direct on (b, partner of b) (2986-2989)
+        const int cpairs[6][2] = {{0, 0}, {3, 3}, {0, 3}, {3, 0}, {1, 2}, {2, 1}};
+        for (int pi = 0; pi < (coll ? 6 : 1); pi++) {
+            const int br = cpairs[pi][0], bc = cpairs[pi][1];
+            const int partner = (br == 0 || br == 3) ? br : 3 - br;
+            const int exch = (br == 0 || br == 3) && (bc == 0 || bc == 3);
+            if ((st = launch_coupling(c, br, bc, bc == partner ? 1 : 0, exch ? 1 : 0))) return st;
+        }
     }
     if (coll) {
         const int64_t nn = c->N * c->N;
-        if (mixed) spin_rotate_kernel<float2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, (float2*)c->d_H);
-        else spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, (double2*)c->d_H);
+        if (mixed) {
+            spin_rotate_kernel<float2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, (float2*)c->d_H, ld);
+        } else {
+            spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(c->N, (double2*)c->d_H, ld);
+            if (c->coupled)   // the coupling part is rotated the same way (3096-3105)
+                spin_rotate_kernel<double2><<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(
+                    c->N, (double2*)c->d_H + ld * (ld / 2), ld);
+        }
+        c->launches += c->coupled ? 2 : 1;
+    }
+    if (c->coupled) {
+        const int64_t NA = ld / 2;
+        coupled_lower_blocks_kernel<<<(unsigned)((NA * NA + 255) / 256), 256, 0, c->stream>>>(NA, (double2*)c->d_H);
         c->launches++;
     }
     stage_end(c, 2);
@@ -712,7 +759,12 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     // stream while the FP32 eigensolve runs, or by the refinement itself)
     c->h64_pending = mixed && !c->p.ipa && c->p.n_refine > 0;
     c->h64_side = false;
-    if (coll) {
+    if (coll && c->coupled) {
+        const int64_t n4 = 4 * c->N;
+        gather_coupled_blocks_kernel<<<(unsigned)((n4 * n4 + 255) / 256), 256, 0, c->stream>>>(
+            c->N, (const double2*)c->d_H, (double2*)c->d_blk, (double2*)c->d_blk + n4 * n4);
+        c->launches++;
+    } else if (coll) {
         const int64_t n2 = 2 * c->N;
         const size_t bb = (size_t)n2 * n2 * c->h_elem;
         if (mixed)
@@ -734,10 +786,10 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
         } else {
             if ((st = cuda_check(c, cudaMemcpyAsync(h_out, c->d_H, n * sizeof(double2), cudaMemcpyDeviceToHost, c->stream), "H copy"))) return st;
             if (c->coupled) {
-                // the device holds M; the caller gets the reference's matrix H = J M (rows N..2N-1 negated)
+                // the device holds M; the caller gets the reference's matrix H = J M (rows NA..2NA-1 negated)
                 if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "H copy sync"))) return st;
                 for (int64_t j = 0; j < ld; j++)
-                    for (int64_t i = c->N; i < ld; i++) {
+                    for (int64_t i = ld / 2; i < ld; i++) {
                         h_out[2 * (i + ld * j)] = -h_out[2 * (i + ld * j)];
                         h_out[2 * (i + ld * j) + 1] = -h_out[2 * (i + ld * j) + 1];
                     }

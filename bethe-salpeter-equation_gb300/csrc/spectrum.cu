@@ -128,7 +128,7 @@ int run_eps(bse_ctx* c, const double* omega, int n_omega, double gamma, double* 
     double* d_e1 = d_e2 + n_omega;
     if ((st = cuda_check(c, cudaMemcpyAsync(d_om, omega, b, cudaMemcpyHostToDevice, c->stream), "omega upload"))) return st;
     stage_begin(c, 6);
-    const double* E = c->S ? c->d_E + 2 * c->N : c->d_E;
+    const double* E = c->d_E + (c->n_exc - c->n_opt);   // collinear: the optically active block's values
     eps_kernel<<<(unsigned)(((int64_t)n_omega * 32 + 255) / 256), 256, 0, c->stream>>>(
         c->n_opt, E, c->d_f, d_om, n_omega, gamma, eps_prefactor(c), c->coupled ? 1 : 0, d_e2, d_e1);
     c->launches++;

@@ -91,7 +91,7 @@ typedef struct bse_params {
     double scissor;              /* added to conduction energies (815-816) */
     double q[3];                 /* excitonic momentum, q -> 0 (minval * x, 3590-3601) */
     int32_t tamm_dancoff;        /* 1: resonant block only; 0: full BSE with the coupling block B
-                                    (add_coupling_part 2929-3040), n_spin = 1 and BSE_FP64 only;
+                                    (add_coupling_part 2929-3040), BSE_FP64 only;
                                     no effect with ipa = 1 */
     int32_t ipa;                 /* 1: no kernel, H = diag(E_c - E_v) (3346-3365) */
     int32_t small_momentum;      /* 1: G=0 pair density is the dipole i q.<c|r|v> (1535-1650) */
@@ -116,8 +116,7 @@ int bse_version(void);
 
 /* Sizes derived from model+params: n_exc = (3*spin+1)*N eigenvalues, n_rho = (spin+1)*N
  * pair-density rows, n_h = dimension of the (full, before the spin split) BSE matrix.
- * Full BSE (tamm_dancoff = 0): each doubles (resonant rows, then anti-resonant; the sizes of the
- * reference's collinear full BSE are reported although bse_create accepts n_spin = 1 only). */
+ * Full BSE (tamm_dancoff = 0): each doubles (resonant rows, then anti-resonant). */
 int bse_sizes(const bse_model* model, const bse_params* params,
               int64_t* n_bse, int64_t* n_exc, int64_t* n_rho, int64_t* n_h);
 

@@ -19,10 +19,11 @@ SOLVERS = {"own": 0, "cusolver": 1}
 
 def _prob(synth, name):
     return {"hbn8": lambda: synth.hbn_problem(grid=8), "cubic4": lambda: synth.cubic3d_problem(grid=4),
-            "mag8": lambda: synth.magnetic4_problem(grid=8), "orb8_3": lambda: synth.orb8_problem(grid=3)}[name]()
+            "mag8": lambda: synth.magnetic4_problem(grid=8), "orb8_3": lambda: synth.orb8_problem(grid=3),
+            "coll3": lambda: synth.collinear_problem(grid=3), "coll4": lambda: synth.collinear_problem(grid=4)}[name]()
 
 
-@pytest.mark.parametrize("name", ["hbn8", "cubic4", "mag8", "orb8_3"])
+@pytest.mark.parametrize("name", ["hbn8", "cubic4", "mag8", "orb8_3", "coll3", "coll4"])
 def test_coupled_build_matches_oracle(synth, oracle, gpu, name):
     prob = _prob(synth, name)
     bands = oracle.bands(prob)
@@ -30,13 +31,14 @@ def test_coupled_build_matches_oracle(synth, oracle, gpu, name):
     with gpu.BSEContext(prob, tamm_dancoff=0) as ctx:
         ctx.set_bands(*bands)
         H, rho = ctx.build_kernel(want_h=True, want_rho=True)
-    assert H.shape == H_ref.shape == (2 * prob.n_bse, 2 * prob.n_bse)
+    nh = 2 * (3 * (prob.model.n_spin - 1) + 1) * prob.n_bse
+    assert H.shape == H_ref.shape == (nh, nh)
     assert np.abs(H - H_ref).max() < 1e-11 * np.abs(H_ref).max()
     assert np.abs(rho - rho_ref).max() < 1e-11 * max(1.0, np.abs(rho_ref).max())
 
 
 @pytest.mark.parametrize("solver", ["own", "cusolver"])
-@pytest.mark.parametrize("name", ["hbn8", "cubic4", "mag8"])
+@pytest.mark.parametrize("name", ["hbn8", "cubic4", "mag8", "coll4"])
 def test_coupled_solve_matches_oracle(synth, oracle, gpu, name, solver):
     prob = _prob(synth, name)
     bands = oracle.bands(prob)
@@ -48,7 +50,9 @@ def test_coupled_solve_matches_oracle(synth, oracle, gpu, name, solver):
         f = ctx.oscillators()
         e2, e1 = ctx.eps(OMEGA, GAMMA)
     assert np.abs(E - ref["E"]).max() < 1e-8
-    # |f|^2 per pair (phases are a gauge) where the level is separated from its neighbours
+    # |f|^2 per pair (phases are a gauge) where the level is separated from its neighbours;
+    # collinear: the pairs of the optically active block H1 (the second half of E)
+    E = E[len(E) - len(f):]
     gap = np.minimum(np.r_[np.inf, np.diff(E)], np.r_[np.diff(E), np.inf])
     sep = gap > 1e-6
     f2, f2r = np.abs(f) ** 2, np.abs(ref["f"]) ** 2
@@ -58,18 +62,22 @@ def test_coupled_solve_matches_oracle(synth, oracle, gpu, name, solver):
 
 
 @pytest.mark.parametrize("solver", ["own", "cusolver"])
-def test_coupled_vectors(synth, oracle, gpu, solver):
-    """a_out: the 2N eigenvectors of H = [[A, B], [-B^H, -A*]], J-normalised (x^H J x = sign E),
-    and f = rho^H x from them equals the oscillators of the solve."""
-    prob = _prob(synth, "hbn8")
+@pytest.mark.parametrize("name", ["hbn8", "coll4"])
+def test_coupled_vectors(synth, oracle, gpu, solver, name):
+    """a_out: the eigenvectors of H = [[A, B], [-B^H, -A*]] (collinear: of the optically active
+    block H1), J-normalised (x^H J x = sign E), and f = rho^H x from them equals the oscillators."""
+    prob = _prob(synth, name)
     bands = oracle.bands(prob)
     H_ref, rho_ref = oracle.build(prob, bands, tamm_dancoff=0)
-    N = prob.n_bse
+    if prob.model.n_spin == 2:
+        H_ref = oracle.split_blocks_coupled(H_ref, prob.n_bse)[1]
+    N = H_ref.shape[0] // 2
     J = np.r_[np.ones(N), -np.ones(N)]
     with gpu.BSEContext(prob, tamm_dancoff=0, eig_solver=SOLVERS[solver]) as ctx:
         ctx.set_bands(*bands)
         ctx.build_kernel()
         E, X = ctx.diagonalize(want_vectors=True)
+        E = E[len(E) - X.shape[1]:]
         f = ctx.oscillators()
     res = np.linalg.norm(H_ref @ X - X * E[None, :], axis=0)
     assert res.max() < 1e-8 * np.abs(H_ref).max() * 2 * N
