@@ -51,7 +51,7 @@ struct bse_ctx {
     // sizes
     int nw, ns, nb, nk, ng, nv, nc, S, nr;
     int64_t N, n_h, n_rho, n_exc, n_opt;
-    bool coupled = false;        // full BSE with the coupling block (tamm_dancoff = 0, not IPA; spinless, FP64)
+    bool coupled = false;        // full BSE with the coupling block (tamm_dancoff = 0, not IPA; FP64)
     bse_params p;
     bse::Geometry geo;
     bse::Interaction itx;

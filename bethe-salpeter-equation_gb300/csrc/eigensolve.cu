@@ -684,7 +684,7 @@ __global__ void jnorm_scale_kernel(int64_t n, int64_t ncols, const double* __res
 
 }  // namespace
 
-// Full BSE (tamm_dancoff = 0, spinless, FP64): common_diagonalization's eig_gen of the 2N x 2N
+// Full BSE (tamm_dancoff = 0, FP64): common_diagonalization's eig_gen of the 2N x 2N
 // matrix (bse.version13.cpp:3326) replaced by a structure-preserving Hermitian solve.  The build
 // left M = [[A, B], [B^H, conj(A)]] (H = J M) in d_H.  With M = L L^H (potrf; M must be positive
 // definite, the stable-ground-state case), H = J L L^H is similar to the Hermitian W = L^H J L,

@@ -154,11 +154,13 @@ int bse_build_kernel(bse_ctx* ctx, double* h_out, double* rho_out);
  * Full BSE (eig_gen of the 2N x 2N matrix, 3326): a structure-preserving solve through the
  * Cholesky factor of [[A, B], [B^H, conj(A)]], which must be positive definite (a stable
  * ground state; otherwise BSE_ERR_BAD_INPUT).  e_out: all 2N eigenvalues ascending, -E then +E;
- * a_out: 2N x 2N eigenvectors of H in that order, J-normalised: x^H diag(1,-1) x = sign(E). */
+ * a_out: 2N x 2N eigenvectors of H in that order, J-normalised: x^H diag(1,-1) x = sign(E).
+ * Collinear full BSE: the two 4N spin blocks (H0 = {1,2}, H1 = {0,3} of every quadrant) each solved
+ * that way; e_out holds H0's 4N values then H1's, a_out H1's 4N x 4N eigenvectors. */
 int bse_diagonalize(bse_ctx* ctx, double* e_out, double* a_out);
 
 /* Stage d: oscillator strengths f_l = sum_i conj(rho_i(G0)) A_il (3486-3502),
- * complex128, one per optically active exciton (spinless N, collinear 2N; full BSE 2N, from the
+ * complex128, one per optically active exciton (spinless N, collinear 2N; full BSE 2N / 4N, from the
  * J-normalised vectors and rho = (rho_cv; rho_vc)). */
 int bse_oscillators(bse_ctx* ctx, double* f_out);
 
