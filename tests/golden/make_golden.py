@@ -7,6 +7,7 @@ restatement; the GPU parity tests compare against the live oracle):
   coll3_golden.npz  collinear two-channel model, 3x3 grid, N = 9 (H is 36 x 36)
   hbn4_full_golden.npz  the hbn4 workload as a full BSE (tamm_dancoff = 0: coupling block,
                     2N = 32 eigenvalues, non-TDA spectrum)
+  coll3_full_golden.npz the coll3 workload as a full BSE (8N = 72 matrix, both 4N spin blocks)
 Run: python tests/golden/make_golden.py
 """
 import os
@@ -36,6 +37,9 @@ def main():
     r = orc.solve(synth.hbn_problem(grid=4), omega, gamma, tamm_dancoff=0)
     np.savez(os.path.join(HERE, "hbn4_full_golden.npz"), omega=omega, gamma=gamma, E=r["E"], eps2=r["eps2"],
              eps1=r["eps1"], absH=np.abs(r["H"]), absf=np.abs(r["f"]))
+    r = orc.solve(synth.collinear_problem(grid=3), omega, gamma, tamm_dancoff=0)
+    np.savez(os.path.join(HERE, "coll3_full_golden.npz"), omega=omega, gamma=gamma, E=r["E"], eps2=r["eps2"],
+             eps1=r["eps1"], absH=np.abs(r["H"]))
     print("wrote golden vectors")
 
 

@@ -177,3 +177,11 @@ def test_single_transition_closed_form(synth, oracle):
     X = r["A"]
     jn = np.einsum("il,i,il->l", X.conj(), np.array([1.0, -1.0]), X).real
     assert np.allclose(jn, [-1, 1], atol=1e-12)
+
+
+def test_golden_vectors_collinear(synth, oracle):
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "coll3_full_golden.npz"))
+    r = oracle.solve(synth.collinear_problem(grid=3), g["omega"], float(g["gamma"]), tamm_dancoff=0)
+    assert np.abs(r["E"] - g["E"]).max() < 1e-12 * np.abs(g["E"]).max()
+    assert np.abs(r["eps2"] - g["eps2"]).max() < 1e-12 * np.abs(g["eps2"]).max()
+    assert np.abs(np.abs(r["H"]) - g["absH"]).max() < 1e-12 * g["absH"].max()
