@@ -160,9 +160,11 @@ int validate(const bse_model* m, const bse_params* p) {
     if (p->nv > 8 || p->nc > 8) return fail(nullptr, BSE_ERR_BAD_INPUT, "nv, nc above 8 are not supported");
     if (p->tamm_dancoff != 0 && p->tamm_dancoff != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "tamm_dancoff must be 0 or 1");
     if (p->precision != BSE_FP64 && p->precision != BSE_MIXED) return fail(nullptr, BSE_ERR_BAD_INPUT, "precision");
-    if (p->tamm_dancoff == 0 && !p->ipa) {
-        if (p->precision != BSE_FP64)
-            return fail(nullptr, BSE_ERR_BAD_INPUT, "the full BSE (tamm_dancoff = 0) runs in FP64: set precision = BSE_FP64");
+    if (p->tamm_dancoff == 0 && !p->ipa && p->precision == BSE_MIXED) {
+        if (m->n_spin != 1)
+            return fail(nullptr, BSE_ERR_BAD_INPUT, "the mixed full BSE (tamm_dancoff = 0) is implemented for n_spin = 1");
+        if (p->eig_solver != BSE_EIG_OWN)
+            return fail(nullptr, BSE_ERR_BAD_INPUT, "the mixed full BSE (tamm_dancoff = 0) uses the own eigensolver");
     }
     if (p->eig_solver != BSE_EIG_OWN && p->eig_solver != BSE_EIG_CUSOLVER) return fail(nullptr, BSE_ERR_BAD_INPUT, "eig_solver");
     if (p->coulomb_kind != BSE_V_BARE_3D && p->coulomb_kind != BSE_V_BARE_2D) return fail(nullptr, BSE_ERR_BAD_INPUT, "coulomb_kind");
@@ -360,7 +362,7 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
         CK(dmalloc(c, &c->d_phi32, nphi * 8, "Phi32"));
         CK(dmalloc(c, &c->d_qx32, (size_t)c->N * nw * ns * ns * 8, "Qx32"));
     }
-    c->h_elem = mixed ? 8 : 16;
+    c->h_elem = mixed && !c->coupled ? 8 : 16;   // the full BSE is built in FP64 in both precisions
     CK(dmalloc(c, &c->d_H, (size_t)c->n_h * c->n_h * c->h_elem, "H"));
     if (c->coupled) {
         // spinless: L^H J L (2N); collinear: the two 4N blocks M0, M1 and L^H J L (4N)
@@ -370,7 +372,7 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     } else if (c->S) {
         CK(dmalloc(c, &c->d_blk, 2 * (size_t)(2 * c->N) * (2 * c->N) * c->h_elem, "spin blocks"));
     }
-    if (mixed && !p->ipa && p->n_refine > 0) {
+    if (mixed && !c->coupled && !p->ipa && p->n_refine > 0) {
         const size_t n64 = c->S ? 4 * c->N : c->N;
         CK(dmalloc(c, &c->d_H64, n64 * n64 * 16, "H64"));
     }

@@ -703,7 +703,7 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     if (!c->bands_valid) return fail(c, BSE_ERR_STATE, "bands not computed");
     if (!c->tables_valid && (st = run_tables(c))) return st;
     stage_begin(c, 2);
-    const bool mixed = c->p.precision == BSE_MIXED;
+    const bool mixed = c->p.precision == BSE_MIXED && !c->coupled;   // the full BSE is built in FP64
     const bool coll = c->S == 1;
     // the own eigensolver reads full Hermitian storage; cuSOLVER reads the lower triangle
     const bool lower = !full && !coll && !c->coupled && h_out == nullptr && c->p.eig_solver != BSE_EIG_OWN;
