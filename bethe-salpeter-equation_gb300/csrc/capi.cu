@@ -122,6 +122,22 @@ void analyse_k(bse_ctx* c, const bse_model* m) {
             d.idx[k] = packed;
         }
         d.on_grid = true;
+        // a complete periodic grid: k - dk and k + dk are grid points for every grid offset dk
+        const int64_t ncell = (int64_t)d.m[0] * d.m[1] * d.m[2];
+        bool per = ncell == nk;
+        for (int i = 0; i < 3 && per; i++)
+            if (d.m[i] > 1 && std::fabs(d.step[i] * d.m[i] - 1.0) > 1e-9) per = false;
+        if (per) {
+            d.inv.assign(ncell, -1);
+            for (int k = 0; k < nk && per; k++) {
+                const int32_t x = d.idx[k];
+                const int64_t cell = ((int64_t)(x & 1023) * d.m[1] + ((x >> 10) & 1023)) * d.m[2] + ((x >> 20) & 1023);
+                if (d.inv[cell] >= 0) per = false;
+                else d.inv[cell] = k;
+            }
+        }
+        d.periodic = per;
+        if (!per) d.inv.clear();
         d.n_delta = (int64_t)(2 * d.m[0] - 1) * (2 * d.m[1] - 1) * (2 * d.m[2] - 1);
     } else {
         d.on_grid = false;
@@ -168,7 +184,14 @@ int validate(const bse_model* m, const bse_params* p) {
     }
     if (p->eig_solver != BSE_EIG_OWN && p->eig_solver != BSE_EIG_CUSOLVER) return fail(nullptr, BSE_ERR_BAD_INPUT, "eig_solver");
     if (p->coulomb_kind != BSE_V_BARE_3D && p->coulomb_kind != BSE_V_BARE_2D) return fail(nullptr, BSE_ERR_BAD_INPUT, "coulomb_kind");
-    if (p->w_kind < BSE_W_EMPIRICAL || p->w_kind > BSE_W_BARE) return fail(nullptr, BSE_ERR_BAD_INPUT, "w_kind");
+    if (p->w_kind < BSE_W_EMPIRICAL || p->w_kind > BSE_W_RPA) return fail(nullptr, BSE_ERR_BAD_INPUT, "w_kind");
+    if (p->w_kind == BSE_W_RPA && !p->ipa) {
+        if (p->tamm_dancoff == 0)
+            return fail(nullptr, BSE_ERR_BAD_INPUT, "RPA screening is implemented for the Tamm-Dancoff BSE");
+        if (p->rpa_order != 0 && p->rpa_order != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_order must be 0 or 1");
+        if (p->rpa_points < 2 || p->rpa_points % 2) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_points must be even and >= 2");
+        if (!(p->rpa_eta >= 0.0) || !std::isfinite(p->rpa_eta)) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_eta must be >= 0");
+    }
     const size_t nw = m->nw, nr = m->n_r, ns = m->n_spin;
     if (!finite_all(m->r_cart, 3 * nr) || !finite_all(m->weights, nr) || !finite_all(m->h_r, 2 * nw * nw * nr * ns) ||
         !finite_all(m->centres, 3 * nw * ns) || !finite_all(m->lattice, 9) || !finite_all(m->k_cart, 3 * (size_t)m->n_k) ||
@@ -312,6 +335,10 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     it.nx = c->geo.normal[0]; it.ny = c->geo.normal[1]; it.nz = c->geo.normal[2]; it.lz = c->geo.lz;
     it.cell_avg = cell_average(c);
     analyse_k(c, m);
+    if (p->w_kind == BSE_W_RPA && !p->ipa && !c->dmap.periodic) {
+        destroy_ctx(c);
+        return fail(nullptr, BSE_ERR_BAD_INPUT, "RPA screening needs a complete periodic k grid (k - dk on the grid)");
+    }
     const int NWs = c->nw <= 2 ? 2 : c->nw <= 4 ? 4 : c->nw <= 8 ? 8 : 16;
     const int nblk = 3 * c->S + 1;
     if (!c->dmap.on_grid && (double)c->dmap.n_delta * nblk * NWs * NWs * 24.0 > 16e9) {
@@ -398,6 +425,7 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
         for (int i = 0; i < 3; i++)
             for (int j = 0; j < 3; j++) b[3 * i + j] = x[i][j] * 2.0 * kPi / c->geo.vol;
         CK(upload(c, c->d_bmat, b, 72, "b"));
+        std::memcpy(c->bmat_h, b, sizeof(b));
     }
     if (c->dmap.on_grid) CK(upload(c, c->d_kidx, c->dmap.idx.data(), nk * 4, "k index"));
     CK(cuda_check(c, cudaStreamSynchronize(c->stream), "uploads"));

@@ -150,3 +150,19 @@ def test_null_context_is_an_error_not_a_crash(gpu):
                                one.ctypes.data_as(C.POINTER(C.c_double)), dp, None) == -1
     assert b"n_exc" in lib.bse_last_error(None)
     assert lib.bse_eps_noalloc(4, dp, dp, 1.0, dp, 4, 0.05, dp, dp, None) == -1
+
+
+def test_rpa_validation(synth, gpu):
+    """BSE_W_RPA: even rpa_points >= 2, rpa_order 0 or 1, Tamm-Dancoff, a complete periodic k grid."""
+    prob = synth.hbn_problem(grid=3)
+    st, msg = _create(gpu, prob, w_kind=3, rpa_points=3)
+    assert st == -1 and "rpa_points" in msg
+    st, msg = _create(gpu, prob, w_kind=3, rpa_order=2)
+    assert st == -1 and "rpa_order" in msg
+    st, msg = _create(gpu, prob, w_kind=3, tamm_dancoff=0)
+    assert st == -1 and "Tamm-Dancoff" in msg
+    part = prob.__class__(prob.model, prob.k_cart[:-1], prob.g_cart, prob.params)
+    st, msg = _create(gpu, part, w_kind=3)
+    assert st in (-1, -2)          # the grid check needs the context: NO_DEVICE here, BAD_INPUT on a GPU
+    st, _ = _create(gpu, prob, w_kind=3)
+    assert st in (0, -2)
