@@ -94,6 +94,7 @@ struct bse_ctx {
 
     // kernel tables
     double2* d_phi = nullptr;    // [n_delta][nblk][nw][nw] direct-kernel lattice sums (FP64)
+    double2* d_phi_c = nullptr;  // RPA + full BSE: the coupling block's sums, with conj(W) (FP64)
     float2* d_phi32 = nullptr;   // the same in FP32 for the mixed build
     double2* d_X = nullptr;      // [ns][ns][nw][nw] exchange lattice sums
     double2* d_qx = nullptr;     // [ns][ns][nw][n_rho/ns] exchange row factors  Qx[s1][s2][beta][r]

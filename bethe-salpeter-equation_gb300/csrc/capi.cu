@@ -186,8 +186,6 @@ int validate(const bse_model* m, const bse_params* p) {
     if (p->coulomb_kind != BSE_V_BARE_3D && p->coulomb_kind != BSE_V_BARE_2D) return fail(nullptr, BSE_ERR_BAD_INPUT, "coulomb_kind");
     if (p->w_kind < BSE_W_EMPIRICAL || p->w_kind > BSE_W_RPA) return fail(nullptr, BSE_ERR_BAD_INPUT, "w_kind");
     if (p->w_kind == BSE_W_RPA && !p->ipa) {
-        if (p->tamm_dancoff == 0)
-            return fail(nullptr, BSE_ERR_BAD_INPUT, "RPA screening is implemented for the Tamm-Dancoff BSE");
         if (p->rpa_order != 0 && p->rpa_order != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_order must be 0 or 1");
         if (p->rpa_points < 2 || p->rpa_points % 2) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_points must be even and >= 2");
         if (!(p->rpa_eta >= 0.0) || !std::isfinite(p->rpa_eta)) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_eta must be >= 0");
@@ -232,7 +230,7 @@ void destroy_ctx(bse_ctx* c) {
     if (c->side) cudaStreamSynchronize(c->side);
     if (c->side2) cudaStreamSynchronize(c->side2);
     void* ptrs[] = {c->d_rcart, c->d_weights, c->d_hr, c->d_centres, c->d_k, c->d_bmat, c->d_kidx, c->d_g, c->d_status,
-                    c->d_ec, c->d_ev, c->d_cc, c->d_cv, c->d_phi, c->d_phi32, c->d_X, c->d_qx, c->d_qx32, c->d_rho,
+                    c->d_ec, c->d_ev, c->d_cc, c->d_cv, c->d_phi, c->d_phi_c, c->d_phi32, c->d_X, c->d_qx, c->d_qx32, c->d_rho,
                     c->d_H, c->d_H64, c->d_blk, c->d_aux, c->d_E, c->d_f, c->d_work};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -384,6 +382,7 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     CK(dmalloc(c, &c->d_qx, (size_t)c->N * nw * ns * ns * 16, "Qx"));
     const size_t nphi = (size_t)c->dmap.n_delta * nblk * NWs * NWs;
     CK(dmalloc(c, &c->d_phi, nphi * 16, "Phi"));
+    if (c->coupled && p->w_kind == BSE_W_RPA) CK(dmalloc(c, &c->d_phi_c, nphi * 16, "Phi (coupling)"));
     const bool mixed = p->precision == BSE_MIXED;
     if (mixed) {
         CK(dmalloc(c, &c->d_phi32, nphi * 8, "Phi32"));

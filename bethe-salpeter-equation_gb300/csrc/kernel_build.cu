@@ -606,10 +606,12 @@ __global__ void rpa_w_kernel(int D, int ng, const double* __restrict__ qs, const
     }
 }
 
-// Phi[dd][blk][a][b] = sum_GG' e^{-i(G+q).tau^{sc}_a} W_GG' e^{i(G'+q).tau^{sv}_b} for D table entries
+// Phi[dd][blk][a][b] = sum_GG' e^{-i(G+q).tau^{sc}_a} W_GG' e^{i(G'+q).tau^{sv}_b} for D table entries;
+// conj_w: the same sums with conj(W_GG'), the coupling block's table (for a real diagonal W the two agree)
 __global__ void rpa_phi_kernel(int D, const int64_t* __restrict__ didx, const double* __restrict__ qs, int nblk, int nw,
                                int stride, int ng, const double* __restrict__ gcart, const double* __restrict__ centres,
-                               const double2* __restrict__ W, double2* __restrict__ phi, float2* __restrict__ phi32) {
+                               const double2* __restrict__ W, double2* __restrict__ phi, float2* __restrict__ phi32,
+                               int conj_w) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= (int64_t)D * nblk * nw * nw) return;
     const int b = (int)(t % nw), a = (int)((t / nw) % nw);
@@ -631,7 +633,8 @@ __global__ void rpa_phi_kernel(int D, const int64_t* __restrict__ didx, const do
             const double pi_ = -((Gi[0] + q[0]) * ta[0] + (Gi[1] + q[1]) * ta[1] + (Gi[2] + q[2]) * ta[2]);
             double si_, ci_;
             sincos(pi_, &si_, &ci_);
-            const double2 x = w[i + (int64_t)ng * j];
+            double2 x = w[i + (int64_t)ng * j];
+            if (conj_w) x.y = -x.y;
             sr += ci_ * x.x - si_ * x.y;
             si += ci_ * x.y + si_ * x.x;
         }
@@ -741,7 +744,8 @@ int launch_coupling_nw(bse_ctx* c, int br, int bc, int direct, int exch) {
         smem_err = cudaFuncSetAttribute(coupling_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * 16 * 32 * 16);
     });
     if (smem_err != cudaSuccess) return cuda_check(c, smem_err, "coupling smem attribute");
-    coupling_kernel<NW><<<grid, block, smem, c->stream>>>(a, c->d_phi, c->d_qx, (double2*)c->d_H);
+    // with an RPA W the coupling block pairs the states through conj(W) (its own table)
+    coupling_kernel<NW><<<grid, block, smem, c->stream>>>(a, c->d_phi_c ? c->d_phi_c : c->d_phi, c->d_qx, (double2*)c->d_H);
     c->launches++;
     return cuda_check(c, cudaGetLastError(), "coupling kernel launch");
 }
@@ -799,6 +803,7 @@ int run_tables(bse_ctx* c) {
         const int64_t total = c->dmap.n_delta * nblk * NWs * NWs;
         if ((st = cuda_check(c, cudaMemsetAsync(c->d_phi, 0, total * sizeof(double2), c->stream), "phi clear"))) return st;
         if (c->d_phi32 && (st = cuda_check(c, cudaMemsetAsync(c->d_phi32, 0, total * sizeof(float2), c->stream), "phi32 clear"))) return st;
+        if (c->d_phi_c && (st = cuda_check(c, cudaMemsetAsync(c->d_phi_c, 0, total * sizeof(double2), c->stream), "phi clear"))) return st;
         if (c->p.w_kind == BSE_W_RPA) {
             if ((st = run_rpa_tables(c))) return st;
         } else {
@@ -942,8 +947,13 @@ int run_rpa_tables(bse_ctx* c) {
         const int64_t tp = Dn * nblk * nw * nw;
         rpa_phi_kernel<<<(unsigned)((tp + 255) / 256), 256, 0, c->stream>>>(
             (int)Dn, ddi, dqs, nblk, nw, NWs, ng, c->d_g, c->d_centres, W, c->d_phi,
-            c->p.precision == BSE_MIXED ? c->d_phi32 : nullptr);
+            c->p.precision == BSE_MIXED && !c->coupled ? c->d_phi32 : nullptr, 0);
         c->launches += 2;
+        if (c->d_phi_c) {
+            rpa_phi_kernel<<<(unsigned)((tp + 255) / 256), 256, 0, c->stream>>>(
+                (int)Dn, ddi, dqs, nblk, nw, NWs, ng, c->d_g, c->d_centres, W, c->d_phi_c, nullptr, 1);
+            c->launches++;
+        }
         // the host arrays of this chunk must outlive its copies
         if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "RPA chunk"))) break;
     }
@@ -999,8 +1009,13 @@ int run_rpa_tables(bse_ctx* c) {
             if (!st) {
                 rpa_phi_kernel<<<(unsigned)((nblk * nw * nw + 255) / 256), 256, 0, c->stream>>>(
                     1, ddi, dqs, nblk, nw, NWs, ng, c->d_g, c->d_centres, W, c->d_phi,
-                    c->p.precision == BSE_MIXED ? c->d_phi32 : nullptr);
+                    c->p.precision == BSE_MIXED && !c->coupled ? c->d_phi32 : nullptr, 0);
                 c->launches++;
+                if (c->d_phi_c) {
+                    rpa_phi_kernel<<<(unsigned)((nblk * nw * nw + 255) / 256), 256, 0, c->stream>>>(
+                        1, ddi, dqs, nblk, nw, NWs, ng, c->d_g, c->d_centres, W, c->d_phi_c, nullptr, 1);
+                    c->launches++;
+                }
                 st = cuda_check(c, cudaStreamSynchronize(c->stream), "RPA dk = 0");
             }
         }

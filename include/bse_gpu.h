@@ -64,7 +64,7 @@ enum { BSE_V_BARE_3D = 0, BSE_V_BARE_2D = 1 };
  *                    eps^-1_GG'(dk) v(dk + G') with the static RPA eps^-1 of the kept bands
  *                    (Dielectric_Function::pull_values 2214-2315; rpa_order 0 first order, 1 Dyson),
  *                    dk = 0 from rpa_points seeded points of the mini-BZ sphere.  Needs a complete
- *                    periodic k grid and the Tamm-Dancoff BSE. */
+ *                    periodic k grid. */
 enum { BSE_W_EMPIRICAL = 0, BSE_W_RYTOVA_KELDYSH = 1, BSE_W_BARE = 2, BSE_W_RPA = 3 };
 
 /* Arithmetic of the build and of the dense solve. */

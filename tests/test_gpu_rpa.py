@@ -54,3 +54,15 @@ def test_rpa_mixed_build(synth, oracle, gpu):
         ctx.set_bands(*bands)
         H, _ = ctx.build_kernel(want_h=True)
     assert np.abs(H - H_ref).max() < 2e-6 * np.abs(H_ref).max()
+
+
+def test_rpa_full_bse_build(synth, oracle, gpu):
+    """RPA W with the coupling block: the coupling pairs the states through conj(W), its own table."""
+    prob = _prob(synth, "hbn6")
+    kw = dict(w_kind=3, rpa_order=1, rpa_points=8, rpa_seed=3, tamm_dancoff=0)
+    bands = oracle.bands(prob)
+    H_ref, _ = oracle.build(prob, bands, **kw)
+    with gpu.BSEContext(prob, **kw) as ctx:
+        ctx.set_bands(*bands)
+        H, _ = ctx.build_kernel(want_h=True)
+    assert np.abs(H - H_ref).max() < 1e-10 * np.abs(H_ref).max()
