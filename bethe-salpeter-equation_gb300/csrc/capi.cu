@@ -177,8 +177,6 @@ int validate(const bse_model* m, const bse_params* p) {
     if (p->tamm_dancoff != 0 && p->tamm_dancoff != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "tamm_dancoff must be 0 or 1");
     if (p->precision != BSE_FP64 && p->precision != BSE_MIXED) return fail(nullptr, BSE_ERR_BAD_INPUT, "precision");
     if (p->tamm_dancoff == 0 && !p->ipa && p->precision == BSE_MIXED) {
-        if (m->n_spin != 1)
-            return fail(nullptr, BSE_ERR_BAD_INPUT, "the mixed full BSE (tamm_dancoff = 0) is implemented for n_spin = 1");
         if (p->eig_solver != BSE_EIG_OWN)
             return fail(nullptr, BSE_ERR_BAD_INPUT, "the mixed full BSE (tamm_dancoff = 0) uses the own eigensolver");
     }

@@ -808,8 +808,10 @@ __global__ void mu_to_lambda_kernel(int64_t n, int64_t npos, const double* __res
     const double lam = -1.0 / mu[t];
     const int64_t o = t < npos ? (n - npos) + t : t - npos;
     E[o] = lam;
-    const double s = sqrt(fabs(lam));
-    f[o] = make_double2(fmu[t].x * s, fmu[t].y * s);
+    if (f) {
+        const double s = sqrt(fabs(lam));
+        f[o] = make_double2(fmu[t].x * s, fmu[t].y * s);
+    }
 }
 
 // S = Pbot - Ptop = -X^H J X (m x m)
@@ -861,13 +863,12 @@ __global__ void coupled_refined_kernel(int64_t n, int64_t N, const double* __res
 // f from (L^{-1} rho)^H y, the lowest n_refine + guard vectors), then an FP64 Rayleigh-Ritz step on the
 // definite pencil J x = (1/E) M x in the span of x = L^{-H} y: (S, G) = (-X^H J X, X^H M X), products
 // in compensated FP32, eigenpairs by the Ogita-Aishima refinement (dense fallback).
-int run_eig_coupled_mixed(bse_ctx* c) {
+// One n x n block: M64 the FP64 M (consumed), L / K two n x n FP32 workspaces, E the n eigenvalues,
+// rho0 / f the optical vector and oscillators (null for a values-only block, which is not refined).
+int mixed_coupled_block(bse_ctx* c, int64_t n, double2* M64, float2* L, float2* K, const double2* rho0, double* E,
+                        double2* f) {
     int st;
-    const int64_t n = c->n_h, N = n / 2;
-    double2* M64 = (double2*)c->d_H;
-    float2* L = (float2*)c->d_blk;
-    float2* K = L + n * n;
-    const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
+    const int64_t N = n / 2;
     cublasSetStream(c->cublas, c->stream);
     cusolverDnSetStream(c->cusolver, c->stream);
     narrow_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, c->stream>>>(n * n, M64, L);
@@ -905,17 +906,20 @@ int run_eig_coupled_mixed(bse_ctx* c) {
                                           n, n, &one, (const cuComplex*)L, n, (const cuComplex*)K, n, (cuComplex*)K, n),
                            "-Li J Li^H"))) return st;
     hermitian_part32_kernel<<<gb, 256, 0, c->stream>>>(n, K);
-    trmv_lower32_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(n, L, rho0, c->d_aux);   // L^{-1} rho
-    c->launches += 2;
+    c->launches++;
+    if (rho0) {
+        trmv_lower32_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(n, L, rho0, c->d_aux);   // L^{-1} rho
+        c->launches++;
+    }
     if ((st = cuda_check(c, cudaGetLastError(), "mixed coupled setup"))) return st;
-    const int64_t m = c->p.n_refine > 0 ? std::min<int64_t>(N, (int64_t)c->p.n_refine + kGuard) : 0;
+    const int64_t m = (rho0 && c->p.n_refine > 0) ? std::min<int64_t>(N, (int64_t)c->p.n_refine + kGuard) : 0;
     const int64_t nref = std::min<int64_t>(N, std::max(c->p.n_refine, 0));
     // mu into the upper half of d_E's storage is not possible (n doubles needed): use the arena top
     double* mu = nullptr;
     double2* fmu = nullptr;
     if ((st = cuda_check(c, cudaMallocAsync((void**)&mu, n * sizeof(double), c->stream), "mu"))) return st;
-    if ((st = cuda_check(c, cudaMallocAsync((void**)&fmu, n * sizeof(double2), c->stream), "f(mu)"))) return st;
-    st = own_heevd(c, (int)n, K, (int)n, false, mu, (int)m, c->d_aux, fmu);
+    if (rho0 && (st = cuda_check(c, cudaMallocAsync((void**)&fmu, n * sizeof(double2), c->stream), "f(mu)"))) return st;
+    st = own_heevd(c, (int)n, K, (int)n, false, mu, (int)m, rho0 ? c->d_aux : nullptr, fmu);
     if (!st) {
         // count the negative mu (= positive lambda) on the host
         std::vector<double> hmu(n);
@@ -925,17 +929,14 @@ int run_eig_coupled_mixed(bse_ctx* c) {
         for (double v : hmu) npos += v < 0.0;
         if (!st && npos < m) st = fail(c, BSE_ERR_NOT_CONVERGED, "full BSE: fewer positive excitations than refined pairs");
         if (!st) {
-            mu_to_lambda_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, npos, mu, fmu, c->d_E, c->d_f);
+            mu_to_lambda_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, npos, mu, fmu, E, f);
             c->launches++;
             st = cuda_check(c, cudaGetLastError(), "mu -> lambda");
         }
     }
     cudaFreeAsync(mu, c->stream);
-    cudaFreeAsync(fmu, c->stream);
+    if (fmu) cudaFreeAsync(fmu, c->stream);
     if (st) return st;
-    c->f_from_eig = true;
-    c->n_vec_valid = 0;
-    c->n_refined = 0;
     if (m == 0) return BSE_OK;
     // X = L^{-H} Y for the m lowest mu (the m smallest positive excitation energies)
     if ((st = cublas_check(c, cublasCtrmm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
@@ -986,7 +987,7 @@ int run_eig_coupled_mixed(bse_ctx* c) {
     // refined vectors XZ (M-normalised) and M XZ; then E, J-normalised f and residuals of the lowest nref
     if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, (const float4*)X4, n, (const double2*)Zb, m, X, n, Pw, pcap))) return st;  // X Z
     if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, (const float4*)Y4, n, (const double2*)Zb, m, Y, n, Pw, pcap))) return st;  // M X Z
-    coupled_refined_kernel<<<(unsigned)nref, 256, 0, c->stream>>>(n, N, theta, X, Y, rho0, c->d_E + N, c->d_f + N, rn);
+    coupled_refined_kernel<<<(unsigned)nref, 256, 0, c->stream>>>(n, N, theta, X, Y, rho0, E + N, f + N, rn);
     c->launches++;
     std::vector<double> hrn(nref);
     if ((st = cuda_check(c, cudaMemcpyAsync(hrn.data(), rn, nref * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "residuals"))) return st;
@@ -996,6 +997,26 @@ int run_eig_coupled_mixed(bse_ctx* c) {
     c->n_refined = nref;
     stage_end(c, 4);
     return cuda_check(c, cudaGetLastError(), "mixed coupled refinement");
+}
+
+int run_eig_coupled_mixed(bse_ctx* c) {
+    int st;
+    const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
+    c->f_from_eig = true;
+    c->n_vec_valid = 0;
+    c->n_refined = 0;
+    if (c->S == 0) {
+        const int64_t n = c->n_h;
+        float2* L = (float2*)c->d_blk;
+        return mixed_coupled_block(c, n, (double2*)c->d_H, L, L + n * n, rho0, c->d_E, c->d_f);
+    }
+    // collinear: M0 (values only) and the optically active M1, each 4N; L and K in the third slot
+    const int64_t n4 = c->n_opt;
+    double2* M0 = (double2*)c->d_blk;
+    double2* M1 = M0 + n4 * n4;
+    float2* L = (float2*)(M1 + n4 * n4);
+    if ((st = mixed_coupled_block(c, n4, M0, L, L + n4 * n4, nullptr, c->d_E, nullptr))) return st;
+    return mixed_coupled_block(c, n4, M1, L, L + n4 * n4, rho0, c->d_E + n4, c->d_f);
 }
 
 int run_eig_coupled(bse_ctx* c, bool want_vectors) {

@@ -64,15 +64,15 @@ def test_rejects_nan(synth, gpu):
 
 
 def test_full_bse_validation(synth, gpu):
-    """tamm_dancoff = 0 (coupling block): FP64, or mixed with the own solver for n_spin = 1."""
+    """tamm_dancoff = 0 (coupling block): FP64, or mixed with the own solver."""
     st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=2)
     assert st == -1 and "tamm_dancoff" in msg
     st, _ = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0, precision=1)
     assert st in (0, -2)
     st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0, precision=1, eig_solver=1)
     assert st == -1 and "own eigensolver" in msg
-    st, msg = _create(gpu, synth.collinear_problem(grid=2), tamm_dancoff=0, precision=1)
-    assert st == -1 and "n_spin" in msg
+    st, _ = _create(gpu, synth.collinear_problem(grid=2), tamm_dancoff=0, precision=1)
+    assert st in (0, -2)
     st, _ = _create(gpu, synth.collinear_problem(grid=2), tamm_dancoff=0)
     assert st in (0, -2)
     st, _ = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0)

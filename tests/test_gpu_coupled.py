@@ -111,7 +111,7 @@ def test_coupled_not_positive_definite_is_an_error(synth, gpu):
             ctx.diagonalize()
 
 
-@pytest.mark.parametrize("name", ["hbn8", "mag8"])
+@pytest.mark.parametrize("name", ["hbn8", "mag8", "coll4"])
 def test_coupled_mixed_matches_oracle(synth, oracle, gpu, name):
     """BSE_MIXED full BSE: FP32 Cholesky / inverse and the own FP32 solve of -L^-1 J L^-H, FP64
     refinement of the lowest n_refine positive pairs on the definite pencil (J, M).  Refined
@@ -128,14 +128,14 @@ def test_coupled_mixed_matches_oracle(synth, oracle, gpu, name):
         f = ctx.oscillators()
         e2, _ = ctx.eps(OMEGA, GAMMA)
         dg = ctx.diagnostics()
-    N = prob.n_bse
     Er = ref["E"]
-    assert np.abs(E[N:N + n_ref] - Er[N:N + n_ref]).max() < 1e-8
-    emin = Er[N]
+    N = len(f) // 2            # positive pairs of the optically active block
+    off = len(E) - len(f)      # collinear: that block's values follow the spin-flip block's
+    assert np.abs(E[off + N:off + N + n_ref] - Er[off + N:off + N + n_ref]).max() < 1e-8
+    emin = np.abs(Er).min()
     assert np.all(np.abs(E - Er) <= np.maximum(1e-5, 1e-6 * Er ** 2 / emin))
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-4 * np.linalg.norm(ref["eps2"])
     assert dg["n_refined"] == n_ref and dg["max_refined_residual"] < 1e-8 * np.abs(Er).max()
-    assert len(f) == 2 * N
 
 
 def test_coupled_mixed_limits(synth, gpu):
