@@ -96,7 +96,7 @@ typedef struct bse_params {
     double scissor;              /* added to conduction energies (815-816) */
     double q[3];                 /* excitonic momentum, q -> 0 (minval * x, 3590-3601) */
     int32_t tamm_dancoff;        /* 1: resonant block only; 0: full BSE with the coupling block B
-                                    (add_coupling_part 2929-3040), BSE_FP64 only;
+                                    (add_coupling_part 2929-3040); BSE_MIXED uses the own solver;
                                     no effect with ipa = 1 */
     int32_t ipa;                 /* 1: no kernel, H = diag(E_c - E_v) (3346-3365) */
     int32_t small_momentum;      /* 1: G=0 pair density is the dipole i q.<c|r|v> (1535-1650) */
