@@ -9,6 +9,10 @@
   *_centres.xyz  count line, comment line, nw lines "X x y z", then the atoms
                  (repeated per spin channel, bse.version13.cpp:608-634)
   k list         3 numbers per line, crystal or cartesian (bse.version13.cpp:186-203)
+  spectrum       output of pull_macroscopic_bse_dielectric_function (3644-3656): a header line, then
+                 per frequency "(w,0) (eps_xx) (w,0) (eps_yy) (w,0) (eps_zz) Im(eps_avg)/3" with
+                 complex numbers printed as "(re,im)"; only xx is computed, so yy = zz = (0,0) and the
+                 last column is Im(eps_xx)/3 (quirk Q16)
 
 The reader keeps the reference's semantics: the R vectors of a block are the ones given
 on the first line of each group of nw*nw lines, converted crystal->cartesian with the
@@ -169,3 +173,67 @@ def read_model_files(paths, nw: int, n_r: int, n_atoms: int, n_spin: int = 1,
     centres = read_centres(paths["centres"], nw, n_atoms, n_spin)
     return TBModel(lattice=lat, r_cryst=r_cryst, weights=weights, h_r=h_r,
                    centres=centres, dim=dim, name=name)
+
+
+def _cx(z: complex) -> str:
+    return f"({z.real:.10g},{z.imag:.10g})"
+
+
+def write_spectrum(path, omega, eps2, eps1):
+    """The reference's dielectric-function file for eps_xx = eps1 + i eps2 (3644-3656)."""
+    with open(path, "w") as fh:
+        fh.write("### omega xx xy xz yx yy yz zx zy zz\n")
+        for w, e2, e1 in zip(np.asarray(omega, float), np.asarray(eps2, float), np.asarray(eps1, float)):
+            wc = _cx(complex(w, 0.0))
+            fh.write(f"{wc} {_cx(complex(e1, e2))} {wc} (0,0) {wc} (0,0) {e2 / 3:.10g}\n")
+
+
+def read_spectrum(path):
+    """(omega, eps_xx) from a dielectric-function file in the reference's layout."""
+    om, eps = [], []
+    with open(path) as fh:
+        for line in fh:
+            if line.startswith("#") or not line.strip():
+                continue
+            f = line.split()
+            w = complex(*map(float, f[0].strip("()").split(",")))
+            e = complex(*map(float, f[1].strip("()").split(",")))
+            om.append(w.real)
+            eps.append(e)
+    return np.asarray(om), np.asarray(eps)
+
+
+def read_band_path(path, n_segments: int, crystal: bool = False, reciprocal=None):
+    """Segments of a band-structure path, the file of Hamiltonian_TB::pull_bands
+    (bse.version13.cpp:823-875): per segment "kx ky kz  kx ky kz  n" (start, end, points).
+    crystal: coordinates in units of the reciprocal vectors (columns of `reciprocal`), converted
+    to cartesian as 841-851 do.  Returns [(k_start, k_end, n), ...] in cartesian coordinates."""
+    vals = np.loadtxt(path).reshape(-1, 7)[:n_segments]
+    segs = []
+    for row in vals:
+        a, b, n = row[:3].copy(), row[3:6].copy(), int(row[6])
+        if crystal:
+            a, b = np.asarray(reciprocal) @ a, np.asarray(reciprocal) @ b
+        segs.append((a, b, n))
+    return segs
+
+
+def band_path_points(segments) -> np.ndarray:
+    """k points of the path: n points per segment from start to end inclusive (853-857)."""
+    pts = []
+    for a, b, n in segments:
+        for j in range(n):
+            t = j / (n - 1) if n > 1 else 0.0
+            pts.append(a * (1.0 - t) + b * t)
+    return np.asarray(pts).reshape(-1, 3)
+
+
+def write_bands(path, e_v, e_c, n_spin: int):
+    """The bands file of pull_bands (858-864): per k, for each spin row the selected valence
+    bands (top-down from E_F) then the conduction bands (bottom-up, with the scissor)."""
+    with open(path, "w") as fh:
+        for k in range(e_v.shape[1]):
+            row = []
+            for s in range(n_spin):
+                row += [f"{x:.10g}" for x in e_v[s, k]] + [f"{x:.10g}" for x in e_c[s, k]]
+            fh.write(" ".join(row) + " \n")
