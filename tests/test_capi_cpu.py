@@ -152,6 +152,34 @@ def test_null_context_is_an_error_not_a_crash(gpu):
     assert lib.bse_eps_noalloc(4, dp, dp, 1.0, dp, 4, 0.05, dp, dp, None) == -1
 
 
+def test_rejects_out_of_range_inputs(synth, gpu):
+    """Empty lists, more than 16 orbitals or 8 bands, unknown enum values, a missing -R partner:
+    BSE_ERR_BAD_INPUT before any device work."""
+    import dataclasses
+    base = synth.hbn_problem(grid=2)
+    cases = []
+    cases.append((dataclasses.replace(base, k_cart=base.k_cart[:0]), {}, "empty"))
+    cases.append((dataclasses.replace(base, g_cart=base.g_cart[:0]), {}, "empty"))
+    cases.append((base, {"nv": 9}, None))
+    cases.append((base, {"precision": 2}, "precision"))
+    cases.append((base, {"eig_solver": 5}, "eig_solver"))
+    cases.append((base, {"coulomb_kind": 7}, "coulomb_kind"))
+    cases.append((base, {"w_kind": 9}, "w_kind"))
+    cases.append((base, {"scissor": float("inf")}, "NaN"))
+    for prob, kw, word in cases:
+        st, msg = _create(gpu, prob, **kw)
+        assert st == -1, (kw, msg)
+        if word:
+            assert word in msg, (kw, msg)
+    # H(R) without its -R partner: drop the first non-zero R
+    m = base.model
+    drop = next(i for i in range(m.n_r) if np.abs(m.r_cryst[i]).sum() > 0)
+    keep = [i for i in range(m.n_r) if i != drop]
+    m2 = dataclasses.replace(m, r_cryst=m.r_cryst[keep], weights=m.weights[keep], h_r=m.h_r[:, keep])
+    st, msg = _create(gpu, dataclasses.replace(base, model=m2))
+    assert st == -1 and "-R" in msg
+
+
 def test_rpa_validation(synth, gpu):
     """BSE_W_RPA: even rpa_points >= 2, rpa_order 0 or 1, a complete periodic k grid."""
     prob = synth.hbn_problem(grid=3)

@@ -163,3 +163,17 @@ def test_golden_vectors(synth, oracle):
     assert np.abs(r["E"] - g["E"]).max() < 1e-12
     assert np.abs(r["eps2"] - g["eps2"]).max() < 1e-12 * np.abs(g["eps2"]).max()
     assert np.abs(np.abs(r["H"]) - g["absH"]).max() < 1e-12 * g["absH"].max()
+
+
+def test_single_transition_closed_form(synth, oracle):
+    """One k point, 1v x 1c: H = [[a, b], [-b*, -a]] has the eigenvalues +-sqrt(a^2 - |b|^2)."""
+    prob = synth.hbn_problem(grid=1)
+    H, _ = oracle.build(prob, tamm_dancoff=0)
+    assert H.shape == (2, 2)
+    a, b = H[0, 0].real, H[0, 1]
+    r = oracle.solve(prob, OMEGA, GAMMA, tamm_dancoff=0)
+    e = np.sqrt(a * a - abs(b) ** 2)
+    assert np.abs(r["E"] - np.array([-e, e])).max() < 1e-12 * a
+    X = r["A"]
+    jn = np.einsum("il,i,il->l", X.conj(), np.array([1.0, -1.0]), X).real
+    assert np.allclose(jn, [-1, 1], atol=1e-12)
