@@ -29,6 +29,7 @@ class BseParams(C.Structure):
         ("w_kind", C.c_int32), ("inv_eps", C.c_double), ("rk_r0", C.c_double), ("rk_eps", C.c_double),
         ("spin_factor", C.c_double),
         ("precision", C.c_int32), ("eig_solver", C.c_int32), ("n_refine", C.c_int32),
+        ("rpa_eta", C.c_double), ("rpa_order", C.c_int32), ("rpa_points", C.c_int32), ("rpa_seed", C.c_uint64),
     ]
 
 
@@ -67,7 +68,8 @@ class Marshalled:
             coulomb_radius=p.coulomb_radius, coulomb_min_k2=p.coulomb_min_k2,
             w_kind=p.w_kind, inv_eps=p.inv_eps, rk_r0=p.rk_r0, rk_eps=p.rk_eps,
             spin_factor=p.spin_factor, precision=p.precision, eig_solver=p.eig_solver,
-            n_refine=p.n_refine)
+            n_refine=p.n_refine, rpa_eta=p.rpa_eta, rpa_order=p.rpa_order, rpa_points=p.rpa_points,
+            rpa_seed=p.rpa_seed)
         self.p = p
         S = m.n_spin - 1
         self.nk, self.nc, self.nv, self.ng = prob.nk, p.nc, p.nv, prob.ng

@@ -12,7 +12,7 @@ INV_EPS_EMPIRICAL = 0.086206897               # bse.version13.cpp:2697 (1/11.6, 
 
 # include/bse_gpu.h enums
 BSE_V_BARE_3D, BSE_V_BARE_2D = 0, 1
-BSE_W_EMPIRICAL, BSE_W_RYTOVA_KELDYSH, BSE_W_BARE = 0, 1, 2
+BSE_W_EMPIRICAL, BSE_W_RYTOVA_KELDYSH, BSE_W_BARE, BSE_W_RPA = 0, 1, 2, 3
 BSE_FP64, BSE_MIXED = 0, 1
 BSE_EIG_OWN, BSE_EIG_CUSOLVER = 0, 1
 

@@ -150,24 +150,32 @@ __global__ void __launch_bounds__(64) band_subset_kernel(
 }
 
 template <int NW>
-void launch_bands(bse_ctx* c) {
+void launch_bands(bse_ctx* c, const double* q, double* ec, double* ev, double2* cc, double2* cv) {
     const int threads = 64, blocks = (2 * c->nk + threads - 1) / threads;
     band_subset_kernel<NW><<<blocks, threads, 0, c->stream>>>(
         c->nk, c->nw, c->ns, c->nr, c->nv, c->nc, c->d_rcart, c->d_weights, c->d_hr, c->d_k,
-        c->p.q[0], c->p.q[1], c->p.q[2], c->p.fermi_energy, c->p.scissor,
-        c->d_ec, c->d_ev, c->d_cc, c->d_cv, c->d_status);
+        q[0], q[1], q[2], c->p.fermi_energy, c->p.scissor, ec, ev, cc, cv, c->d_status);
     c->launches++;
 }
 
+void launch_bands_any(bse_ctx* c, const double* q, double* ec, double* ev, double2* cc, double2* cv) {
+    if (c->nw <= 4) launch_bands<4>(c, q, ec, ev, cc, cv);
+    else if (c->nw <= 8) launch_bands<8>(c, q, ec, ev, cc, cv);
+    else launch_bands<16>(c, q, ec, ev, cc, cv);
+}
+
 }  // namespace
+
+int band_states_shifted(bse_ctx* c, const double* q, double* ec, double* ev, double2* cc, double2* cv) {
+    launch_bands_any(c, q, ec, ev, cc, cv);
+    return cuda_check(c, cudaGetLastError(), "band kernel launch");
+}
 
 int run_bands(bse_ctx* c) {
     stage_begin(c, 0);
     int st;
     if ((st = cuda_check(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream), "status reset"))) return st;
-    if (c->nw <= 4) launch_bands<4>(c);
-    else if (c->nw <= 8) launch_bands<8>(c);
-    else launch_bands<16>(c);
+    launch_bands_any(c, c->p.q, c->d_ec, c->d_ev, c->d_cc, c->d_cv);
     if ((st = cuda_check(c, cudaGetLastError(), "band kernel launch"))) return st;
     stage_end(c, 0);
     int h_status = 0;

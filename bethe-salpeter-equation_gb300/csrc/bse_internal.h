@@ -43,6 +43,8 @@ struct DeltaMap {
     double step[3] = {0, 0, 0};    // spacing per axis (crystal units)
     int64_t n_delta = 0;           // (2m0-1)(2m1-1)(2m2-1) or nk*nk
     std::vector<int32_t> idx;      // per k: packed integer grid coordinates (on_grid)
+    bool periodic = false;         // on_grid, every grid point present once, step * m = 1 on each axis
+    std::vector<int32_t> inv;      // periodic: k index of grid coordinates (i0 * m1 + i1) * m2 + i2
 };
 
 }  // namespace bse
@@ -56,6 +58,7 @@ struct bse_ctx {
     bse::Geometry geo;
     bse::Interaction itx;
     bse::DeltaMap dmap;
+    double bmat_h[9] = {};       // reciprocal vectors b1 b2 b3 as columns (host copy of d_bmat)
     int device;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;           // concurrent work of the own solver (joined before use)
@@ -91,6 +94,7 @@ struct bse_ctx {
 
     // kernel tables
     double2* d_phi = nullptr;    // [n_delta][nblk][nw][nw] direct-kernel lattice sums (FP64)
+    double2* d_phi_c = nullptr;  // RPA + full BSE: the coupling block's sums, with conj(W) (FP64)
     float2* d_phi32 = nullptr;   // the same in FP32 for the mixed build
     double2* d_X = nullptr;      // [ns][ns][nw][nw] exchange lattice sums
     double2* d_qx = nullptr;     // [ns][ns][nw][n_rho/ns] exchange row factors  Qx[s1][s2][beta][r]
@@ -131,6 +135,11 @@ void stage_end(bse_ctx* c, int s);
 
 // --- stages (each returns a bse_status) ---
 int run_bands(bse_ctx* c);
+// band subset with conduction states at k and valence states at k - q into the given buffers
+// (layouts of d_ec, d_ev, d_cc, d_cv); errors land in d_status as for run_bands (bands.cu)
+int band_states_shifted(bse_ctx* c, const double* q, double* ec, double* ev, double2* cc, double2* cv);
+// RPA screened interaction: the direct-kernel tables Phi (and Phi32) from W = eps^-1 v (kernel_build.cu)
+int run_rpa_tables(bse_ctx* c);
 int run_tables(bse_ctx* c);
 int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out);
 int run_eig(bse_ctx* c, bool want_vectors);

@@ -122,6 +122,22 @@ void analyse_k(bse_ctx* c, const bse_model* m) {
             d.idx[k] = packed;
         }
         d.on_grid = true;
+        // a complete periodic grid: k - dk and k + dk are grid points for every grid offset dk
+        const int64_t ncell = (int64_t)d.m[0] * d.m[1] * d.m[2];
+        bool per = ncell == nk;
+        for (int i = 0; i < 3 && per; i++)
+            if (d.m[i] > 1 && std::fabs(d.step[i] * d.m[i] - 1.0) > 1e-9) per = false;
+        if (per) {
+            d.inv.assign(ncell, -1);
+            for (int k = 0; k < nk && per; k++) {
+                const int32_t x = d.idx[k];
+                const int64_t cell = ((int64_t)(x & 1023) * d.m[1] + ((x >> 10) & 1023)) * d.m[2] + ((x >> 20) & 1023);
+                if (d.inv[cell] >= 0) per = false;
+                else d.inv[cell] = k;
+            }
+        }
+        d.periodic = per;
+        if (!per) d.inv.clear();
         d.n_delta = (int64_t)(2 * d.m[0] - 1) * (2 * d.m[1] - 1) * (2 * d.m[2] - 1);
     } else {
         d.on_grid = false;
@@ -160,13 +176,18 @@ int validate(const bse_model* m, const bse_params* p) {
     if (p->nv > 8 || p->nc > 8) return fail(nullptr, BSE_ERR_BAD_INPUT, "nv, nc above 8 are not supported");
     if (p->tamm_dancoff != 0 && p->tamm_dancoff != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "tamm_dancoff must be 0 or 1");
     if (p->precision != BSE_FP64 && p->precision != BSE_MIXED) return fail(nullptr, BSE_ERR_BAD_INPUT, "precision");
-    if (p->tamm_dancoff == 0 && !p->ipa) {
-        if (p->precision != BSE_FP64)
-            return fail(nullptr, BSE_ERR_BAD_INPUT, "the full BSE (tamm_dancoff = 0) runs in FP64: set precision = BSE_FP64");
+    if (p->tamm_dancoff == 0 && !p->ipa && p->precision == BSE_MIXED) {
+        if (p->eig_solver != BSE_EIG_OWN)
+            return fail(nullptr, BSE_ERR_BAD_INPUT, "the mixed full BSE (tamm_dancoff = 0) uses the own eigensolver");
     }
     if (p->eig_solver != BSE_EIG_OWN && p->eig_solver != BSE_EIG_CUSOLVER) return fail(nullptr, BSE_ERR_BAD_INPUT, "eig_solver");
     if (p->coulomb_kind != BSE_V_BARE_3D && p->coulomb_kind != BSE_V_BARE_2D) return fail(nullptr, BSE_ERR_BAD_INPUT, "coulomb_kind");
-    if (p->w_kind < BSE_W_EMPIRICAL || p->w_kind > BSE_W_BARE) return fail(nullptr, BSE_ERR_BAD_INPUT, "w_kind");
+    if (p->w_kind < BSE_W_EMPIRICAL || p->w_kind > BSE_W_RPA) return fail(nullptr, BSE_ERR_BAD_INPUT, "w_kind");
+    if (p->w_kind == BSE_W_RPA && !p->ipa) {
+        if (p->rpa_order != 0 && p->rpa_order != 1) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_order must be 0 or 1");
+        if (p->rpa_points < 2 || p->rpa_points % 2) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_points must be even and >= 2");
+        if (!(p->rpa_eta >= 0.0) || !std::isfinite(p->rpa_eta)) return fail(nullptr, BSE_ERR_BAD_INPUT, "rpa_eta must be >= 0");
+    }
     const size_t nw = m->nw, nr = m->n_r, ns = m->n_spin;
     if (!finite_all(m->r_cart, 3 * nr) || !finite_all(m->weights, nr) || !finite_all(m->h_r, 2 * nw * nw * nr * ns) ||
         !finite_all(m->centres, 3 * nw * ns) || !finite_all(m->lattice, 9) || !finite_all(m->k_cart, 3 * (size_t)m->n_k) ||
@@ -207,7 +228,7 @@ void destroy_ctx(bse_ctx* c) {
     if (c->side) cudaStreamSynchronize(c->side);
     if (c->side2) cudaStreamSynchronize(c->side2);
     void* ptrs[] = {c->d_rcart, c->d_weights, c->d_hr, c->d_centres, c->d_k, c->d_bmat, c->d_kidx, c->d_g, c->d_status,
-                    c->d_ec, c->d_ev, c->d_cc, c->d_cv, c->d_phi, c->d_phi32, c->d_X, c->d_qx, c->d_qx32, c->d_rho,
+                    c->d_ec, c->d_ev, c->d_cc, c->d_cv, c->d_phi, c->d_phi_c, c->d_phi32, c->d_X, c->d_qx, c->d_qx32, c->d_rho,
                     c->d_H, c->d_H64, c->d_blk, c->d_aux, c->d_E, c->d_f, c->d_work};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -310,6 +331,10 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     it.nx = c->geo.normal[0]; it.ny = c->geo.normal[1]; it.nz = c->geo.normal[2]; it.lz = c->geo.lz;
     it.cell_avg = cell_average(c);
     analyse_k(c, m);
+    if (p->w_kind == BSE_W_RPA && !p->ipa && !c->dmap.periodic) {
+        destroy_ctx(c);
+        return fail(nullptr, BSE_ERR_BAD_INPUT, "RPA screening needs a complete periodic k grid (k - dk on the grid)");
+    }
     const int NWs = c->nw <= 2 ? 2 : c->nw <= 4 ? 4 : c->nw <= 8 ? 8 : 16;
     const int nblk = 3 * c->S + 1;
     if (!c->dmap.on_grid && (double)c->dmap.n_delta * nblk * NWs * NWs * 24.0 > 16e9) {
@@ -355,12 +380,13 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     CK(dmalloc(c, &c->d_qx, (size_t)c->N * nw * ns * ns * 16, "Qx"));
     const size_t nphi = (size_t)c->dmap.n_delta * nblk * NWs * NWs;
     CK(dmalloc(c, &c->d_phi, nphi * 16, "Phi"));
+    if (c->coupled && p->w_kind == BSE_W_RPA) CK(dmalloc(c, &c->d_phi_c, nphi * 16, "Phi (coupling)"));
     const bool mixed = p->precision == BSE_MIXED;
     if (mixed) {
         CK(dmalloc(c, &c->d_phi32, nphi * 8, "Phi32"));
         CK(dmalloc(c, &c->d_qx32, (size_t)c->N * nw * ns * ns * 8, "Qx32"));
     }
-    c->h_elem = mixed ? 8 : 16;
+    c->h_elem = mixed && !c->coupled ? 8 : 16;   // the full BSE is built in FP64 in both precisions
     CK(dmalloc(c, &c->d_H, (size_t)c->n_h * c->n_h * c->h_elem, "H"));
     if (c->coupled) {
         // spinless: L^H J L (2N); collinear: the two 4N blocks M0, M1 and L^H J L (4N)
@@ -370,7 +396,7 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     } else if (c->S) {
         CK(dmalloc(c, &c->d_blk, 2 * (size_t)(2 * c->N) * (2 * c->N) * c->h_elem, "spin blocks"));
     }
-    if (mixed && !p->ipa && p->n_refine > 0) {
+    if (mixed && !c->coupled && !p->ipa && p->n_refine > 0) {
         const size_t n64 = c->S ? 4 * c->N : c->N;
         CK(dmalloc(c, &c->d_H64, n64 * n64 * 16, "H64"));
     }
@@ -396,6 +422,7 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
         for (int i = 0; i < 3; i++)
             for (int j = 0; j < 3; j++) b[3 * i + j] = x[i][j] * 2.0 * kPi / c->geo.vol;
         CK(upload(c, c->d_bmat, b, 72, "b"));
+        std::memcpy(c->bmat_h, b, sizeof(b));
     }
     if (c->dmap.on_grid) CK(upload(c, c->d_kidx, c->dmap.idx.data(), nk * 4, "k index"));
     CK(cuda_check(c, cudaStreamSynchronize(c->stream), "uploads"));

@@ -752,8 +752,280 @@ int solve_coupled_block(bse_ctx* c, int64_t n, double2* M, double2* W, const dou
     return cuda_check(c, cudaGetLastError(), "coupled eigenvectors");
 }
 
+namespace {
+
+// T = -L^{-1} J (Li = L^{-1} lower, FP32): strict upper triangle cleared, columns j < N negated
+__global__ void neg_jl32_kernel(int64_t n, int64_t N, const float2* __restrict__ Li, float2* __restrict__ T) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    const int64_t i = t % n, j = t / n;
+    float2 l = i >= j ? Li[t] : make_float2(0.f, 0.f);
+    if (j < N) l = make_float2(-l.x, -l.y);
+    T[t] = l;
+}
+
+__global__ void hermitian_part32_kernel(int64_t n, float2* __restrict__ W) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    const int64_t i = t % n, j = t / n;
+    if (i < j) return;
+    if (i == j) {
+        W[t].y = 0.f;
+        return;
+    }
+    const float2 a = W[t], b = W[j + n * i];
+    const float2 m = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+    W[t] = m;
+    W[j + n * i] = make_float2(m.x, -m.y);
+}
+
+// y = Li x (Li lower triangular, FP32; x, y FP64): one warp per row
+__global__ void trmv_lower32_kernel(int64_t n, const float2* __restrict__ Li, const double2* __restrict__ x,
+                                    double2* __restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    double re = 0, im = 0;
+    for (int64_t j = lane; j <= i; j += 32) {
+        const float2 l = Li[i + n * j];
+        const double2 v = x[j];
+        re += (double)l.x * v.x - (double)l.y * v.y;
+        im += (double)l.x * v.y + (double)l.y * v.x;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) y[i] = make_double2(re, im);
+}
+
+// mu ascending (eigenvalues of -L^{-1} J L^{-H}, mu = -1/lambda) -> lambda ascending with the
+// J-normalised oscillators: negative mu (the first npos) are the positive lambda, in ascending order
+__global__ void mu_to_lambda_kernel(int64_t n, int64_t npos, const double* __restrict__ mu, const double2* __restrict__ fmu,
+                                    double* __restrict__ E, double2* __restrict__ f) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double lam = -1.0 / mu[t];
+    const int64_t o = t < npos ? (n - npos) + t : t - npos;
+    E[o] = lam;
+    if (f) {
+        const double s = sqrt(fabs(lam));
+        f[o] = make_double2(fmu[t].x * s, fmu[t].y * s);
+    }
+}
+
+// S = Pbot - Ptop = -X^H J X (m x m)
+__global__ void sub_m_kernel(int64_t mm, const double2* __restrict__ Pt, const double2* __restrict__ Pb, double2* __restrict__ S) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < mm) S[t] = make_double2(Pb[t].x - Pt[t].x, Pb[t].y - Pt[t].y);
+}
+
+// refined pair j: E_j = -1/theta_j, x_j = E_j^{1/2} XZ_j (J-normalised), f_j = rho^H x_j,
+// residual ||M x - E J x|| / E^{1/2} = ||MXZ_j - E_j J XZ_j||; one block per column
+__global__ void coupled_refined_kernel(int64_t n, int64_t N, const double* __restrict__ theta, const double2* __restrict__ XZ,
+                                       const double2* __restrict__ MXZ, const double2* __restrict__ rho,
+                                       double* __restrict__ E, double2* __restrict__ f, double* __restrict__ res) {
+    __shared__ double red[3][32];
+    const int j = blockIdx.x;
+    const double lam = -1.0 / theta[j];
+    const double2* x = XZ + (int64_t)j * n;
+    const double2* mx = MXZ + (int64_t)j * n;
+    double r2 = 0, fr = 0, fi = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double sg = i < N ? lam : -lam;
+        const double dx = mx[i].x - sg * x[i].x, dy = mx[i].y - sg * x[i].y;
+        r2 += dx * dx + dy * dy;
+        fr += rho[i].x * x[i].x + rho[i].y * x[i].y;     // conj(rho) x
+        fi += rho[i].x * x[i].y - rho[i].y * x[i].x;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+        fr += __shfl_xor_sync(0xffffffffu, fr, o);
+        fi += __shfl_xor_sync(0xffffffffu, fi, o);
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { red[0][w] = r2; red[1][w] = fr; red[2][w] = fi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); k++) { r2 += red[0][k]; fr += red[1][k]; fi += red[2][k]; }
+        const double s = sqrt(fabs(lam));
+        E[j] = lam;
+        f[j] = make_double2(fr * s, fi * s);
+        res[j] = sqrt(r2);
+    }
+}
+
+}  // namespace
+
+// Mixed full BSE (spinless, tamm_dancoff = 0, BSE_MIXED): the FP64 M of the build, its FP32 Cholesky
+// factor L and inverse, the Hermitian K = -L^{-1} J L^{-H} whose eigenvalues are mu = -1/lambda (the
+// smallest positive excitation energies are the lowest mu), the own FP32 eigensolver on K (all values,
+// f from (L^{-1} rho)^H y, the lowest n_refine + guard vectors), then an FP64 Rayleigh-Ritz step on the
+// definite pencil J x = (1/E) M x in the span of x = L^{-H} y: (S, G) = (-X^H J X, X^H M X), products
+// in compensated FP32, eigenpairs by the Ogita-Aishima refinement (dense fallback).
+// One n x n block: M64 the FP64 M (consumed), L / K two n x n FP32 workspaces, E the n eigenvalues,
+// rho0 / f the optical vector and oscillators (null for a values-only block, which is not refined).
+int mixed_coupled_block(bse_ctx* c, int64_t n, double2* M64, float2* L, float2* K, const double2* rho0, double* E,
+                        double2* f) {
+    int st;
+    const int64_t N = n / 2;
+    cublasSetStream(c->cublas, c->stream);
+    cusolverDnSetStream(c->cusolver, c->stream);
+    narrow_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, c->stream>>>(n * n, M64, L);
+    c->launches++;
+    {
+        cusolverDnParams_t prm;
+        if ((st = cusolver_check(c, cusolverDnCreateParams(&prm), "params"))) return st;
+        size_t dws1 = 0, hws1 = 0, dws2 = 0, hws2 = 0;
+        st = cusolver_check(c, cusolverDnXpotrf_bufferSize(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_32F, L, n,
+                                                           CUDA_C_32F, &dws1, &hws1), "potrf size");
+        if (!st) st = cusolver_check(c, cusolverDnXtrtri_bufferSize(c->cusolver, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n,
+                                                                    CUDA_C_32F, L, n, &dws2, &hws2), "trtri size");
+        if (!st) st = ensure_work(c, std::max(dws1, dws2) + 256);
+        if (st) { cusolverDnDestroyParams(prm); return st; }
+        int* dinfo = (int*)c->d_work;
+        std::vector<char> hbuf(std::max<size_t>(std::max(hws1, hws2), 1));
+        st = cusolver_check(c, cusolverDnXpotrf(c->cusolver, prm, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_32F, L, n, CUDA_C_32F,
+                                                (char*)c->d_work + 256, dws1, hbuf.data(), hws1, dinfo), "potrf");
+        cusolverDnDestroyParams(prm);
+        if (st) return st;
+        int info = 0;
+        if ((st = cuda_check(c, cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "potrf info"))) return st;
+        if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "potrf sync"))) return st;
+        if (info != 0)
+            return fail(c, BSE_ERR_BAD_INPUT, "full BSE: [[A, B], [B*, A*]] is not positive definite (FP32 leading minor " +
+                                                  std::to_string(info) + "); the structure-preserving solve needs a stable ground state");
+        if ((st = cusolver_check(c, cusolverDnXtrtri(c->cusolver, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, CUDA_C_32F, L, n,
+                                                     (char*)c->d_work + 256, dws2, hbuf.data(), hws2, dinfo), "trtri"))) return st;
+    }
+    const unsigned gb = (unsigned)((n * n + 255) / 256);
+    neg_jl32_kernel<<<gb, 256, 0, c->stream>>>(n, N, L, K);   // K = -Li J (L now holds Li, lower)
+    c->launches++;
+    const cuComplex one = make_cuComplex(1.f, 0.f);
+    if ((st = cublas_check(c, cublasCtrmm(c->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
+                                          n, n, &one, (const cuComplex*)L, n, (const cuComplex*)K, n, (cuComplex*)K, n),
+                           "-Li J Li^H"))) return st;
+    hermitian_part32_kernel<<<gb, 256, 0, c->stream>>>(n, K);
+    c->launches++;
+    if (rho0) {
+        trmv_lower32_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(n, L, rho0, c->d_aux);   // L^{-1} rho
+        c->launches++;
+    }
+    if ((st = cuda_check(c, cudaGetLastError(), "mixed coupled setup"))) return st;
+    const int64_t m = (rho0 && c->p.n_refine > 0) ? std::min<int64_t>(N, (int64_t)c->p.n_refine + kGuard) : 0;
+    const int64_t nref = std::min<int64_t>(N, std::max(c->p.n_refine, 0));
+    // mu into the upper half of d_E's storage is not possible (n doubles needed): use the arena top
+    double* mu = nullptr;
+    double2* fmu = nullptr;
+    if ((st = cuda_check(c, cudaMallocAsync((void**)&mu, n * sizeof(double), c->stream), "mu"))) return st;
+    if (rho0 && (st = cuda_check(c, cudaMallocAsync((void**)&fmu, n * sizeof(double2), c->stream), "f(mu)"))) return st;
+    st = own_heevd(c, (int)n, K, (int)n, false, mu, (int)m, rho0 ? c->d_aux : nullptr, fmu);
+    if (!st) {
+        // count the negative mu (= positive lambda) on the host
+        std::vector<double> hmu(n);
+        st = cuda_check(c, cudaMemcpyAsync(hmu.data(), mu, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "mu copy");
+        if (!st) st = cuda_check(c, cudaStreamSynchronize(c->stream), "mu sync");
+        int64_t npos = 0;
+        for (double v : hmu) npos += v < 0.0;
+        if (!st && npos < m) st = fail(c, BSE_ERR_NOT_CONVERGED, "full BSE: fewer positive excitations than refined pairs");
+        if (!st) {
+            mu_to_lambda_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, npos, mu, fmu, E, f);
+            c->launches++;
+            st = cuda_check(c, cudaGetLastError(), "mu -> lambda");
+        }
+    }
+    cudaFreeAsync(mu, c->stream);
+    if (fmu) cudaFreeAsync(fmu, c->stream);
+    if (st) return st;
+    if (m == 0) return BSE_OK;
+    // X = L^{-H} Y for the m lowest mu (the m smallest positive excitation energies)
+    if ((st = cublas_check(c, cublasCtrmm(c->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT,
+                                          n, m, &one, (const cuComplex*)L, n, (const cuComplex*)K, n, (cuComplex*)K, n),
+                           "Li^H Y"))) return st;
+    // FP64 Rayleigh-Ritz on the pencil (-J, M) in span(X)
+    stage_begin(c, 4);
+    size_t off = 0;
+    auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    const size_t oX = carve(n * m * sizeof(double2)), oY = carve(n * m * sizeof(double2));
+    const size_t oXs = carve(n * m * sizeof(float4)), oYs = carve(n * m * sizeof(float4));
+    const size_t oS = carve(m * m * sizeof(double2)), oG = carve(m * m * sizeof(double2));
+    const size_t oPt = carve(m * m * sizeof(double2)), oPb = carve(m * m * sizeof(double2));
+    const size_t oZb = carve(m * m * sizeof(double2)), oT = carve(m * sizeof(double)), oR = carve(m * sizeof(double));
+    const size_t oOA = carve(oa_workspace(m)), oP = carve((size_t)kMaxSplits * m * m * sizeof(double2));
+    if ((st = ensure_work(c, off))) return st;
+    char* base = (char*)c->d_work;
+    double2* X = (double2*)(base + oX);
+    double2* Y = (double2*)(base + oY);
+    float4* X4 = (float4*)(base + oXs);
+    float4* Y4 = (float4*)(base + oYs);
+    double2* S = (double2*)(base + oS);
+    double2* G = (double2*)(base + oG);
+    double2* Pt = (double2*)(base + oPt);
+    double2* Pb = (double2*)(base + oPb);
+    double2* Zb = (double2*)(base + oZb);
+    double* theta = (double*)(base + oT);
+    double* rn = (double*)(base + oR);
+    double2* Pw = (double2*)(base + oP);
+    const int64_t pcap = (int64_t)kMaxSplits * m * m;
+    widen_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, c->stream>>>(n * m, K, X);
+    float4* M4 = reinterpret_cast<float4*>(M64);   // the FP64 M is split in place (the solve consumes it)
+    split_df_kernel<<<(unsigned)((n * n + 255) / 256), 256, 0, c->stream>>>(n * n, M64, M4);
+    split_df_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, c->stream>>>(n * m, X, X4);
+    c->launches += 3;
+    hemm_df_kernel<<<dim3((unsigned)((n + HM_TM - 1) / HM_TM), (unsigned)((m + HM_TN - 1) / HM_TN)), 256, 0, c->stream>>>(
+        (int)n, (int)m, M4, X4, Y);                                                                            // M X
+    split_df_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, c->stream>>>(n * m, Y, Y4);
+    c->launches += 2;
+    if ((st = gemm_df(c, true, (int)m, (int)m, (int)n, (const float4*)X4, n, (const float4*)Y4, n, G, m, Pw, pcap))) return st;    // X^H M X
+    if ((st = gemm_df(c, true, (int)m, (int)m, (int)N, (const float4*)X4, n, (const float4*)X4, n, Pt, m, Pw, pcap))) return st;   // top rows
+    if ((st = gemm_df(c, true, (int)m, (int)m, (int)N, (const float4*)(X4 + N), n, (const float4*)(X4 + N), n, Pb, m, Pw, pcap))) return st;
+    sub_m_kernel<<<(unsigned)((m * m + 255) / 256), 256, 0, c->stream>>>(m * m, Pt, Pb, S);                    // -X^H J X
+    c->launches++;
+    bool refined = false;
+    if ((st = oa_refine(c, (int)m, S, G, Zb, theta, Pw, pcap, base + oOA, &refined))) return st;
+    if (!refined) return fail(c, BSE_ERR_NOT_CONVERGED, "full BSE: the pencil refinement did not converge");
+    // refined vectors XZ (M-normalised) and M XZ; then E, J-normalised f and residuals of the lowest nref
+    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, (const float4*)X4, n, (const double2*)Zb, m, X, n, Pw, pcap))) return st;  // X Z
+    if ((st = gemm_df(c, false, (int)n, (int)m, (int)m, (const float4*)Y4, n, (const double2*)Zb, m, Y, n, Pw, pcap))) return st;  // M X Z
+    coupled_refined_kernel<<<(unsigned)nref, 256, 0, c->stream>>>(n, N, theta, X, Y, rho0, E + N, f + N, rn);
+    c->launches++;
+    std::vector<double> hrn(nref);
+    if ((st = cuda_check(c, cudaMemcpyAsync(hrn.data(), rn, nref * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "residuals"))) return st;
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "residuals"))) return st;
+    c->max_residual = 0;
+    for (double v : hrn) c->max_residual = std::max(c->max_residual, v);
+    c->n_refined = nref;
+    stage_end(c, 4);
+    return cuda_check(c, cudaGetLastError(), "mixed coupled refinement");
+}
+
+int run_eig_coupled_mixed(bse_ctx* c) {
+    int st;
+    const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
+    c->f_from_eig = true;
+    c->n_vec_valid = 0;
+    c->n_refined = 0;
+    if (c->S == 0) {
+        const int64_t n = c->n_h;
+        float2* L = (float2*)c->d_blk;
+        return mixed_coupled_block(c, n, (double2*)c->d_H, L, L + n * n, rho0, c->d_E, c->d_f);
+    }
+    // collinear: M0 (values only) and the optically active M1, each 4N; L and K in the third slot
+    const int64_t n4 = c->n_opt;
+    double2* M0 = (double2*)c->d_blk;
+    double2* M1 = M0 + n4 * n4;
+    float2* L = (float2*)(M1 + n4 * n4);
+    if ((st = mixed_coupled_block(c, n4, M0, L, L + n4 * n4, nullptr, c->d_E, nullptr))) return st;
+    return mixed_coupled_block(c, n4, M1, L, L + n4 * n4, rho0, c->d_E + n4, c->d_f);
+}
+
 int run_eig_coupled(bse_ctx* c, bool want_vectors) {
     int st;
+    if (c->p.precision == BSE_MIXED) {
+        if (want_vectors)
+            return fail(c, BSE_ERR_STATE, "the mixed full BSE forms no eigenvectors: use precision = BSE_FP64 for a_out");
+        return run_eig_coupled_mixed(c);
+    }
     const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
     if (c->S == 0) {
         double2* W = (double2*)c->d_blk;

@@ -21,7 +21,10 @@
 // (2n-1)^d of them); the build kernel then writes each element of H exactly once, k1
 // fastest so that a warp stores 32 consecutive elements of one column: the kernel is
 // bound by the N^2 store of H, not by arithmetic (inner dimension nw <= 16).
+#include <cmath>
 #include <mutex>
+#include <random>
+#include <vector>
 
 #include "bse_internal.h"
 
@@ -490,6 +493,159 @@ __global__ void gather_coupled_blocks_kernel(int64_t N, const double2* __restric
     M1[t] = M[map1(i) + ld * map1(j)];
 }
 
+// ---- RPA screened interaction (pull_coulomb_potentials 2597-2690, Dielectric_Function::pull_values
+// 2214-2315).  Per momentum q (a grid Delta k, or a point of the dk = 0 sphere):
+//   rho1_r(G) = sum_a conj(c_ca(k)) e^{i(G+q).tau_a} c_va(k - q),   E1 = E_c(k) - E_v(k - q)
+//   rho2_r(G) = sum_a conj(c_ca(k)) e^{-i(G+q).tau_a} c_va(k + q),  E2 = E_c(k) - E_v(k + q)
+//   chi0 = 1/(V nk) [rho1^H diag(m1) rho1 + conj(rho2^H diag(conj m2) rho2)],
+//   m1 = 1/(-E1 + i eta), m2 = -1/(E2 - i eta)  (omega = 0; the -q densities of the anti-resonant term)
+//   eps^-1 = 1 + diag(v) chi0 (order 0) or 1 + diag(v) (1 - chi0 diag(v))^-1 chi0, v_G = v(q + G)
+//   W_GG' = eps^-1_GG' v(q + G'),  Phi_ab = sum_GG' e^{-i(G+q).tau^c_a} W_GG' e^{i(G'+q).tau^v_b}
+// r = ((s nc + c) nv + v) nk + k; the rho arrays are column-major R x ng per momentum.
+__global__ void rpa_rho_kernel(int D, int64_t R, int ng, int nk, int nc, int nv, int nw, int ns,
+                               const double* __restrict__ qs, const int* __restrict__ map_m,
+                               const int* __restrict__ map_p, const double* __restrict__ gcart,
+                               const double* __restrict__ centres, const double2* __restrict__ cc,
+                               const double* __restrict__ ec, const double2* __restrict__ cvm,
+                               const double* __restrict__ evm, const double2* __restrict__ cvp,
+                               const double* __restrict__ evp, double eta, double2* __restrict__ rho1,
+                               double2* __restrict__ q1, double2* __restrict__ rho2, double2* __restrict__ q2) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t per = R * ng;
+    if (t >= per * D) return;
+    const int d = (int)(t / per);
+    const int64_t rem = t % per;
+    const int g = (int)(rem / R);
+    const int64_t r = rem % R;
+    const int k = (int)(r % nk), v = (int)((r / nk) % nv);
+    const int c = (int)((r / ((int64_t)nk * nv)) % nc), s = (int)(r / ((int64_t)nk * nv * nc));
+    const int km = map_m ? map_m[(size_t)d * nk + k] : k, kp = map_p ? map_p[(size_t)d * nk + k] : k;
+    const int nb = nw * ns;
+    const double* q = qs + 3 * d;
+    const double* G = gcart + 3 * g;
+    double2 a1 = make_double2(0, 0), a2 = make_double2(0, 0);
+    for (int a = 0; a < nw; a++) {
+        const double* ta = centres + 3 * ((size_t)s * nw + a);
+        const double ph = ta[0] * (G[0] + q[0]) + ta[1] * (G[1] + q[1]) + ta[2] * (G[2] + q[2]);
+        double sn, cs;
+        sincos(ph, &sn, &cs);
+        const double2 cca = cconj(cc[((size_t)k * nc + c) * nb + s * nw + a]);
+        const double2 x1 = cmul(cmul(cca, make_double2(cs, sn)), cvm[((size_t)km * nv + v) * nb + s * nw + a]);
+        const double2 x2 = cmul(cmul(cca, make_double2(cs, -sn)), cvp[((size_t)kp * nv + v) * nb + s * nw + a]);
+        a1.x += x1.x; a1.y += x1.y;
+        a2.x += x2.x; a2.y += x2.y;
+    }
+    const double E1 = ec[((size_t)s * nk + k) * nc + c] - evm[((size_t)s * nk + km) * nv + v];
+    const double E2 = ec[((size_t)s * nk + k) * nc + c] - evp[((size_t)s * nk + kp) * nv + v];
+    const double d1 = E1 * E1 + eta * eta, d2 = E2 * E2 + eta * eta;
+    const double2 m1 = make_double2(-E1 / d1, -eta / d1);    // 1/(-E1 + i eta)
+    const double2 m2c = make_double2(-E2 / d2, eta / d2);    // conj(-1/(E2 - i eta))
+    const int64_t o = (int64_t)d * per + (int64_t)g * R + r;
+    rho1[o] = a1;
+    q1[o] = cmul(m1, a1);
+    rho2[o] = a2;
+    q2[o] = cmul(m2c, a2);
+}
+
+// chi0 = fchi (C1 + conj(C2)) into chi0; order 0: einv = 1 + diag(v) chi0; order 1: A = 1 - chi0 diag(v)
+__global__ void rpa_chi0_kernel(int D, int ng, double fchi, const double* __restrict__ qs, const double* __restrict__ gcart,
+                                Interaction it, int order, const double2* __restrict__ C1, const double2* __restrict__ C2,
+                                double2* __restrict__ chi0, double2* __restrict__ A, double2* __restrict__ einv) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t gg = (int64_t)ng * ng;
+    if (t >= gg * D) return;
+    const int d = (int)(t / gg);
+    const int i = (int)((t % gg) % ng), j = (int)((t % gg) / ng);
+    const double* q = qs + 3 * d;
+    const double2 chi = make_double2(fchi * (C1[t].x + C2[t].x), fchi * (C1[t].y - C2[t].y));
+    chi0[t] = chi;
+    const double* Gi = gcart + 3 * i;
+    const double* Gj = gcart + 3 * j;
+    if (order == 0) {
+        const double vi = dev_coulomb(it, q[0] + Gi[0], q[1] + Gi[1], q[2] + Gi[2]);
+        einv[t] = make_double2((i == j ? 1.0 : 0.0) + vi * chi.x, vi * chi.y);
+    } else {
+        const double vj = dev_coulomb(it, q[0] + Gj[0], q[1] + Gj[1], q[2] + Gj[2]);
+        A[t] = make_double2((i == j ? 1.0 : 0.0) - chi.x * vj, -chi.y * vj);
+    }
+}
+
+// order 1: einv = 1 + diag(v) X with X = A^-1 chi0 from the batched solve
+__global__ void rpa_einv_kernel(int D, int ng, const double* __restrict__ qs, const double* __restrict__ gcart, Interaction it,
+                                const double2* __restrict__ X, double2* __restrict__ einv) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t gg = (int64_t)ng * ng;
+    if (t >= gg * D) return;
+    const int d = (int)(t / gg);
+    const int i = (int)((t % gg) % ng), j = (int)((t % gg) / ng);
+    const double* q = qs + 3 * d;
+    const double* Gi = gcart + 3 * i;
+    const double vi = dev_coulomb(it, q[0] + Gi[0], q[1] + Gi[1], q[2] + Gi[2]);
+    einv[t] = make_double2((i == j ? 1.0 : 0.0) + vi * X[t].x, vi * X[t].y);
+}
+
+// W = einv v(q + G_col) for grid momenta; sphere points accumulate <W> with the head keeping <eps^-1_00>
+__global__ void rpa_w_kernel(int D, int ng, const double* __restrict__ qs, const double* __restrict__ gcart, Interaction it,
+                             const double2* __restrict__ einv, double2* __restrict__ W, int accumulate) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t gg = (int64_t)ng * ng;
+    if (t >= gg * D) return;
+    const int d = (int)(t / gg);
+    const int i = (int)((t % gg) % ng), j = (int)((t % gg) / ng);
+    const double* q = qs + 3 * d;
+    const double* Gj = gcart + 3 * j;
+    const int g0 = ng / 2;
+    const double vj = (accumulate && i == g0 && j == g0) ? 1.0 : dev_coulomb(it, q[0] + Gj[0], q[1] + Gj[1], q[2] + Gj[2]);
+    const double2 w = make_double2(einv[t].x * vj, einv[t].y * vj);
+    if (accumulate) {
+        const int64_t u = t % gg;
+        W[u].x += w.x;
+        W[u].y += w.y;
+    } else {
+        W[t] = w;
+    }
+}
+
+// Phi[dd][blk][a][b] = sum_GG' e^{-i(G+q).tau^{sc}_a} W_GG' e^{i(G'+q).tau^{sv}_b} for D table entries;
+// conj_w: the same sums with conj(W_GG'), the coupling block's table (for a real diagonal W the two agree)
+__global__ void rpa_phi_kernel(int D, const int64_t* __restrict__ didx, const double* __restrict__ qs, int nblk, int nw,
+                               int stride, int ng, const double* __restrict__ gcart, const double* __restrict__ centres,
+                               const double2* __restrict__ W, double2* __restrict__ phi, float2* __restrict__ phi32,
+                               int conj_w) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)D * nblk * nw * nw) return;
+    const int b = (int)(t % nw), a = (int)((t / nw) % nw);
+    const int blk = (int)((t / ((int64_t)nw * nw)) % nblk);
+    const int d = (int)(t / ((int64_t)nw * nw * nblk));
+    const double* q = qs + 3 * d;
+    const double* ta = centres + 3 * ((size_t)c_exc_spin[blk].c * nw + a);
+    const double* tb = centres + 3 * ((size_t)c_exc_spin[blk].v * nw + b);
+    const double2* w = W + (int64_t)d * ng * ng;
+    double re = 0, im = 0;
+    for (int j = 0; j < ng; j++) {
+        const double* Gj = gcart + 3 * j;
+        const double pj = (Gj[0] + q[0]) * tb[0] + (Gj[1] + q[1]) * tb[1] + (Gj[2] + q[2]) * tb[2];
+        double sj, cj;
+        sincos(pj, &sj, &cj);
+        double sr = 0, si = 0;   // sum_i e^{-i(G_i+q).tau_a} W_ij
+        for (int i = 0; i < ng; i++) {
+            const double* Gi = gcart + 3 * i;
+            const double pi_ = -((Gi[0] + q[0]) * ta[0] + (Gi[1] + q[1]) * ta[1] + (Gi[2] + q[2]) * ta[2]);
+            double si_, ci_;
+            sincos(pi_, &si_, &ci_);
+            double2 x = w[i + (int64_t)ng * j];
+            if (conj_w) x.y = -x.y;
+            sr += ci_ * x.x - si_ * x.y;
+            si += ci_ * x.y + si_ * x.x;
+        }
+        re += sr * cj - si * sj;
+        im += sr * sj + si * cj;
+    }
+    const size_t o = (((size_t)didx[d] * nblk + blk) * stride + a) * stride + b;
+    phi[o] = make_double2(re, im);
+    if (phi32) phi32[o] = make_float2((float)re, (float)im);
+}
+
 // Collinear spin rotation U H U (spin_transformation, bse.version13.cpp:3048-3117), in place per
 // (row, col) position across the 4x4 spin blocks, so no block reads an already rotated one (Q24).
 template <typename T2>
@@ -588,7 +744,8 @@ int launch_coupling_nw(bse_ctx* c, int br, int bc, int direct, int exch) {
         smem_err = cudaFuncSetAttribute(coupling_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * 16 * 32 * 16);
     });
     if (smem_err != cudaSuccess) return cuda_check(c, smem_err, "coupling smem attribute");
-    coupling_kernel<NW><<<grid, block, smem, c->stream>>>(a, c->d_phi, c->d_qx, (double2*)c->d_H);
+    // with an RPA W the coupling block pairs the states through conj(W) (its own table)
+    coupling_kernel<NW><<<grid, block, smem, c->stream>>>(a, c->d_phi_c ? c->d_phi_c : c->d_phi, c->d_qx, (double2*)c->d_H);
     c->launches++;
     return cuda_check(c, cudaGetLastError(), "coupling kernel launch");
 }
@@ -646,18 +803,229 @@ int run_tables(bse_ctx* c) {
         const int64_t total = c->dmap.n_delta * nblk * NWs * NWs;
         if ((st = cuda_check(c, cudaMemsetAsync(c->d_phi, 0, total * sizeof(double2), c->stream), "phi clear"))) return st;
         if (c->d_phi32 && (st = cuda_check(c, cudaMemsetAsync(c->d_phi32, 0, total * sizeof(float2), c->stream), "phi32 clear"))) return st;
-        const int64_t tk = c->dmap.n_delta * nblk * nw * nw;
-        phi_table_kernel<<<(unsigned)((tk + 255) / 256), 256, 0, c->stream>>>(
-            c->dmap.n_delta, nblk, nw, NWs, ng, c->itx, c->dmap.on_grid, c->dmap.m[0], c->dmap.m[1], c->dmap.m[2],
-            c->dmap.step[0], c->dmap.step[1], c->dmap.step[2], c->d_bmat, c->d_k, c->nk,
-            c->d_g, c->d_centres, c->d_phi, c->p.precision == BSE_MIXED ? c->d_phi32 : nullptr);
-        c->launches++;
-        if ((st = cuda_check(c, cudaGetLastError(), "phi kernel"))) return st;
+        if (c->d_phi_c && (st = cuda_check(c, cudaMemsetAsync(c->d_phi_c, 0, total * sizeof(double2), c->stream), "phi clear"))) return st;
+        if (c->p.w_kind == BSE_W_RPA) {
+            if ((st = run_rpa_tables(c))) return st;
+        } else {
+            const int64_t tk = c->dmap.n_delta * nblk * nw * nw;
+            phi_table_kernel<<<(unsigned)((tk + 255) / 256), 256, 0, c->stream>>>(
+                c->dmap.n_delta, nblk, nw, NWs, ng, c->itx, c->dmap.on_grid, c->dmap.m[0], c->dmap.m[1], c->dmap.m[2],
+                c->dmap.step[0], c->dmap.step[1], c->dmap.step[2], c->d_bmat, c->d_k, c->nk,
+                c->d_g, c->d_centres, c->d_phi, c->p.precision == BSE_MIXED ? c->d_phi32 : nullptr);
+            c->launches++;
+            if ((st = cuda_check(c, cudaGetLastError(), "phi kernel"))) return st;
+        }
     }
     stage_end(c, 1);
     if ((st = cuda_check(c, cudaGetLastError(), "tables"))) return st;
     c->tables_valid = true;
     return BSE_OK;
+}
+
+// RPA direct-kernel tables: W per grid Delta k (chunks of momenta: densities, two batched ZGEMMs for
+// chi0, batched LU for the Dyson form), the dk = 0 entry from the seeded sphere points.
+int run_rpa_tables(bse_ctx* c) {
+    int st;
+    const int nk = c->nk, ng = c->ng, nw = c->nw, ns = c->ns, nc = c->nc, nv = c->nv, nb = c->nb;
+    const int64_t R = (int64_t)ns * nk * nc * nv, gg = (int64_t)ng * ng;
+    const int nblk = 3 * c->S + 1, NWs = table_stride(nw), order = c->p.rpa_order;
+    const double eta = c->p.rpa_eta, fchi = 1.0 / (c->geo.vol * nk);
+    const DeltaMap& dm = c->dmap;
+    const int m0 = dm.m[0], m1 = dm.m[1], m2 = dm.m[2];
+    const int64_t nd = dm.n_delta;
+    const int64_t dcenter = (int64_t)(m0 - 1) + (int64_t)(2 * m0 - 1) * ((m1 - 1) + (int64_t)(2 * m1 - 1) * (m2 - 1));
+    // momenta per chunk: the densities dominate, 4 R ng complex per momentum
+    const int64_t per_d = 4 * R * ng * 16 + 6 * gg * 16 + 2 * (int64_t)nk * 4 + 64;
+    const int64_t D = std::max<int64_t>(1, std::min<int64_t>(nd, (int64_t)(2e9 / (double)per_d)));
+    // scratch: valence states at the grid k (and the sphere's k -+ q), conduction dummies, chunk arrays
+    char* buf = nullptr;
+    size_t off = 0;
+    auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    const size_t oE = carve(2 * (size_t)nk * nc * 8), oC = carve((size_t)nk * nc * nb * 16);
+    const size_t oEv0 = carve(2 * (size_t)nk * nv * 8), oCv0 = carve((size_t)nk * nv * nb * 16);
+    const size_t oEvm = carve(2 * (size_t)nk * nv * 8), oCvm = carve((size_t)nk * nv * nb * 16);
+    const size_t oEvp = carve(2 * (size_t)nk * nv * 8), oCvp = carve((size_t)nk * nv * nb * 16);
+    const size_t oR1 = carve(D * R * ng * 16), oQ1 = carve(D * R * ng * 16), oR2 = carve(D * R * ng * 16), oQ2 = carve(D * R * ng * 16);
+    const size_t oC1 = carve(D * gg * 16), oC2 = carve(D * gg * 16), oChi = carve(D * gg * 16), oA = carve(D * gg * 16);
+    const size_t oEi = carve(D * gg * 16), oW = carve(D * gg * 16), oAvg = carve(gg * 16);
+    const size_t oQs = carve(D * 3 * 8), oDi = carve(D * 8), oMm = carve(D * nk * 4), oMp = carve(D * nk * 4);
+    const size_t oPiv = carve(D * ng * 4), oInfo = carve(D * 4), oPa = carve(D * 8), oPb = carve(D * 8);
+    if ((st = cuda_check(c, cudaMallocAsync((void**)&buf, off, c->stream), "RPA workspace"))) return st;
+    double* ecs = (double*)(buf + oE);
+    double2* ccs = (double2*)(buf + oC);
+    double* ev0 = (double*)(buf + oEv0);
+    double2* cv0 = (double2*)(buf + oCv0);
+    double* evm = (double*)(buf + oEvm);
+    double2* cvm = (double2*)(buf + oCvm);
+    double* evp = (double*)(buf + oEvp);
+    double2* cvp = (double2*)(buf + oCvp);
+    double2 *r1 = (double2*)(buf + oR1), *q1 = (double2*)(buf + oQ1), *r2 = (double2*)(buf + oR2), *q2 = (double2*)(buf + oQ2);
+    double2 *C1 = (double2*)(buf + oC1), *C2 = (double2*)(buf + oC2), *chi = (double2*)(buf + oChi), *A = (double2*)(buf + oA);
+    double2 *einv = (double2*)(buf + oEi), *W = (double2*)(buf + oW), *avg = (double2*)(buf + oAvg);
+    double* dqs = (double*)(buf + oQs);
+    int64_t* ddi = (int64_t*)(buf + oDi);
+    int* dmm = (int*)(buf + oMm);
+    int* dmp = (int*)(buf + oMp);
+    int* piv = (int*)(buf + oPiv);
+    int* info = (int*)(buf + oInfo);
+    cuDoubleComplex** pa = (cuDoubleComplex**)(buf + oPa);
+    cuDoubleComplex** pb = (cuDoubleComplex**)(buf + oPb);
+    cublasSetStream(c->cublas, c->stream);
+    const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
+    // chi0 -> eps^-1 for the first Dn momenta of the chunk arrays (qs, rho already set)
+    auto eps_inv = [&](int64_t Dn) -> int {
+        if (cublasZgemmStridedBatched(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, ng, ng, (int)R, &one, (const cuDoubleComplex*)r1, (int)R,
+                                      R * ng, (const cuDoubleComplex*)q1, (int)R, R * ng, &zero, (cuDoubleComplex*)C1, ng, gg,
+                                      (int)Dn) != CUBLAS_STATUS_SUCCESS ||
+            cublasZgemmStridedBatched(c->cublas, CUBLAS_OP_C, CUBLAS_OP_N, ng, ng, (int)R, &one, (const cuDoubleComplex*)r2, (int)R,
+                                      R * ng, (const cuDoubleComplex*)q2, (int)R, R * ng, &zero, (cuDoubleComplex*)C2, ng, gg,
+                                      (int)Dn) != CUBLAS_STATUS_SUCCESS)
+            return fail(c, BSE_ERR_CUDA, "cuBLAS failed in chi0");
+        const unsigned gb = (unsigned)((Dn * gg + 255) / 256);
+        rpa_chi0_kernel<<<gb, 256, 0, c->stream>>>((int)Dn, ng, fchi, dqs, c->d_g, c->itx, order, C1, C2, chi, A, einv);
+        c->launches++;
+        if (order == 1) {
+            std::vector<cuDoubleComplex*> ha(Dn), hb(Dn);
+            for (int64_t d = 0; d < Dn; d++) {
+                ha[d] = (cuDoubleComplex*)(A + d * gg);
+                hb[d] = (cuDoubleComplex*)(chi + d * gg);
+            }
+            int sst;
+            if ((sst = cuda_check(c, cudaMemcpyAsync(pa, ha.data(), Dn * 8, cudaMemcpyHostToDevice, c->stream), "LU pointers"))) return sst;
+            if ((sst = cuda_check(c, cudaMemcpyAsync(pb, hb.data(), Dn * 8, cudaMemcpyHostToDevice, c->stream), "LU pointers"))) return sst;
+            int hinfo = 0;
+            if (cublasZgetrfBatched(c->cublas, ng, pa, ng, piv, info, (int)Dn) != CUBLAS_STATUS_SUCCESS ||
+                cublasZgetrsBatched(c->cublas, CUBLAS_OP_N, ng, ng, (const cuDoubleComplex* const*)pa, ng, piv, pb, ng, &hinfo,
+                                    (int)Dn) != CUBLAS_STATUS_SUCCESS || hinfo != 0)
+                return fail(c, BSE_ERR_CUDA, "cuBLAS failed in the Dyson solve");
+            // the host vectors must outlive the copies: wait for them
+            if ((sst = cuda_check(c, cudaStreamSynchronize(c->stream), "Dyson solve"))) return sst;
+            rpa_einv_kernel<<<gb, 256, 0, c->stream>>>((int)Dn, ng, dqs, c->d_g, c->itx, chi, einv);
+            c->launches++;
+        }
+        return cuda_check(c, cudaGetLastError(), "RPA eps^-1");
+    };
+    const double zq[3] = {0, 0, 0};
+    st = band_states_shifted(c, zq, ecs, ev0, ccs, cv0);                    // valence at the grid k
+    // grid coordinates of every k
+    std::vector<int> ci(nk), cj(nk), ck(nk);
+    for (int k = 0; k < nk; k++) {
+        const int32_t x = dm.idx[k];
+        ci[k] = x & 1023; cj[k] = (x >> 10) & 1023; ck[k] = (x >> 20) & 1023;
+    }
+    auto wrap = [](int a, int m) { return ((a % m) + m) % m; };
+    const int64_t gtot = (int64_t)D * R * ng;
+    for (int64_t d0 = 0; d0 < nd && !st; d0 += D) {
+        const int64_t Dn = std::min<int64_t>(D, nd - d0);
+        std::vector<double> hq(3 * Dn);
+        std::vector<int64_t> hdi(Dn);
+        std::vector<int> hmm(Dn * nk), hmp(Dn * nk);
+        for (int64_t d = 0; d < Dn; d++) {
+            const int64_t dd = d0 + d;
+            const int o0 = (int)(dd % (2 * m0 - 1)) - (m0 - 1);
+            const int o1 = (int)((dd / (2 * m0 - 1)) % (2 * m1 - 1)) - (m1 - 1);
+            const int o2 = (int)(dd / ((int64_t)(2 * m0 - 1) * (2 * m1 - 1))) - (m2 - 1);
+            const double cr[3] = {o0 * dm.step[0], o1 * dm.step[1], o2 * dm.step[2]};
+            for (int x = 0; x < 3; x++)
+                hq[3 * d + x] = c->bmat_h[x] * cr[0] + c->bmat_h[3 + x] * cr[1] + c->bmat_h[6 + x] * cr[2];
+            hdi[d] = dd;
+            for (int k = 0; k < nk; k++) {
+                hmm[d * nk + k] = dm.inv[((int64_t)wrap(ci[k] - o0, m0) * m1 + wrap(cj[k] - o1, m1)) * m2 + wrap(ck[k] - o2, m2)];
+                hmp[d * nk + k] = dm.inv[((int64_t)wrap(ci[k] + o0, m0) * m1 + wrap(cj[k] + o1, m1)) * m2 + wrap(ck[k] + o2, m2)];
+            }
+        }
+        if ((st = cuda_check(c, cudaMemcpyAsync(dqs, hq.data(), 3 * Dn * 8, cudaMemcpyHostToDevice, c->stream), "RPA q"))) break;
+        if ((st = cuda_check(c, cudaMemcpyAsync(ddi, hdi.data(), Dn * 8, cudaMemcpyHostToDevice, c->stream), "RPA index"))) break;
+        if ((st = cuda_check(c, cudaMemcpyAsync(dmm, hmm.data(), Dn * nk * 4, cudaMemcpyHostToDevice, c->stream), "RPA map"))) break;
+        if ((st = cuda_check(c, cudaMemcpyAsync(dmp, hmp.data(), Dn * nk * 4, cudaMemcpyHostToDevice, c->stream), "RPA map"))) break;
+        rpa_rho_kernel<<<(unsigned)((Dn * R * ng + 255) / 256), 256, 0, c->stream>>>(
+            (int)Dn, R, ng, nk, nc, nv, nw, ns, dqs, dmm, dmp, c->d_g, c->d_centres, c->d_cc, c->d_ec, cv0, ev0, cv0, ev0, eta,
+            r1, q1, r2, q2);
+        c->launches++;
+        if ((st = eps_inv(Dn))) break;
+        rpa_w_kernel<<<(unsigned)((Dn * gg + 255) / 256), 256, 0, c->stream>>>((int)Dn, ng, dqs, c->d_g, c->itx, einv, W, 0);
+        const int64_t tp = Dn * nblk * nw * nw;
+        rpa_phi_kernel<<<(unsigned)((tp + 255) / 256), 256, 0, c->stream>>>(
+            (int)Dn, ddi, dqs, nblk, nw, NWs, ng, c->d_g, c->d_centres, W, c->d_phi,
+            c->p.precision == BSE_MIXED && !c->coupled ? c->d_phi32 : nullptr, 0);
+        c->launches += 2;
+        if (c->d_phi_c) {
+            rpa_phi_kernel<<<(unsigned)((tp + 255) / 256), 256, 0, c->stream>>>(
+                (int)Dn, ddi, dqs, nblk, nw, NWs, ng, c->d_g, c->d_centres, W, c->d_phi_c, nullptr, 1);
+            c->launches++;
+        }
+        // the host arrays of this chunk must outlive its copies
+        if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "RPA chunk"))) break;
+    }
+    (void)gtot;
+    // dk = 0: <W(q)> over the seeded sphere points, in +-q pairs (the points of the CPU restatement)
+    if (!st) st = cuda_check(c, cudaMemsetAsync(avg, 0, gg * 16, c->stream), "RPA average");
+    if (!st) {
+        const double radius = 2.0 * kPi * std::pow(3.0 / (4.0 * kPi * nk * c->geo.vol), 1.0 / 3.0);
+        std::mt19937_64 gen(c->p.rpa_seed);
+        auto uni = [&gen]() { return (double)(gen() >> 11) * 0x1.0p-53; };
+        double x[3] = {0, 0, 0};
+        for (int n = 0; n < c->p.rpa_points && !st;) {
+            double y[3];
+            for (int i = 0; i < 3; i++) y[i] = uni() > 0.5 ? -uni() * radius : uni() * radius;
+            const double ny = std::sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+            if (!(ny <= radius && ny > kMinval * kMinval)) continue;
+            for (int i = 0; i < 3; i++) x[i] = y[i];
+            // valence at k - x and at k + x; the partner -x swaps them
+            const double mx[3] = {-x[0], -x[1], -x[2]};
+            if ((st = band_states_shifted(c, x, ecs, evm, ccs, cvm))) break;
+            if ((st = band_states_shifted(c, mx, ecs, evp, ccs, cvp))) break;
+            for (int sgn = 0; sgn < 2 && !st; sgn++) {
+                const double hq[3] = {sgn ? -x[0] : x[0], sgn ? -x[1] : x[1], sgn ? -x[2] : x[2]};
+                if ((st = cuda_check(c, cudaMemcpyAsync(dqs, hq, 24, cudaMemcpyHostToDevice, c->stream), "RPA q"))) break;
+                rpa_rho_kernel<<<(unsigned)((R * ng + 255) / 256), 256, 0, c->stream>>>(
+                    1, R, ng, nk, nc, nv, nw, ns, dqs, nullptr, nullptr, c->d_g, c->d_centres, c->d_cc, c->d_ec,
+                    sgn ? cvp : cvm, sgn ? evp : evm, sgn ? cvm : cvp, sgn ? evm : evp, eta, r1, q1, r2, q2);
+                c->launches++;
+                if ((st = eps_inv(1))) break;
+                rpa_w_kernel<<<(unsigned)((gg + 255) / 256), 256, 0, c->stream>>>(1, ng, dqs, c->d_g, c->itx, einv, avg, 1);
+                c->launches++;
+                if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "RPA sphere point"))) break;
+            }
+            n += 2;
+        }
+    }
+    if (!st) {
+        // <W> / n_points, the head times the cell average of v; then the dk = 0 table entry
+        std::vector<double2> h(gg);
+        st = cuda_check(c, cudaMemcpyAsync(h.data(), avg, gg * 16, cudaMemcpyDeviceToHost, c->stream), "RPA average");
+        if (!st) st = cuda_check(c, cudaStreamSynchronize(c->stream), "RPA average");
+        if (!st) {
+            const double inv_n = 1.0 / c->p.rpa_points;
+            for (auto& v : h) { v.x *= inv_n; v.y *= inv_n; }
+            const int g0 = ng / 2;
+            h[g0 + (int64_t)ng * g0].x *= c->itx.cell_avg;
+            h[g0 + (int64_t)ng * g0].y *= c->itx.cell_avg;
+            const double hz[3] = {0, 0, 0};
+            const int64_t hd = dcenter;
+            st = cuda_check(c, cudaMemcpyAsync(W, h.data(), gg * 16, cudaMemcpyHostToDevice, c->stream), "RPA W0");
+            if (!st) st = cuda_check(c, cudaMemcpyAsync(dqs, hz, 24, cudaMemcpyHostToDevice, c->stream), "RPA q0");
+            if (!st) st = cuda_check(c, cudaMemcpyAsync(ddi, &hd, 8, cudaMemcpyHostToDevice, c->stream), "RPA index");
+            if (!st) {
+                rpa_phi_kernel<<<(unsigned)((nblk * nw * nw + 255) / 256), 256, 0, c->stream>>>(
+                    1, ddi, dqs, nblk, nw, NWs, ng, c->d_g, c->d_centres, W, c->d_phi,
+                    c->p.precision == BSE_MIXED && !c->coupled ? c->d_phi32 : nullptr, 0);
+                c->launches++;
+                if (c->d_phi_c) {
+                    rpa_phi_kernel<<<(unsigned)((nblk * nw * nw + 255) / 256), 256, 0, c->stream>>>(
+                        1, ddi, dqs, nblk, nw, NWs, ng, c->d_g, c->d_centres, W, c->d_phi_c, nullptr, 1);
+                    c->launches++;
+                }
+                st = cuda_check(c, cudaStreamSynchronize(c->stream), "RPA dk = 0");
+            }
+        }
+    }
+    cudaFreeAsync(buf, c->stream);
+    int h_status = 0;
+    if (!st) st = cuda_check(c, cudaMemcpyAsync(&h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "status");
+    if (!st) st = cuda_check(c, cudaStreamSynchronize(c->stream), "RPA tables");
+    if (!st && h_status) st = fail(c, h_status, "band states of the RPA screening");
+    return st;
 }
 
 int build_h64(bse_ctx* c) {
@@ -703,7 +1071,7 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     if (!c->bands_valid) return fail(c, BSE_ERR_STATE, "bands not computed");
     if (!c->tables_valid && (st = run_tables(c))) return st;
     stage_begin(c, 2);
-    const bool mixed = c->p.precision == BSE_MIXED;
+    const bool mixed = c->p.precision == BSE_MIXED && !c->coupled;   // the full BSE is built in FP64
     const bool coll = c->S == 1;
     // the own eigensolver reads full Hermitian storage; cuSOLVER reads the lower triangle
     const bool lower = !full && !coll && !c->coupled && h_out == nullptr && c->p.eig_solver != BSE_EIG_OWN;

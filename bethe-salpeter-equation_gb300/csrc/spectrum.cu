@@ -89,7 +89,8 @@ int run_oscillators(bse_ctx* c) {
     const int64_t n = c->n_opt;
     const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
     // the own solver already produced f = y^H z for every exciton; only refined vectors need a new dot
-    const int64_t ncols = c->f_from_eig ? c->n_refined : n;
+    // (the full BSE's solves write f for every pair, refined ones included)
+    const int64_t ncols = c->f_from_eig ? (c->coupled ? 0 : c->n_refined) : n;
     if (ncols > 0) {
         const unsigned blocks = (unsigned)((ncols * 32 + 255) / 256);
         if (c->p.precision == BSE_MIXED)

@@ -109,6 +109,10 @@ class BSEParams:
     precision: int = BSE_FP64
     eig_solver: int = BSE_EIG_OWN
     n_refine: int = 256
+    rpa_eta: float = 0.0
+    rpa_order: int = 1
+    rpa_points: int = 64
+    rpa_seed: int = 1
 
     def replace(self, **kw) -> "BSEParams":
         return dataclasses.replace(self, **kw)

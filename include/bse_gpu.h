@@ -59,8 +59,13 @@ enum { BSE_V_BARE_3D = 0, BSE_V_BARE_2D = 1 };
  *                    (2697-2728), Delta k = 0 handled by the cell average of v.
  *   BSE_W_RYTOVA_KELDYSH: 2-D screened W = conv*Lz / (2 |q| (eps + r0 |q|)); no
  *                    counterpart in the reference; Delta k = 0 uses the disk average.
- *   BSE_W_BARE:      metal branch without screening, W = v(Delta k + G) (2584-2591). */
-enum { BSE_W_EMPIRICAL = 0, BSE_W_RYTOVA_KELDYSH = 1, BSE_W_BARE = 2 };
+ *   BSE_W_BARE:      metal branch without screening, W = v(Delta k + G) (2584-2591).
+ *   BSE_W_RPA:       insulator branch with adding_screening = 1 (2597-2690): W_GG'(dk) =
+ *                    eps^-1_GG'(dk) v(dk + G') with the static RPA eps^-1 of the kept bands
+ *                    (Dielectric_Function::pull_values 2214-2315; rpa_order 0 first order, 1 Dyson),
+ *                    dk = 0 from rpa_points seeded points of the mini-BZ sphere.  Needs a complete
+ *                    periodic k grid. */
+enum { BSE_W_EMPIRICAL = 0, BSE_W_RYTOVA_KELDYSH = 1, BSE_W_BARE = 2, BSE_W_RPA = 3 };
 
 /* Arithmetic of the build and of the dense solve. */
 enum { BSE_FP64 = 0,   /* complex128 H, FP64 eigensolve */
@@ -91,7 +96,7 @@ typedef struct bse_params {
     double scissor;              /* added to conduction energies (815-816) */
     double q[3];                 /* excitonic momentum, q -> 0 (minval * x, 3590-3601) */
     int32_t tamm_dancoff;        /* 1: resonant block only; 0: full BSE with the coupling block B
-                                    (add_coupling_part 2929-3040), BSE_FP64 only;
+                                    (add_coupling_part 2929-3040); BSE_MIXED uses the own solver;
                                     no effect with ipa = 1 */
     int32_t ipa;                 /* 1: no kernel, H = diag(E_c - E_v) (3346-3365) */
     int32_t small_momentum;      /* 1: G=0 pair density is the dipole i q.<c|r|v> (1535-1650) */
@@ -105,6 +110,10 @@ typedef struct bse_params {
     int32_t precision;           /* BSE_FP64 / BSE_MIXED */
     int32_t eig_solver;          /* BSE_EIG_OWN / BSE_EIG_CUSOLVER */
     int32_t n_refine;            /* MIXED: lowest excitons refined in FP64 */
+    double rpa_eta;              /* BSE_W_RPA: broadening of chi0 (eV), 0 for an insulator */
+    int32_t rpa_order;           /* BSE_W_RPA: 0 eps^-1 = 1 + v chi0; 1 the Dyson equation */
+    int32_t rpa_points;          /* BSE_W_RPA: sphere points for dk = 0 (even: +-q pairs) */
+    uint64_t rpa_seed;           /* BSE_W_RPA: seed of those points (std::mt19937_64) */
 } bse_params;
 
 typedef struct bse_ctx bse_ctx;

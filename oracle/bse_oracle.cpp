@@ -779,7 +779,7 @@ int oracle_rpa_w(const bse_model* m, const bse_params* p, double eta, int order,
     // Delta k = 0: sphere average of eps^-1 (2614-2650), points drawn as the reference draws them
     const double radius = 2.0 * kPi * std::pow(3.0 / (4.0 * kPi * nk * geo.vol), 1.0 / 3.0);
     std::mt19937_64 gen(seed);
-    std::uniform_real_distribution<double> dis(0.0, 1.0);
+    auto dis = [&gen](std::mt19937_64&) { return (double)(gen() >> 11) * 0x1.0p-53; };   // uniform [0, 1)
     double xprev[3] = {0, 0, 0};
     for (int n = 0; n < n_points;) {
         double x[3];

@@ -111,6 +111,8 @@ def build(prob, band_states=None, w_table=None, **overrides):
     M = _pkg().capi.Marshalled(prob, **overrides)
     if band_states is None:
         band_states = bands(prob, **overrides)
+    if w_table is None and M.p.w_kind == 3 and not M.p.ipa:       # BSE_W_RPA
+        w_table = rpa_w(prob, M.p.rpa_eta, M.p.rpa_order, M.p.rpa_points, M.p.rpa_seed, **overrides)
     ec, ev, cc, cv = [np.ascontiguousarray(x) for x in band_states]
     H = np.zeros((M.n_h, M.n_h), np.complex128, order="F")
     rho = np.zeros((M.ng, M.n_rho), np.complex128)      # C order (ng, n_rho) == column-major n_rho x ng

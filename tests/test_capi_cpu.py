@@ -64,11 +64,15 @@ def test_rejects_nan(synth, gpu):
 
 
 def test_full_bse_validation(synth, gpu):
-    """tamm_dancoff = 0 (coupling block): FP64 only; other values are rejected."""
+    """tamm_dancoff = 0 (coupling block): FP64, or mixed with the own solver."""
     st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=2)
     assert st == -1 and "tamm_dancoff" in msg
-    st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0, precision=1)
-    assert st == -1 and "FP64" in msg
+    st, _ = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0, precision=1)
+    assert st in (0, -2)
+    st, msg = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0, precision=1, eig_solver=1)
+    assert st == -1 and "own eigensolver" in msg
+    st, _ = _create(gpu, synth.collinear_problem(grid=2), tamm_dancoff=0, precision=1)
+    assert st in (0, -2)
     st, _ = _create(gpu, synth.collinear_problem(grid=2), tamm_dancoff=0)
     assert st in (0, -2)
     st, _ = _create(gpu, synth.hbn_problem(grid=2), tamm_dancoff=0)
@@ -174,3 +178,19 @@ def test_rejects_out_of_range_inputs(synth, gpu):
     m2 = dataclasses.replace(m, r_cryst=m.r_cryst[keep], weights=m.weights[keep], h_r=m.h_r[:, keep])
     st, msg = _create(gpu, dataclasses.replace(base, model=m2))
     assert st == -1 and "-R" in msg
+
+
+def test_rpa_validation(synth, gpu):
+    """BSE_W_RPA: even rpa_points >= 2, rpa_order 0 or 1, a complete periodic k grid."""
+    prob = synth.hbn_problem(grid=3)
+    st, msg = _create(gpu, prob, w_kind=3, rpa_points=3)
+    assert st == -1 and "rpa_points" in msg
+    st, msg = _create(gpu, prob, w_kind=3, rpa_order=2)
+    assert st == -1 and "rpa_order" in msg
+    st, _ = _create(gpu, prob, w_kind=3, tamm_dancoff=0)
+    assert st in (0, -2)
+    part = prob.__class__(prob.model, prob.k_cart[:-1], prob.g_cart, prob.params)
+    st, msg = _create(gpu, part, w_kind=3)
+    assert st in (-1, -2)          # the grid check needs the context: NO_DEVICE here, BAD_INPUT on a GPU
+    st, _ = _create(gpu, prob, w_kind=3)
+    assert st in (0, -2)

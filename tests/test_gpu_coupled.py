@@ -109,3 +109,42 @@ def test_coupled_not_positive_definite_is_an_error(synth, gpu):
         ctx.build_kernel()
         with pytest.raises(gpu.BSEError):
             ctx.diagonalize()
+
+
+@pytest.mark.parametrize("name", ["hbn8", "mag8", "coll4"])
+def test_coupled_mixed_matches_oracle(synth, oracle, gpu, name):
+    """BSE_MIXED full BSE: FP32 Cholesky / inverse and the own FP32 solve of -L^-1 J L^-H, FP64
+    refinement of the lowest n_refine positive pairs on the definite pencil (J, M).  Refined
+    eigenvalues within 1e-8 eV; the others within the FP32 error of mu = -1/E, 1e-6 E^2 / E_min;
+    eps2 relative L2 1e-4."""
+    prob = _prob(synth, name)
+    bands = oracle.bands(prob)
+    ref = oracle.solve(prob, OMEGA, GAMMA, band_states=bands, tamm_dancoff=0)
+    n_ref = 32
+    with gpu.BSEContext(prob, tamm_dancoff=0, precision=1, n_refine=n_ref) as ctx:
+        ctx.set_bands(*bands)
+        ctx.build_kernel()
+        E, _ = ctx.diagonalize()
+        f = ctx.oscillators()
+        e2, _ = ctx.eps(OMEGA, GAMMA)
+        dg = ctx.diagnostics()
+    Er = ref["E"]
+    N = len(f) // 2            # positive pairs of the optically active block
+    off = len(E) - len(f)      # collinear: that block's values follow the spin-flip block's
+    assert np.abs(E[off + N:off + N + n_ref] - Er[off + N:off + N + n_ref]).max() < 1e-8
+    emin = np.abs(Er).min()
+    assert np.all(np.abs(E - Er) <= np.maximum(1e-5, 1e-6 * Er ** 2 / emin))
+    assert np.linalg.norm(e2 - ref["eps2"]) < 1e-4 * np.linalg.norm(ref["eps2"])
+    assert dg["n_refined"] == n_ref and dg["max_refined_residual"] < 1e-8 * np.abs(Er).max()
+
+
+def test_coupled_mixed_limits(synth, gpu):
+    prob = _prob(synth, "hbn8")
+    with pytest.raises(gpu.BSEError):
+        gpu.BSEContext(prob, tamm_dancoff=0, precision=1, eig_solver=1)
+    with gpu.BSEContext(prob, tamm_dancoff=0, precision=1, n_refine=8) as ctx:
+        ctx.compute_bands()
+        ctx.build_kernel()
+        with pytest.raises(gpu.BSEError) as ei:
+            ctx.diagonalize(want_vectors=True)
+        assert "eigenvectors" in str(ei.value)
