@@ -260,6 +260,7 @@ struct BuildArgs {
     bool on_grid;
     int m0, m1, m2;
     int nblk;
+    int k1_lo, k1_hi;           // rows built: k1 in [k1_lo, k1_hi) (a k tile; the whole list by default)
     const int32_t* kidx;
     const double* ec;
     const double* ev;
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(256) build_kernel(BuildArgs a, const typename 
     const int lane = threadIdx.x, warp = threadIdx.y, KW = blockDim.y;
     const int nb = a.nw * a.ns;
     T2* sC = reinterpret_cast<T2*>(smem_raw) + (size_t)warp * (a.nc + a.nv) * nb;   // [nc+nv][nb] of k2
-    const int k1 = blockIdx.x * 32 + lane;
+    const int k1 = a.k1_lo + blockIdx.x * 32 + lane;
     const int k2 = blockIdx.y * KW + warp;
     if (k2 < a.nk) {
         for (int i = lane; i < a.nc * nb; i += 32) {
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(256) build_kernel(BuildArgs a, const typename 
         }
     }
     __syncwarp();
-    if (k1 >= a.nk || k2 >= a.nk) return;
+    if (k1 >= a.k1_hi || k2 >= a.nk) return;
 
     const int sc = c_exc_spin[a.br].c, sv = c_exc_spin[a.br].v;   // direct: diagonal spin block br
     const int s1 = a.br / 3, s2 = a.bc / 3;                        // exchange: blocks 0 / 3
@@ -704,10 +705,12 @@ int launch_build_nw(bse_ctx* c, void* H, int64_t ld, bool lower, const void* phi
     a.on_grid = c->dmap.on_grid;
     a.m0 = c->dmap.m[0]; a.m1 = c->dmap.m[1]; a.m2 = c->dmap.m[2];
     a.nblk = 3 * c->S + 1;
+    a.k1_lo = c->build_k_lo;
+    a.k1_hi = c->build_k_hi > 0 ? c->build_k_hi : c->nk;
     a.kidx = c->d_kidx;
     a.ec = c->d_ec; a.ev = c->d_ev; a.cc = c->d_cc; a.cv = c->d_cv;
     const int KW = 8;
-    dim3 block(32, KW), grid((c->nk + 31) / 32, (c->nk + KW - 1) / KW, 1);
+    dim3 block(32, KW), grid((a.k1_hi - a.k1_lo + 31) / 32, (c->nk + KW - 1) / KW, 1);
     size_t smem = (size_t)KW * (c->nc + c->nv) * c->nb * sizeof(typename cplx<T>::t);
     // process-wide attribute: set once to the largest size (nc, nv <= 8, nb <= 32)
     static std::once_flag smem_once;
@@ -730,6 +733,8 @@ int launch_coupling_nw(bse_ctx* c, int br, int bc, int direct, int exch) {
     a.N = c->N; a.ld = c->n_h;
     a.br = br; a.bc = bc; a.do_direct = direct; a.do_exch = exch;
     a.fw = -1.0 / (c->geo.vol * c->nk);   // bse.version13.cpp:2960
+    a.k1_lo = 0;
+    a.k1_hi = c->nk;
     a.on_grid = c->dmap.on_grid;
     a.m0 = c->dmap.m[0]; a.m1 = c->dmap.m[1]; a.m2 = c->dmap.m[2];
     a.nblk = 3 * c->S + 1;
@@ -837,6 +842,9 @@ int run_rpa_tables(bse_ctx* c) {
     // momenta per chunk: the densities dominate, 4 R ng complex per momentum
     const int64_t per_d = 4 * R * ng * 16 + 6 * gg * 16 + 2 * (int64_t)nk * 4 + 64;
     const int64_t D = std::max<int64_t>(1, std::min<int64_t>(nd, (int64_t)(2e9 / (double)per_d)));
+    // the band kernels below report into the status word: start it at zero (bands may have been
+    // set from the host, in which case no band kernel has reset it)
+    if ((st = cuda_check(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream), "status reset"))) return st;
     // scratch: valence states at the grid k (and the sphere's k -+ q), conduction dummies, chunk arrays
     char* buf = nullptr;
     size_t off = 0;
@@ -1074,11 +1082,13 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
     const bool mixed = c->p.precision == BSE_MIXED && !c->coupled;   // the full BSE is built in FP64
     const bool coll = c->S == 1;
     // the own eigensolver reads full Hermitian storage; cuSOLVER reads the lower triangle
-    const bool lower = !full && !coll && !c->coupled && h_out == nullptr && c->p.eig_solver != BSE_EIG_OWN;
+    const bool tile = c->build_k_hi > 0;   // rows of one k tile (bse_build_kernel_rows)
+    const bool lower = !full && !tile && !coll && !c->coupled && h_out == nullptr && c->p.eig_solver != BSE_EIG_OWN;
     const int64_t ld = c->n_h;
     // every element the solver reads is written by the build (lower triangle, or all of it);
     // only the collinear layout has blocks the build never touches
-    if (coll && (st = cuda_check(c, cudaMemsetAsync(c->d_H, 0, (size_t)ld * ld * c->h_elem, c->stream), "H clear"))) return st;
+    if ((coll || tile) && (st = cuda_check(c, cudaMemsetAsync(c->d_H, 0, (size_t)ld * ld * c->h_elem, c->stream), "H clear")))
+        return st;
     const int dd = c->p.ipa ? 0 : 1, de = c->p.ipa ? 0 : 1;
     const void* phi = mixed ? (const void*)c->d_phi32 : (const void*)c->d_phi;
     const void* qx = mixed ? (const void*)c->d_qx32 : (const void*)c->d_qx;
@@ -1168,6 +1178,101 @@ int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out) {
         if ((st = cuda_check(c, cudaMemcpyAsync(rho_out, c->d_rho, (size_t)c->n_rho * c->ng * sizeof(double2), cudaMemcpyDeviceToHost, c->stream), "rho copy"))) return st;
     }
     if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "build sync"))) return st;
+    c->h_valid = true;
+    c->eig_valid = c->osc_valid = false;
+    return BSE_OK;
+}
+
+
+// rows r = g * nk + k (g over the n_h / nk groups (spin block, c, v), k in [k_lo, k_hi)) of H into
+// a compact column-major (nrows x n_h) complex128 block
+template <typename T2>
+__global__ void gather_rows_kernel(int64_t n_h, int nk, int k_lo, int nt, const T2* __restrict__ H, double2* __restrict__ out) {
+    const int64_t nrows = (n_h / nk) * nt;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nrows * n_h) return;
+    const int64_t i = t % nrows, j = t / nrows;
+    const int64_t r = (i / nt) * nk + k_lo + (i % nt);
+    const T2 v = H[r + n_h * j];
+    out[t] = make_double2((double)v.x, (double)v.y);
+}
+
+__global__ void narrow_h_kernel(int64_t n, const double2* __restrict__ in, float2* __restrict__ out) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < n) out[t] = make_float2((float)in[t].x, (float)in[t].y);
+}
+
+// The rows of H whose k index lies in [k_lo, k_hi) (bse_build_kernel_rows): the build restricted to
+// that k tile, the rows copied out in ascending order.  The context's matrix is left incomplete.
+int run_build_rows(bse_ctx* c, int k_lo, int k_hi, double* h_rows) {
+    int st;
+    if (c->coupled) return fail(c, BSE_ERR_BAD_INPUT, "row tiles of the build are for the Tamm-Dancoff matrix");
+    if (k_lo < 0 || k_hi > c->nk || k_lo >= k_hi) return fail(c, BSE_ERR_BAD_INPUT, "k tile outside [0, n_k)");
+    if (!h_rows) return fail(c, BSE_ERR_BAD_INPUT, "null row buffer");
+    c->build_k_lo = k_lo;
+    c->build_k_hi = k_hi;
+    st = run_build(c, true, nullptr, nullptr);
+    c->build_k_lo = c->build_k_hi = 0;
+    c->h_valid = false;
+    c->h64_pending = false;
+    if (st) return st;
+    const int64_t n_h = c->n_h, nt = k_hi - k_lo, nrows = (n_h / c->nk) * nt, tot = nrows * n_h;
+    double2* buf = nullptr;
+    if ((st = cuda_check(c, cudaMallocAsync((void**)&buf, (size_t)tot * sizeof(double2), c->stream), "row buffer"))) return st;
+    const unsigned g = (unsigned)((tot + 255) / 256);
+    if (c->p.precision == BSE_MIXED)
+        gather_rows_kernel<float2><<<g, 256, 0, c->stream>>>(n_h, c->nk, k_lo, (int)nt, (const float2*)c->d_H, buf);
+    else
+        gather_rows_kernel<double2><<<g, 256, 0, c->stream>>>(n_h, c->nk, k_lo, (int)nt, (const double2*)c->d_H, buf);
+    c->launches++;
+    st = cuda_check(c, cudaGetLastError(), "row gather");
+    if (!st) st = cuda_check(c, cudaMemcpyAsync(h_rows, buf, (size_t)tot * sizeof(double2), cudaMemcpyDeviceToHost, c->stream), "rows copy");
+    cudaFreeAsync(buf, c->stream);
+    if (!st) st = cuda_check(c, cudaStreamSynchronize(c->stream), "rows sync");
+    return st;
+}
+
+// H from the host (bse_set_kernel): the matrix a build would have left, e.g. gathered from row
+// tiles built on other devices; the pair densities (oscillators) and, for the mixed path, the
+// tables of the FP64 refinement come from this context's own bands and tables.
+int run_set_kernel(bse_ctx* c, const double* h) {
+    int st;
+    if (c->coupled) return fail(c, BSE_ERR_BAD_INPUT, "bse_set_kernel takes the Tamm-Dancoff matrix");
+    if (!h) return fail(c, BSE_ERR_BAD_INPUT, "null H");
+    if (!c->bands_valid && (st = run_bands(c))) return st;
+    if (!c->tables_valid && (st = run_tables(c))) return st;
+    const int64_t n_h = c->n_h, nn = n_h * n_h;
+    const bool mixed = c->p.precision == BSE_MIXED;
+    if (mixed) {
+        double2* buf = nullptr;
+        if ((st = cuda_check(c, cudaMallocAsync((void**)&buf, (size_t)nn * sizeof(double2), c->stream), "H staging"))) return st;
+        st = cuda_check(c, cudaMemcpyAsync(buf, h, (size_t)nn * sizeof(double2), cudaMemcpyHostToDevice, c->stream), "H upload");
+        if (!st) {
+            narrow_h_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, c->stream>>>(nn, buf, (float2*)c->d_H);
+            c->launches++;
+            st = cuda_check(c, cudaGetLastError(), "H narrow");
+        }
+        cudaFreeAsync(buf, c->stream);
+        if (st) return st;
+    } else if ((st = cuda_check(c, cudaMemcpyAsync(c->d_H, h, (size_t)nn * sizeof(double2), cudaMemcpyHostToDevice, c->stream),
+                                "H upload"))) {
+        return st;
+    }
+    if (c->S == 1) {
+        const int64_t n2 = 2 * c->N;
+        const size_t bb = (size_t)n2 * n2 * c->h_elem;
+        if (mixed)
+            gather_blocks_kernel<float2><<<(unsigned)((n2 * n2 + 255) / 256), 256, 0, c->stream>>>(
+                c->N, (const float2*)c->d_H, (float2*)c->d_blk, (float2*)((char*)c->d_blk + bb));
+        else
+            gather_blocks_kernel<double2><<<(unsigned)((n2 * n2 + 255) / 256), 256, 0, c->stream>>>(
+                c->N, (const double2*)c->d_H, (double2*)c->d_blk, (double2*)((char*)c->d_blk + bb));
+        c->launches++;
+    }
+    if ((st = cuda_check(c, cudaGetLastError(), "set kernel"))) return st;
+    if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "set kernel sync"))) return st;
+    c->h64_pending = mixed && !c->p.ipa && c->p.n_refine > 0;
+    c->h64_side = false;
     c->h_valid = true;
     c->eig_valid = c->osc_valid = false;
     return BSE_OK;

@@ -135,7 +135,10 @@ def test_coupled_mixed_matches_oracle(synth, oracle, gpu, name):
     emin = np.abs(Er).min()
     assert np.all(np.abs(E - Er) <= np.maximum(1e-5, 1e-6 * Er ** 2 / emin))
     assert np.linalg.norm(e2 - ref["eps2"]) < 1e-4 * np.linalg.norm(ref["eps2"])
-    assert dg["n_refined"] == n_ref and dg["max_refined_residual"] < 1e-8 * np.abs(Er).max()
+    # Rayleigh-Ritz in the span of the FP32 stage's vectors: the refined eigenvalues are second
+    # order in that subspace's FP32 error (checked to 1e-8 eV above), their residuals
+    # ||M x - E J x|| first order, a few eps32 * max|E|
+    assert dg["n_refined"] == n_ref and dg["max_refined_residual"] < 1e-6 * np.abs(Er).max()
 
 
 def test_coupled_mixed_limits(synth, gpu):
