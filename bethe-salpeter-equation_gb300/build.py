@@ -59,7 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(out)
     if force or jobs or not os.path.exists(LIB) or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcublas", "-lcusolver", "-lcudart"])
+        run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcublas", "-lcusolver", "-lcudart", "-Xlinker", "--no-undefined"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -513,7 +513,7 @@ int blas_check(bse_ctx* c, cublasStatus_t s, const char* what) {
 
 // Workspace of the two-stage path; the same layout is used by the reduction and the back-transform.
 struct Layout {
-    size_t vall, tall, tau, ybuf, xbuf, lr, small, pnorm, pw, pgram, bc, ab, prog, flags, v2, zrm, total;
+    size_t vall, tall, tau, ybuf, xbuf, lr, small, pnorm, pw, pgram, bc, ab, prog, flags, v2, zrm, tcws, total;
     int npanel, gmax;
     int64_t vsize;
 };
@@ -549,6 +549,7 @@ Layout layout(int n, size_t e, bool keep_q, int gmax, int n_vec) {
     L.flags = carve((size_t)gmax * 128);   // one barrier flag per block, 128 bytes apart
     L.v2 = carve(keep_q ? (size_t)v2_offset(n, n - 1) * e : 0);
     L.zrm = carve(keep_q ? (size_t)n * std::max(n_vec, 1) * e : 0);
+    L.tcws = carve(e == sizeof(float2) ? tc_workspace(n, gmax) : 0);   // tensor-core update operands
     L.total = off;
     return L;
 }
@@ -615,6 +616,21 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
             }
         }
     }
+    // complex64: BSE_BAND_UPDATE=tc puts both products of the trailing update on the tensor cores
+    // (tc_update.cu); otherwise cuBLAS hemm / her2k (or the full-storage GEMMs of "gemm" / "emul")
+    bool use_tc = false, tc_h = false, tc_u = false;
+    if constexpr (sizeof(T2) == sizeof(float2)) {
+        const char* v = std::getenv("BSE_BAND_UPDATE");
+        use_tc = !full_update && v && std::string(v) == "tc" && tc_supported(lda);
+        // BSE_TC (sweeps): "hemm" or "update" keeps only that product on the tensor cores
+        const char* w = std::getenv("BSE_TC");
+        const std::string tw = w ? w : "both";
+        tc_h = use_tc && (tw == "both" || tw == "hemm");
+        tc_u = use_tc && (tw == "both" || tw == "update");
+        if (tc_h && !tc_u) full_update = true;   // the tensor-core hemm reads full storage
+    }
+    char* tcws = ws + Ly.tcws;
+    c->kt_used = 0;   // the kernel timing describes the last reduction
     int64_t voff = 0;
     unsigned* flags = (unsigned*)(ws + Ly.flags);
     if ((st = cuda_check(c, cudaMemsetAsync(flags, 0, (size_t)Ly.gmax * 128, c->stream), "barrier flags"))) return st;
@@ -644,7 +660,17 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
         // A22 <- Q^H A22 Q
         T2* A22 = A + r0 + (int64_t)r0 * lda;
         cublasHandle_t h = c->cublas;
-        if (full_update) {
+        if constexpr (sizeof(T2) == sizeof(float2)) {
+            if (tc_h) {
+                int nl = 0;
+                cudaEvent_t* ev = kernel_timer(c, 0, 8.0 * m * m, 8.0 * m * m * kk);
+                if (tc_hemm(c->stream, nsm, m, kk, A22, lda, Vj, Ybuf, tcws, err, &nl, ev))
+                    return fail(c, BSE_ERR_CUDA, "tensor-core hemm of the two-stage reduction failed to launch");
+                c->launches += nl;
+            }
+        }
+        if (tc_h) {
+        } else if (full_update) {
             if ((st = blas_check(c, cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, kk, m, &one, A22, CUDA_C_32F, (int)lda, Vj, CUDA_C_32F, m,
                                                  &zero, Ybuf, CUDA_C_32F, m, ctype, CUBLAS_GEMM_DEFAULT), "gemm AV"))) return st;
         } else {
@@ -654,7 +680,17 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
         if ((st = blas_check(c, xgemm(h, CUBLAS_OP_C, CUBLAS_OP_N, kk, kk, m, &one, Vj, m, Xbuf, m, &zero, Msm, NB), "gemm VX"))) return st;
         if ((st = blas_check(c, xtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_OP_C, kk, kk, &one, Tj, NB, Msm, NB, Nsm, NB), "trmm T^H"))) return st;
         if ((st = blas_check(c, xgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, kk, kk, &mhalf, Vj, m, Nsm, NB, &one, Xbuf, m), "gemm W"))) return st;
-        if (full_update) {
+        if constexpr (sizeof(T2) == sizeof(float2)) {
+            if (tc_u) {
+                int nl = 0;
+                cudaEvent_t* ev = kernel_timer(c, 1, 16.0 * m * m, 16.0 * m * m * kk);
+                if (tc_rank2k(c->stream, m, kk, A22, lda, Vj, Xbuf, tcws, err, &nl, ev))
+                    return fail(c, BSE_ERR_CUDA, "tensor-core update of the two-stage reduction failed to launch");
+                c->launches += nl;
+            }
+        }
+        if (tc_u) {
+        } else if (full_update) {
             // A22 -= [V W] [W V]^H on full storage, one GEMM with k = 2 kk
             T2* Lm = (T2*)(ws + Ly.lr);
             T2* Rm = Lm + (size_t)2 * NB * n;

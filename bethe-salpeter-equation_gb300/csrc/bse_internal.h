@@ -122,6 +122,17 @@ struct bse_ctx {
     // workspaces
     void* d_work = nullptr;
     size_t work_bytes = 0;
+    // per-launch CUDA-event timing of the tensor-core products of the last two-stage reduction
+    // (BSE_KERNEL_TIMING set at bse_create): kind 0 = hemm, 1 = update; events are reused
+    struct KernelTime {
+        cudaEvent_t ev[2] = {nullptr, nullptr};   // around the launch
+        int kind = 0;
+        double bytes = 0, flops = 0;
+    };
+    int build_k_lo = 0, build_k_hi = 0;   // k tile of the next build (rows k1 in [lo, hi)); hi = 0: all
+    bool ktime = false;
+    std::vector<KernelTime> kt;
+    size_t kt_used = 0;
 };
 
 namespace bse {
@@ -142,6 +153,8 @@ int band_states_shifted(bse_ctx* c, const double* q, double* ec, double* ev, dou
 int run_rpa_tables(bse_ctx* c);
 int run_tables(bse_ctx* c);
 int run_build(bse_ctx* c, bool full, double* h_out, double* rho_out);
+int run_build_rows(bse_ctx* c, int k_lo, int k_hi, double* h_rows);
+int run_set_kernel(bse_ctx* c, const double* h);
 int run_eig(bse_ctx* c, bool want_vectors);
 int run_refine(bse_ctx* c);
 // C = op(A) B for FP64 operands in compensated FP32 arithmetic (eigensolve.cu); C packed (ldc = M)
@@ -172,5 +185,20 @@ int band_tridiag(bse_ctx* c, int n, void* A, int64_t lda, bool fp64, void* d, vo
                  unsigned* bar, int* err, int n_vec);
 int band_backtransform(bse_ctx* c, int n, bool fp64, const void* z, int n_vec, void* X, char* ws, unsigned* bar,
                        int* err);
+
+// tensor-core (tcgen05 + TMA, split TF32) products of the complex64 two-stage reduction's
+// trailing update (tc_update.cu), on the full-storage m x m trailing matrix A22 (lda even):
+// Y = A22 V and A22 -= V W^H + W V^H.  ws: tc_workspace(n, nsm) bytes for every m <= n.
+// Return 0, or nonzero when a tensor map or a launch failed; *err is the device error word.
+size_t tc_workspace(int n, int nsm);
+bool tc_supported(int64_t lda);
+// ev (nullable): two events recorded around the tensor-core kernel itself.
+int tc_hemm(cudaStream_t st, int nsm, int m, int kk, const float2* A22, int64_t lda, const float2* V, float2* Y, char* ws,
+            int* err, int* launches, cudaEvent_t* ev = nullptr);
+int tc_rank2k(cudaStream_t st, int m, int kk, float2* A22, int64_t lda, const float2* V, const float2* W, char* ws, int* err,
+              int* launches, cudaEvent_t* ev = nullptr);
+// next event pair of the kernel timing (null when timing is off); bytes / flops are the launch's
+// algorithmic traffic and arithmetic
+cudaEvent_t* kernel_timer(bse_ctx* c, int kind, double bytes, double flops);
 
 }  // namespace bse

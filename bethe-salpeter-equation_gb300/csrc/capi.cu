@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <atomic>
 #include <map>
@@ -58,6 +59,24 @@ void stage_end(bse_ctx* c, int s) {
     if (c->stage_mute) return;
     cudaEventRecord(c->ev[2 * s + 1], c->stream);
     c->stage_ms[s] = -1.0;   // resolved lazily in bse_stage_times
+}
+
+cudaEvent_t* kernel_timer(bse_ctx* c, int kind, double bytes, double flops) {
+    if (!c->ktime) return nullptr;
+    if (c->kt_used == c->kt.size()) {
+        bse_ctx::KernelTime r;
+        if (cudaEventCreate(&r.ev[0]) != cudaSuccess || cudaEventCreate(&r.ev[1]) != cudaSuccess) {
+            cudaGetLastError();
+            if (r.ev[0]) cudaEventDestroy(r.ev[0]);
+            return nullptr;
+        }
+        c->kt.push_back(r);
+    }
+    auto& r = c->kt[c->kt_used++];
+    r.kind = kind;
+    r.bytes = bytes;
+    r.flops = flops;
+    return r.ev;
 }
 
 }  // namespace bse
@@ -239,6 +258,9 @@ void destroy_ctx(bse_ctx* c) {
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_h64) cudaEventDestroy(c->ev_h64);
+    for (auto& r : c->kt)
+        for (cudaEvent_t e : r.ev)
+            if (e) cudaEventDestroy(e);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->side2) cudaStreamDestroy(c->side2);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -357,6 +379,7 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     CK(cuda_check(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event"));
     CK(cuda_check(c, cudaEventCreateWithFlags(&c->ev_h64, cudaEventDisableTiming), "event"));
     for (auto& e : c->ev) CK(cuda_check(c, cudaEventCreate(&e), "event"));
+    c->ktime = std::getenv("BSE_KERNEL_TIMING") != nullptr;
     if (cublasCreate(&c->cublas) != CUBLAS_STATUS_SUCCESS) CK(fail(c, BSE_ERR_CUDA, "cublasCreate"));
     if (cusolverDnCreate(&c->cusolver) != CUSOLVER_STATUS_SUCCESS) CK(fail(c, BSE_ERR_CUDA, "cusolverDnCreate"));
     cublasSetStream(c->cublas, c->stream);
@@ -371,6 +394,7 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     CK(dmalloc(c, &c->d_kidx, nk * 4, "k index"));
     CK(dmalloc(c, &c->d_g, 3 * ng * 8, "G"));
     CK(dmalloc(c, &c->d_status, 16, "status"));
+    CK(cuda_check(c, cudaMemset(c->d_status, 0, 16), "status clear"));
     CK(dmalloc(c, &c->d_ec, 2 * nk * c->nc * 8, "e_c"));
     CK(dmalloc(c, &c->d_ev, 2 * nk * c->nv * 8, "e_v"));
     CK(dmalloc(c, &c->d_cc, nk * c->nc * nb * 16, "c_c"));
@@ -476,6 +500,20 @@ int bse_build_kernel(bse_ctx* c, double* h_out, double* rho_out) {
     return run_build(c, h_out != nullptr, h_out, rho_out);
 }
 
+int bse_build_kernel_rows(bse_ctx* c, int32_t k_lo, int32_t k_hi, double* h_rows) {
+    if (!c) return BSE_ERR_BAD_INPUT;
+    cudaSetDevice(c->device);
+    int st;
+    if (!c->bands_valid && (st = run_bands(c))) return st;
+    return run_build_rows(c, k_lo, k_hi, h_rows);
+}
+
+int bse_set_kernel(bse_ctx* c, const double* h) {
+    if (!c) return BSE_ERR_BAD_INPUT;
+    cudaSetDevice(c->device);
+    return run_set_kernel(c, h);
+}
+
 int bse_diagonalize(bse_ctx* c, double* e_out, double* a_out) {
     if (!c) return BSE_ERR_BAD_INPUT;
     cudaSetDevice(c->device);
@@ -570,10 +608,26 @@ int bse_stage_times(const bse_ctx* cc, double* ms, int32_t n) {
     return BSE_OK;
 }
 
-int bse_diagnostics(const bse_ctx* c, double* out, int32_t n) {
-    if (!c || !out) return BSE_ERR_BAD_INPUT;
-    const double v[4] = {c->max_residual, (double)c->last_clusters, (double)c->n_refined, (double)c->n_vec_valid};
-    for (int i = 0; i < n && i < 4; i++) out[i] = v[i];
+int bse_diagnostics(const bse_ctx* cc, double* out, int32_t n) {
+    if (!cc || !out) return BSE_ERR_BAD_INPUT;
+    bse_ctx* c = const_cast<bse_ctx*>(cc);
+    double v[12] = {c->max_residual, (double)c->last_clusters, (double)c->n_refined, (double)c->n_vec_valid};
+    // [4 + 4 kind ..]: milliseconds, launches, algorithmic bytes and flops of the tensor-core
+    // products (kind 0 hemm, 1 update) in the last two-stage reduction (BSE_KERNEL_TIMING)
+    if (c->kt_used && n > 4) {
+        cudaStreamSynchronize(c->stream);
+        for (size_t i = 0; i < c->kt_used; i++) {
+            const auto& r = c->kt[i];
+            float t = 0;
+            if (cudaEventElapsedTime(&t, r.ev[0], r.ev[1]) != cudaSuccess) { cudaGetLastError(); t = 0; }
+            double* o = v + 4 + 4 * r.kind;
+            o[0] += t;
+            o[1] += 1;
+            o[2] += r.bytes;
+            o[3] += r.flops;
+        }
+    }
+    for (int i = 0; i < n && i < 12; i++) out[i] = v[i];
     return BSE_OK;
 }
 

@@ -25,7 +25,7 @@ EXPORTS = [
     "bse_create", "bse_destroy", "bse_compute_bands", "bse_get_bands", "bse_set_bands",
     "bse_build_kernel", "bse_diagonalize", "bse_oscillators", "bse_eps", "bse_solve",
     "bse_stage_times", "bse_kernel_launches", "bse_reset_kernel_launches", "bse_eps_noalloc",
-    "bse_solve_many", "bse_diagnostics",
+    "bse_solve_many", "bse_diagnostics", "bse_build_kernel_rows", "bse_set_kernel",
 ]
 
 
@@ -63,6 +63,8 @@ def load(build_if_missing: bool = True):
     L.bse_get_bands.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
     L.bse_set_bands.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
     L.bse_build_kernel.argtypes = [C.c_void_p, _dp, _dp]
+    L.bse_build_kernel_rows.argtypes = [C.c_void_p, C.c_int32, C.c_int32, _dp]
+    L.bse_set_kernel.argtypes = [C.c_void_p, _dp]
     L.bse_diagonalize.argtypes = [C.c_void_p, _dp, _dp]
     L.bse_oscillators.argtypes = [C.c_void_p, _dp]
     L.bse_eps.argtypes = [C.c_void_p, _dp, C.c_int32, C.c_double, _dp, _dp]
@@ -139,6 +141,18 @@ class BSEContext:
         self._check(self.lib.bse_build_kernel(self.h, ptr(Hc), ptr(rho)))
         return (Hc.T if want_h else None), (rho.T if want_rho else None)
 
+    def build_kernel_rows(self, k_lo: int, k_hi: int):
+        """Rows of H with k in [k_lo, k_hi) (ascending r = g nk + k), shape (rows, n_h)."""
+        nrows = (self.m.n_h // self.m.nk) * (k_hi - k_lo)
+        out = np.zeros((self.m.n_h, max(nrows, 0)), np.complex128)   # column-major rows x n_h
+        self._check(self.lib.bse_build_kernel_rows(self.h, int(k_lo), int(k_hi), ptr(out)))
+        return out.T
+
+    def set_kernel(self, H):
+        """Upload the whole n_h x n_h H (numpy (row, col)) as if this context had built it."""
+        Hc = np.ascontiguousarray(np.asarray(H, dtype=np.complex128).T)   # column-major bytes
+        self._check(self.lib.bse_set_kernel(self.h, ptr(Hc)))
+
     def diagonalize(self, want_vectors: bool = False):
         E = np.zeros(self.m.n_exc)
         A = np.zeros((self.m.n_opt, self.m.n_opt), np.complex128) if want_vectors else None
@@ -181,6 +195,20 @@ class BSEContext:
 
     def reset_kernel_launches(self):
         self.lib.bse_reset_kernel_launches(self.h)
+
+
+def eps_noalloc(E, f, F, omega, gamma):
+    """bse_eps_noalloc on host arrays: eps2, eps1 of the Lorentzian sum over the excitons (E, f)."""
+    lib = load()
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    f = np.ascontiguousarray(f, dtype=np.complex128)
+    om = np.ascontiguousarray(omega, dtype=np.float64)
+    e2 = np.zeros(len(om))
+    e1 = np.zeros(len(om))
+    st = lib.bse_eps_noalloc(len(E), ptr(E), ptr(f), float(F), ptr(om), len(om), float(gamma), ptr(e2), ptr(e1), None)
+    if st != 0:
+        raise BSEError(st, lib.bse_last_error(None).decode())
+    return e2, e1
 
 
 def solve_many(contexts, omega, gamma, n_workers=8):

@@ -156,6 +156,19 @@ int bse_set_bands(bse_ctx* ctx, const double* e_c, const double* e_v,
  * rho_vc (2937, 2950). */
 int bse_build_kernel(bse_ctx* ctx, double* h_out, double* rho_out);
 
+/* Stage b split over devices (the build's row tiles, one per GPU; no device collective).
+ * bse_build_kernel_rows builds only the rows r = g * n_k + k with k in [k_lo, k_hi) (g over the
+ * n_h / n_k groups of spin block, c and v) and writes them, ascending, to h_rows as a column-major
+ * ((n_h / n_k) (k_hi - k_lo)) x n_h complex128 block; the context's own matrix is left incomplete
+ * (a diagonalize before the next build or bse_set_kernel is BSE_ERR_STATE).  bse_set_kernel takes
+ * the whole n_h x n_h complex128 matrix (column-major), e.g. gathered from those tiles on the
+ * host, as if this context had built it; the pair densities and, in mixed precision, the FP64
+ * matrix of the refinement come from the context's own bands and tables.  Tamm-Dancoff only
+ * (BSE_ERR_BAD_INPUT for the full BSE).  Same path as bse_build_kernel: the rows of
+ * Excitonic_Hamiltonian::pull_resonant_part_and_rcv (bse.version13.cpp:2767-2928) by k of the row. */
+int bse_build_kernel_rows(bse_ctx* ctx, int32_t k_lo, int32_t k_hi, double* h_rows);
+int bse_set_kernel(bse_ctx* ctx, const double* h);
+
 /* Stage c: dense Hermitian eigensolve == common_diagonalization (3120-3368).
  * e_out (nullable): n_exc eigenvalues ascending (collinear: H0 block then H1 block).
  * a_out (nullable): eigenvectors (spinless n_bse x n_bse; collinear: the
