@@ -1,20 +1,21 @@
 """Benchmark: q->0 Tamm-Dancoff BSE build + diagonalization + eps2 on one GB300.
 
-Workload (one "step" = one BSE solve): the magnetic spinful 4-orbital honeycomb model
-(2 sites x 2 spins, exchange splitting 0.5 eV, SOC 0.05 eV, random NNN hoppings
-sigma = 0.1 eV, seed 1234) on a 24x24 grid, 2 valence x 2 conduction bands, N_BSE = 2304,
-Rytova-Keldysh W + bare 2-D exchange, eps2 on 2000 points over 0-8 eV with 0.05 eV
-broadening.  Mixed precision: complex64 kernel build and FP32 eigensolve, FP64
-Rayleigh-Ritz refinement of the lowest 256 excitons.  Inputs are synthetic (seeded).
+Headline workload (one "step" = one BSE solve): the 8-orbital model (random Hermitian onsite
+blocks, nearest / next-nearest hoppings, seed 2024, gap ~1.5 eV) on a 48x48 grid, 4 valence x 4
+conduction bands, N_BSE = 36864, Rytova-Keldysh W + bare 2-D exchange, eps2 on 2000 points over
+0-8 eV with 0.05 eV broadening.  Mixed precision: complex64 kernel build, FP32 eigensolve (the
+dense -> band products on the tensor cores), FP64 Rayleigh-Ritz refinement of the lowest 256
+excitons.  Inputs are synthetic (seeded); the 10.9 GB matrix is far larger than L2.
 
-value  = device time per solve (CUDA events on the library's stream), inputs resident
-e2e    = the same solve through the C ABI with host buffers: context creation (model
-         upload), solve, copy-back of eigenvalues and eps, destroy -- wall clock
-Other keys: the plain FP64 GPU path (cuSOLVER zheevd) on the same problem, the max
-eigenvalue error of the mixed path against it, the roofline of the dominant kernel (the
-tridiagonal reduction of the own eigensolver; the kernel build as a second figure), the
-eigensolve rate in the 14.7 N^3 flop unit, the CPU oracle baseline and the SM clocks
-sampled during the timed region.
+value  = device time per solve (CUDA events on the library's stream), model resident
+e2e    = the same solve through the C ABI with host buffers, every step: context creation (model
+         upload from host memory), solve, copy-back of the eigenvalues and eps, destroy
+Other keys: the roofline of the dominant kernel (the tensor-core trailing update of the two-stage
+reduction, HBM-bound) with its tensor-pipe rate, the eigensolve rate in the 14.7 N^3 flop unit,
+the plain FP64 GPU path at N_BSE = 36864 (measured by `--workload fp64check`, committed under
+profiles/) and the mixed path's errors against it, the same comparison live at N_BSE = 2304
+(magnetic 4-orbital model, 24x24), the eps2 gradient time, the 64-model batch, the CPU oracle
+baseline and the SM clocks sampled during the timed region.
 """
 from __future__ import annotations
 
@@ -36,8 +37,10 @@ import __graft_entry__ as entry  # noqa: E402
 
 OMEGA = np.arange(2000) * 8.0 / 2000
 GAMMA = 0.05
-WORKLOAD = "magnetic4_24x24_2v2c"
+WORKLOAD = "orb8_48x48_4v4c"          # N_BSE = 36864
+WORKLOAD_SMALL = "magnetic4_24x24_2v2c"  # N_BSE = 2304
 METRIC = "BSE build+diag wall time and eps2 grad time at N_BSE; error vs FP64"
+FP64_LARGE_PROFILE = os.path.join(ROOT, "profiles", "fp64_vs_mixed_orb8_48x48.md")
 
 
 def _dist_env():
@@ -138,6 +141,38 @@ def cpu_oracle_solve_ms(orc, prob, reps=1):
     return min(ts)
 
 
+def cpu_sample_large(orc, synth, prob_small=None):
+    """One bounded CPU sample for the N_BSE = 36864 workload: the oracle's whole solve of the same
+    8-orbital model on a 12x12 grid (N_BSE = 2304), its stages scaled to N_BSE = 36864 -- the band,
+    build and spectrum stages by (36864 / 2304)^2 (their work is per exciton pair), the dense
+    eigensolve (LAPACK zheevd) by (36864 / 2304)^3.  Returns (estimated ms, stage ms, sample text)."""
+    prob = prob_small if prob_small is not None else synth.orb8_problem(grid=12)
+    tm = {}
+    t0 = time.perf_counter()
+    orc.solve(prob, OMEGA, GAMMA, timings=tm)
+    wall = (time.perf_counter() - t0) * 1e3
+    r = 36864 / prob.n_bse
+    quad = (tm["bands"] + tm["build"] + tm["eps"]) * 1e3
+    eig = tm["eig"] * 1e3
+    est = quad * r ** 2 + eig * r ** 3
+    text = (f"oracle solve of orb8 12x12 (N_BSE={prob.n_bse}) in {wall:.0f} ms (bands+build+eps {quad:.0f} ms, "
+            f"zheevd {eig:.0f} ms), scaled to N_BSE=36864: x{r ** 2:.0f} and x{r ** 3:.0f}")
+    return est, {"bands_build_eps_ms": quad, "zheevd_ms": eig, "wall_ms": wall}, text
+
+
+def fp64_large_record():
+    """The plain FP64 GPU solve at N_BSE = 36864 and the mixed path's errors against it, as measured
+    by `bench.py --workload fp64check` (one JSON line kept in the profile file)."""
+    try:
+        for ln in open(FP64_LARGE_PROFILE):
+            ln = ln.strip()
+            if ln.startswith("{") and '"fp64check"' in ln:
+                return json.loads(ln)
+    except OSError:
+        pass
+    return None
+
+
 def run_reference(args):
     ws, rank, _ = _dist_env()
     if rank != 0:
@@ -146,30 +181,83 @@ def run_reference(args):
     from importlib import import_module
     synth = import_module("bse_gb300.synth")
     orc = entry.load_oracle()
-    prob = _problem(synth)
+    small = synth.orb8_problem(grid=12)
     cores = int(orc.lib().oracle_num_threads())
     for _ in range(args.warmup):
-        orc.solve(prob, OMEGA, GAMMA)
+        cpu_sample_large(orc, synth, small)
     ts = []
+    text = ""
     for _ in range(args.steps):
-        t0 = time.perf_counter()
-        orc.solve(prob, OMEGA, GAMMA)
-        ts.append((time.perf_counter() - t0) * 1e3)
-    total = sum(ts)
-    ms = total / args.steps
+        est, _, text = cpu_sample_large(orc, synth, small)
+        ts.append(est)
+    ms = sum(ts) / len(ts)
     line = {
         "impl": "reference", "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_bse": prob.n_bse, "n_g": prob.ng, "precision": "fp64",
+        "config": {"workload": WORKLOAD, "n_bse": 36864, "n_g": small.ng, "precision": "fp64",
                    "l2": "inputs resident in host memory; CPU run"},
         "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port",
-                         "sample": f"full solve of the {WORKLOAD} workload (N_BSE={prob.n_bse}) per step: "
-                                   "C++ OpenMP restatement of the reference loops + LAPACK zheevd (scipy)"},
+                         "sample": "per step: " + text + "; C++ OpenMP restatement of the reference loops "
+                                   "+ LAPACK zheevd (scipy OpenBLAS)"},
         "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def _diag_full(gpu, ctx):
+    out = np.zeros(12)
+    ctx._check(ctx.lib.bse_diagnostics(ctx.h, out.ctypes.data_as(gpu._dp), 12))
+    return out
+
+
+def _small_comparison(gpu, synth, steps, flush):
+    """magnetic4 24x24 (N_BSE = 2304): mixed solve vs the plain FP64 GPU path, live."""
+    prob = synth.magnetic4_problem(grid=24)
+    with gpu.BSEContext(prob, precision=1, n_refine=256, eig_solver=0) as c:
+        c.solve(OMEGA, GAMMA)
+        tm = []
+        for _ in range(steps):
+            _flush(flush)
+            Em, e2m, _ = c.solve(OMEGA, GAMMA)
+            tm.append(c.stage_times()["solve"])
+    with gpu.BSEContext(prob, precision=0, eig_solver=1) as c64:
+        c64.solve(OMEGA, GAMMA)
+        t64 = []
+        for _ in range(max(1, min(3, steps))):
+            _flush(flush)
+            E64, e2_64, _ = c64.solve(OMEGA, GAMMA)
+            t64.append(c64.stage_times()["solve"])
+    mixed_ms, fp64_ms = float(np.median(tm)), float(np.median(t64))
+    return {"workload": WORKLOAD_SMALL, "n_bse": prob.n_bse, "mixed_ms": mixed_ms, "fp64_gpu_ms": fp64_ms,
+            "fp64_path": "cuSOLVER zheevd on the complex128 matrix (bse_solve, precision fp64)",
+            "speedup_vs_fp64_gpu": fp64_ms / mixed_ms,
+            "max_eig_err_ev": {"refined_lowest_256": float(np.abs(Em[:256] - E64[:256]).max()),
+                               "all": float(np.abs(Em - E64).max())},
+            "eps2_rel_l2_vs_fp64": float(np.linalg.norm(e2m - e2_64) / np.linalg.norm(e2_64))}
+
+
+def _batch_figure(gpu, synth, steps):
+    """64 seeded 2- to 4-band models (N_BSE 144 .. 3600): one bse_solve_many over them."""
+    import torch
+    probs = synth.random_batch_problems(n_models=64, seed=77)
+    ctxs = [gpu.BSEContext(p, precision=1, n_refine=64, eig_solver=0) for p in probs]
+    try:
+        gpu.solve_many(ctxs, OMEGA, GAMMA, n_workers=8)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            gpu.solve_many(ctxs, OMEGA, GAMMA, n_workers=8)
+            torch.cuda.synchronize()
+            ts.append((time.perf_counter() - t0) * 1e3)
+    finally:
+        for c in ctxs:
+            c.close()
+    ms = float(np.median(ts))
+    return {"workload": "batch64_rand_2to4band_12to30grid", "wall_ms": ms, "models_per_s": len(probs) / (ms / 1e3),
+            "n_bse_sum": int(sum(p.n_bse for p in probs))}
 
 
 def run_gpu(args):
@@ -179,133 +267,113 @@ def run_gpu(args):
         dist.init_process_group("nccl" if os.environ.get("BSE_BENCH_GLOO") is None else "gloo")
     import torch
     torch.cuda.set_device(local)
+    os.environ["BSE_KERNEL_TIMING"] = "1"     # per-launch events around the tensor-core products
     entry.load_package()
     from importlib import import_module
     synth = import_module("bse_gb300.synth")
     gpu = import_module("bse_gb300.gpu")
+    from bse_gb300.capi import Marshalled
     gpu.load().bse_set_device(local)
-    solver = {"own": 0, "cusolver": 1}[args.solver]
-    prob = _problem(synth)
-    mixed = dict(precision=1, n_refine=256, eig_solver=solver)
+    prob = synth.orb8_problem(grid=48)
+    N = prob.n_bse
+    mixed = dict(precision=1, n_refine=256, eig_solver=0)
+    mm = Marshalled(prob, **mixed)
+    h2d = _model_bytes(mm) + OMEGA.nbytes
+    d2h = mm.n_exc * 8 + 2 * OMEGA.nbytes
     flush = _l2_flush_buffer()
 
-    # --- device-resident timing (value) ---
-    ctx = gpu.BSEContext(prob, **mixed)
+    # --- K steps, each through the C ABI with host buffers: create (model upload), solve, copy-back,
+    # destroy.  value = the solve's device time (events on the library stream), e2e = the wall time ---
     for _ in range(args.warmup):
-        ctx.solve(OMEGA, GAMMA)
-    ctx.reset_kernel_launches()
-    step_ms, build_ms, eig_ms, tri_ms = [], [], [], []
+        with gpu.BSEContext(prob, **mixed) as c:
+            c.solve(OMEGA, GAMMA)
+    dev_ms, e2e_ms, stages, kts = [], [], [], []
+    launches = 0
     _barrier(ws)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
     t_host0 = time.perf_counter()
     for _ in range(args.steps):
-        _flush(flush)                                 # outside the solve's events
-        E_mixed, e2_mixed, _ = ctx.solve(OMEGA, GAMMA)
-        st = ctx.stage_times()
-        step_ms.append(st["solve"])
-        build_ms.append(st["build"])
-        eig_ms.append(st["eig"])
-        tri_ms.append(st["eig_tridiag"])
+        t0 = time.perf_counter()
+        with gpu.BSEContext(prob, **mixed) as c:
+            E_mixed, e2_mixed, _ = c.solve(OMEGA, GAMMA)
+            st = c.stage_times()
+            kts.append(_diag_full(gpu, c))
+            launches += c.kernel_launches()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        dev_ms.append(st["solve"])
+        stages.append(st)
     torch.cuda.synchronize()
     host_s = time.perf_counter() - t_host0
     clk = clocks.stop()
-    launches = ctx.kernel_launches()
-    stage = ctx.stage_times()
-    ctx.close()
     _barrier(ws)
-    dev_total = _max_over_ranks(ws, sum(step_ms))
-    ms_per_step = dev_total / args.steps
-    value = ms_per_step / ws          # whole-job time per solve (each rank solves one problem per step)
+    ms_per_step = _max_over_ranks(ws, sum(dev_ms)) / args.steps
+    value = ms_per_step / ws            # whole-job time per solve (one problem per rank and step)
+    e2e_value = _max_over_ranks(ws, sum(e2e_ms)) / args.steps / ws
+    stage_avg = {k: float(np.mean([s[k] for s in stages])) for k in stages[0]}
+    dg = kts[-1]
 
-    # --- end to end through the C ABI with host buffers (e2e) ---
-    e2e_ms = []
-    for _ in range(max(1, args.steps)):
-        _flush(flush)
-        t0 = time.perf_counter()
-        with gpu.BSEContext(prob, **mixed) as c2:
-            c2.solve(OMEGA, GAMMA)
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_value = _max_over_ranks(ws, sum(e2e_ms)) / len(e2e_ms) / ws
-    from bse_gb300.capi import Marshalled
-    mm = Marshalled(prob)
-    h2d = _model_bytes(mm) + OMEGA.nbytes
-    d2h = mm.n_exc * 8 + 2 * OMEGA.nbytes
-
-    # --- plain FP64 GPU path (cuSOLVER zheevd) and the error of the mixed path ---
-    with gpu.BSEContext(prob, precision=0, eig_solver=1) as c64:
-        c64.solve(OMEGA, GAMMA)
-        t64 = []
-        for _ in range(max(1, min(3, args.steps))):
-            _flush(flush)
-            E64, e2_64, _ = c64.solve(OMEGA, GAMMA)
-            t64.append(c64.stage_times()["solve"])
-    fp64_ms = float(np.median(t64))
-    nref = 256
-    err_ref = float(np.abs(E_mixed[:nref] - E64[:nref]).max())
-    err_all = float(np.abs(E_mixed - E64).max())
-    eps2_err = float(np.linalg.norm(e2_mixed - e2_64) / np.linalg.norm(e2_64))
-
-    # --- rooflines.  Dominant kernel (own solver): the one-stage tridiagonal reduction, which reads
-    # and rewrites the trailing (n-k-1)^2 block of full complex64 storage for every reflector k:
-    # 2 * 8 B * sum_m m^2 per launch.  The 42 MB matrix stays in L2 (ncu: 0.34 MB of DRAM traffic
-    # per launch), so the HBM denominator overstates what bounds it; the figure shows how far the
-    # latency-bound sweep is from streaming.  Second figure: the build kernel (HBM store of H). ---
-    N = prob.n_bse
-    nb = prob.model.nw * prob.model.n_spin
-    build_bytes = N * N * 8 + 16 * prob.nk * nb * (prob.params.nv + prob.params.nc)   # full c64 store (own solver)
-    build_avg_ms = float(np.mean(build_ms))
-    tri_bytes = 16 * (N - 1) * N * (2 * N - 1) // 6
-    tri_avg_ms = float(np.mean(tri_ms))
-    eig_avg_ms = float(np.mean(eig_ms))
+    # --- rooflines from the per-launch events of the timed steps ---
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except OSError:
         pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    bf16 = float(peaks.get("bf16_tflops", 1900.0))
+    src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback"
+    k_arr = np.array(kts)
+    upd_ms, upd_n, upd_bytes, upd_flops = (k_arr[:, 8 + i].sum() for i in range(4))
+    hemm_ms, hemm_n, hemm_bytes, hemm_flops = (k_arr[:, 4 + i].sum() for i in range(4))
+    roof = None
+    if upd_n > 0:
+        gbs = upd_bytes / (upd_ms * 1e-3) / 1e9
+        # tensor work actually issued: six BF16 products of the real-folded complex update
+        # (M = m rows, N = 2 m real columns, K = 4 kk) = 6 * 2 * m * 2m * 4kk = 96 m^2 kk = 6 * flops_alg
+        tflops = 6.0 * upd_flops / (upd_ms * 1e-3) / 1e12
+        roof = {"kernel": "tc_update_kernel (tcgen05 kind::f16, TMA)", "bound": "hbm", "achieved": gbs, "peak": hbm,
+                "peak_source": src, "unit": "GB/s", "frac": gbs / hbm,
+                "traffic": None, "alg_bytes_per_launch": upd_bytes / upd_n, "avg_launch_ms": upd_ms / upd_n,
+                "launches_per_solve": upd_n / args.steps,
+                "alg_bytes_unit": "16 m^2 per launch: the m x m complex64 trailing matrix read and written once",
+                "tensor": {"achieved": tflops, "peak": bf16, "unit": "TFLOP/s", "frac": tflops / bf16,
+                           "note": "BF16 tensor flops issued (6 split products) vs the measured dense BF16 peak"}}
+    hemm_fig = None
+    if hemm_n > 0:
+        gbs = hemm_bytes / (hemm_ms * 1e-3) / 1e9
+        hemm_fig = {"kernel": "tc_hemm_kernel", "bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                    "frac": gbs / hbm, "alg_bytes_per_launch": hemm_bytes / hemm_n, "avg_launch_ms": hemm_ms / hemm_n,
+                    "total_ms_per_solve": hemm_ms / args.steps}
+    eig_ms = stage_avg["eig"]
 
-    # --- eps2 gradient: 12 hopping/onsite parameters + r0, hand-written adjoint (FP64 forward) ---
+    # --- secondary figures (after the timed region) ---
+    small = _small_comparison(gpu, synth, max(1, min(5, args.steps)), flush)
     grad_ms = None
     if not args.no_grad:
         from bse_gb300.adjoint import ParamModel, backward, gpu_forward
         from bse_gb300.synth import MAGNETIC4_NOMINAL
         pm = ParamModel.magnetic4()
+        p2 = synth.magnetic4_problem(grid=24)
         wts = np.random.default_rng(11).uniform(0.0, 1.0, size=len(OMEGA))
-        fwd = gpu_forward(pm, prob, MAGNETIC4_NOMINAL, 10.0, OMEGA, GAMMA)      # warm-up
+        fwd = gpu_forward(pm, p2, MAGNETIC4_NOMINAL, 10.0, OMEGA, GAMMA)      # warm-up
         backward(pm, fwd["prob"], fwd, OMEGA, wts, GAMMA)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        fwd = gpu_forward(pm, prob, MAGNETIC4_NOMINAL, 10.0, OMEGA, GAMMA)
+        fwd = gpu_forward(pm, p2, MAGNETIC4_NOMINAL, 10.0, OMEGA, GAMMA)
         backward(pm, fwd["prob"], fwd, OMEGA, wts, GAMMA)
         torch.cuda.synchronize()
         grad_ms = (time.perf_counter() - t0) * 1e3
+    batch = None if args.no_batch else _batch_figure(gpu, synth, 3)
+    fp64_large = fp64_large_record()
 
-    # --- CPU baseline (oracle, rank 0) ---
     cpu = None
     if rank == 0 and not args.no_cpu:
         orc = entry.load_oracle()
-        cpu_ms = cpu_oracle_solve_ms(orc, prob)
-        cpu = {"value": cpu_ms, "unit": "ms", "cores": int(orc.lib().oracle_num_threads()), "kind": "port",
-               "sample": f"one full CPU solve of {WORKLOAD} (N_BSE={N}): C++ OpenMP restatement of the "
-                         "reference loops + LAPACK zheevd (scipy)"}
+        est, parts, text = cpu_sample_large(orc, synth)
+        cpu = {"value": est, "unit": "ms", "cores": int(orc.lib().oracle_num_threads()), "kind": "port",
+               "sample": text + "; C++ OpenMP restatement of the reference loops + LAPACK zheevd (scipy OpenBLAS)"}
 
-    build_gbs = build_bytes / (build_avg_ms * 1e-3) / 1e9
-    if args.solver == "own" and N <= 8192:
-        tri_gbs = tri_bytes / (tri_avg_ms * 1e-3) / 1e9
-        roof = {"kernel": "tridiag_fused_kernel<float2>", "bound": "hbm", "achieved": tri_gbs, "peak": peak,
-                "peak_source": peak_src, "unit": "GB/s", "frac": tri_gbs / peak,
-                "traffic": 42947840 + 5654784 if N == 2304 else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at N_BSE=2304 "
-                                  "(profiles/tridiag_fused_kernel_magnetic4_24x24.md): the 42 MB matrix is read "
-                                  "from DRAM once and then stays in L2",
-                "alg_bytes_per_launch": int(tri_bytes), "avg_launch_ms": tri_avg_ms}
-    else:
-        roof = {"kernel": "build_kernel<4,float>", "bound": "hbm", "achieved": build_gbs, "peak": peak,
-                "peak_source": peak_src, "unit": "GB/s", "frac": build_gbs / peak, "traffic": None,
-                "alg_bytes_per_launch": int(build_bytes), "avg_launch_ms": build_avg_ms}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "ms", "n_gpus": ws, "steps": args.steps,
@@ -313,28 +381,29 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "c64+fp64-refine", "data": "synthetic",
             "config": {"workload": WORKLOAD, "n_bse": N, "n_k": prob.nk, "n_g": prob.ng, "nw": prob.model.nw,
                        "nv": prob.params.nv, "nc": prob.params.nc, "n_omega": len(OMEGA), "gamma": GAMMA,
-                       "precision": "mixed", "n_refine": nref, "eig_solver": args.solver,
+                       "precision": "mixed", "n_refine": 256, "eig_solver": "own",
                        "parallelism": f"replicas x{ws}",
-                       "l2": "flushed between steps (256 MB write); H is 42 MB"},
+                       "l2": "inputs larger than L2 (the complex64 BSE matrix is 10.9 GB)"},
             "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
             "roofline": roof,
-            "roofline_build": {"kernel": "build_kernel<4,float>", "bound": "hbm", "achieved": build_gbs, "peak": peak,
-                               "peak_source": peak_src, "unit": "GB/s", "frac": build_gbs / peak, "traffic": None,
-                               "alg_bytes_per_launch": int(build_bytes), "avg_launch_ms": build_avg_ms},
-            "eig_rate": {"unit": "TFLOP/s", "flop_per_solve": 14.7 * N ** 3, "eig_ms": eig_avg_ms,
-                         "value": 14.7 * N ** 3 / (eig_avg_ms * 1e-3) / 1e12,
+            "roofline_hemm": hemm_fig,
+            "eig_rate": {"unit": "TFLOP/s", "flop_per_solve": 14.7 * N ** 3, "eig_ms": eig_ms,
+                         "value": 14.7 * N ** 3 / (eig_ms * 1e-3) / 1e12,
                          "note": "14.7 N^3 = zhetrd 16/3 + D&C 4/3 + zunmtr 8 (N^3 real flops), the LAPACK-equivalent count"},
-            "stages_ms": stage,
+            "stages_ms": stage_avg,
+            "max_refined_residual_ev": float(dg[0]),
+            "fp64_gpu_n36864": fp64_large,
+            "n2304_mixed_vs_fp64": small,
             "eps2_grad_ms": grad_ms,
-            "eps2_grad_config": "d(sum_s w_s eps2(w_s))/d(12 hopping/onsite, r0), FP64 forward + hand-written adjoint, N_BSE=2304",
-            "fp64_gpu_ms": fp64_ms,
-            "speedup_vs_fp64_gpu": fp64_ms / ms_per_step,
-            "max_eig_err_ev": {"refined_lowest_256": err_ref, "all": err_all},
-            "eps2_rel_l2_vs_fp64": eps2_err,
+            "eps2_grad_config": "d(sum_s w_s eps2(w_s))/d(12 hopping/onsite, r0), FP64 forward + hand-written adjoint, "
+                                "magnetic4 24x24 (N_BSE=2304)",
+            "batch64": batch,
             "host_wall_s": host_s,
             "clocks": clk,
         }
+        if fp64_large:
+            line["speedup_vs_fp64_gpu"] = fp64_large["fp64_gpu_ms"] / ms_per_step
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -378,54 +447,35 @@ def run_batch(args):
     return 0
 
 
-def run_large(args):
-    """8-orbital model, 4v x 4c, complex64 BSE matrix, FP64 refinement of the lowest 256:
-    a mixed solve at 48x48 (N_BSE = 36864) with its FP64 residual bound, and FP64 (cuSOLVER
-    zheevd) vs mixed solves at 12x12 and 24x24 (N_BSE = 2304, 9216) for the same-size eigenvalue
-    errors and the N^3 extrapolation of the plain FP64 GPU time to N_BSE = 36864."""
-    import torch
+def run_fp64check(args):
+    """The plain FP64 GPU path at N_BSE = 36864 (orb8 48x48): bse_solve in FP64 with cuSOLVER zheevd
+    on the complex128 matrix, against the mixed path on the same problem: its time, the mixed
+    path's eigenvalue errors (refined lowest 256 and all) and the eps2 relative L2 error.  One JSON
+    line (kept in the profile file that the default run reads)."""
     entry.load_package()
     from importlib import import_module
     synth = import_module("bse_gb300.synth")
     gpu = import_module("bse_gb300.gpu")
-    out = {"metric": "BSE build+diag wall time at N_BSE=36864 (mixed) vs plain FP64 GPU path", "unit": "ms",
-           "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
-           "config": {"workload": "orb8_48x48_4v4c", "precision": "mixed", "n_refine": 256, "eig_solver": "own"}}
-    small = {}
-    for grid in (12, 24):
-        prob = synth.orb8_problem(grid=grid)
-        with gpu.BSEContext(prob, precision=0, eig_solver=1) as c64:
-            c64.solve(OMEGA, GAMMA)
-            E64, e2_64, _ = c64.solve(OMEGA, GAMMA)
-            t64 = c64.stage_times()["solve"]
-        with gpu.BSEContext(prob, precision=1, n_refine=256, eig_solver=0) as cm:
-            cm.solve(OMEGA, GAMMA)
-            Em, e2m, _ = cm.solve(OMEGA, GAMMA)
-            tm = cm.stage_times()
-            dg = cm.diagnostics()
-        small[prob.n_bse] = {"fp64_cusolver_ms": t64, "mixed_own_ms": tm["solve"], "mixed_stages_ms": tm,
-                             "max_err_refined_256_ev": float(np.abs(Em[:256] - E64[:256]).max()),
-                             "max_err_all_ev": float(np.abs(Em - E64).max()),
-                             "eps2_rel_l2": float(np.linalg.norm(e2m - e2_64) / np.linalg.norm(e2_64)),
-                             "max_refined_residual_ev": dg["max_refined_residual"], "clusters": dg["clusters"]}
-        print(json.dumps({"n_bse": prob.n_bse, **small[prob.n_bse]}), file=sys.stderr, flush=True)
     prob = synth.orb8_problem(grid=48)
     with gpu.BSEContext(prob, precision=1, n_refine=256, eig_solver=0) as cm:
-        t0 = time.perf_counter()
         cm.solve(OMEGA, GAMMA)
-        first = (time.perf_counter() - t0) * 1e3
-        if args.steps > 1:
-            cm.solve(OMEGA, GAMMA)
-        st = cm.stage_times()
+        Em, e2m, _ = cm.solve(OMEGA, GAMMA)
+        tm = cm.stage_times()
         dg = cm.diagnostics()
-    n1, n2 = 2304, 9216
-    expo = math.log(small[n2]["fp64_cusolver_ms"] / small[n1]["fp64_cusolver_ms"]) / math.log(n2 / n1)
-    fp64_est = small[n2]["fp64_cusolver_ms"] * (36864 / n2) ** 3
-    out.update({"value": st["solve"], "ms_per_step": st["solve"], "first_solve_wall_ms": first, "stages_ms": st,
-                "n_bse": prob.n_bse, "max_refined_residual_ev": dg["max_refined_residual"],
-                "clusters": dg["clusters"], "fp64_cusolver_ms_extrapolated_n3": fp64_est,
-                "fp64_growth_exponent_2304_9216": expo, "speedup_vs_fp64_gpu_extrapolated": fp64_est / st["solve"],
-                "smaller_sizes": small})
+    print(json.dumps({"mixed_ms": tm["solve"], "stages_ms": tm}), file=sys.stderr, flush=True)
+    t0 = time.perf_counter()
+    with gpu.BSEContext(prob, precision=0, eig_solver=1) as c64:
+        E64, e2_64, _ = c64.solve(OMEGA, GAMMA)
+        t64 = c64.stage_times()
+    wall64 = (time.perf_counter() - t0) * 1e3
+    out = {"fp64check": True, "workload": WORKLOAD, "n_bse": prob.n_bse,
+           "fp64_gpu_ms": t64["solve"], "fp64_wall_ms": wall64, "fp64_stages_ms": t64,
+           "fp64_path": "bse_solve, precision fp64: complex128 build + cuSOLVER zheevd (eigenvectors for the oscillators)",
+           "mixed_ms": tm["solve"], "mixed_stages_ms": tm, "speedup_vs_fp64_gpu": t64["solve"] / tm["solve"],
+           "max_eig_err_ev": {"refined_lowest_256": float(np.abs(Em[:256] - E64[:256]).max()),
+                              "all": float(np.abs(Em - E64).max())},
+           "eps2_rel_l2_vs_fp64": float(np.linalg.norm(e2m - e2_64) / np.linalg.norm(e2_64)),
+           "max_refined_residual_ev": dg["max_refined_residual"]}
     print(json.dumps(out))
     return 0
 
@@ -536,10 +586,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--solver", default="own", choices=["own", "cusolver"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
-    ap.add_argument("--workload", default="magnetic4", choices=["magnetic4", "batch", "large", "coupled", "rpa"])
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--workload", default="orb8_48", choices=["orb8_48", "batch", "fp64check", "coupled", "rpa"])
     args = ap.parse_args()
     if args.workload == "rpa":
         return run_rpa(args)
@@ -547,8 +597,8 @@ def main():
         return run_coupled(args)
     if args.workload == "batch":
         return run_batch(args)
-    if args.workload == "large":
-        return run_large(args)
+    if args.workload == "fp64check":
+        return run_fp64check(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
