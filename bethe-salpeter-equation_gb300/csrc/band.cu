@@ -684,7 +684,7 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
             if (tc_u) {
                 int nl = 0;
                 cudaEvent_t* ev = kernel_timer(c, 1, 16.0 * m * m, 16.0 * m * m * kk);
-                if (tc_rank2k(c->stream, m, kk, A22, lda, Vj, Xbuf, tcws, err, &nl, ev))
+                if (tc_rank2k(c->stream, nsm, m, kk, A22, lda, Vj, Xbuf, tcws, err, &nl, ev))
                     return fail(c, BSE_ERR_CUDA, "tensor-core update of the two-stage reduction failed to launch");
                 c->launches += nl;
             }

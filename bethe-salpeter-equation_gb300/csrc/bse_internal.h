@@ -195,8 +195,8 @@ bool tc_supported(int64_t lda);
 // ev (nullable): two events recorded around the tensor-core kernel itself.
 int tc_hemm(cudaStream_t st, int nsm, int m, int kk, const float2* A22, int64_t lda, const float2* V, float2* Y, char* ws,
             int* err, int* launches, cudaEvent_t* ev = nullptr);
-int tc_rank2k(cudaStream_t st, int m, int kk, float2* A22, int64_t lda, const float2* V, const float2* W, char* ws, int* err,
-              int* launches, cudaEvent_t* ev = nullptr);
+int tc_rank2k(cudaStream_t st, int nsm, int m, int kk, float2* A22, int64_t lda, const float2* V, const float2* W, char* ws,
+              int* err, int* launches, cudaEvent_t* ev = nullptr);
 // next event pair of the kernel timing (null when timing is off); bytes / flops are the launch's
 // algorithmic traffic and arithmetic
 cudaEvent_t* kernel_timer(bse_ctx* c, int kind, double bytes, double flops);

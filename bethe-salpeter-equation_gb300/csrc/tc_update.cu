@@ -60,23 +60,27 @@ constexpr uint32_t kWaitPolls = 1u << 22;  // try_wait polls before a wait gives
 
 // Shared-memory blocks: FP32 as TMA writes it (rows of 128 bytes, 128-byte swizzle), BF16 parts
 // as the MMA reads them (rows of 64 bytes, 64-byte swizzle).
-// hemm stage: [A fp32 16 KB | A parts 3 x 8 KB | B parts 3 x 4 KB], 4 stages
-constexpr int kHemmStages = 4;
+// hemm (persistent, stream-K): a ring of kHemmRing [FP32 A block 16 KB | B parts 3 x 4 KB] slots
+// filled by TMA, and kHemmParts slots of converted A parts (3 x 8 KB)
+constexpr int kHemmRing = 6, kHemmParts = 2;
 constexpr int kHemmChunk = 4;   // K blocks per tensor-memory accumulation chain (K = 128)
 constexpr uint32_t kHemmRaw = kRows * kKb * 4, kHemmA = kRows * kKb * 2, kHemmB = 64 * kKb * 2;
-constexpr uint32_t kHemmStage = kHemmRaw + 3 * kHemmA + 3 * kHemmB;
-constexpr size_t kHemmSmem = (size_t)kHemmStages * kHemmStage + 1024 + 256;
-// update: C tile 64 KB + 2 stages of [L fp32 16 KB | R fp32 8 KB | L parts 3 x 8 KB | B parts 3 x 8 KB]
-// (a B part: the 64 rows of R, then the 64 rows of iR)
-constexpr int kUpdStages = 2;
-constexpr int kUpdCols = 64;                               // complex columns per tile
-constexpr uint32_t kUpdC = kRows * 2 * kUpdCols * 4;       // 128 rows (256 reals) x 64 columns
-constexpr uint32_t kUpdRawL = kRows * kKb * 4, kUpdRawR = kUpdCols * kKb * 4;
-constexpr uint32_t kUpdPart = kRows * kKb * 2;             // one 128-row BF16 block
-constexpr uint32_t kUpdStage = kUpdRawL + kUpdRawR + 6 * kUpdPart;
-constexpr size_t kUpdSmem = (size_t)kUpdC + (size_t)kUpdStages * kUpdStage + 1024 + 256;
+constexpr uint32_t kHemmSlot = kHemmRaw + 3 * kHemmB, kHemmPartSlot = 3 * kHemmA;
+constexpr size_t kHemmSmem = (size_t)kHemmRing * kHemmSlot + (size_t)kHemmParts * kHemmPartSlot + 1024 + 512;
+// update (persistent, row strips): the strip's L parts resident (4 K blocks x 3 parts x 8 KB),
+// two C tiles of 128 rows x kUpdCols complex columns, a ring of B slots per K block (3 parts x
+// [kUpdCols rows of R | kUpdCols rows of iR] x 64 bytes)
+constexpr int kUpdCols = 32;                               // complex columns per tile
+constexpr int kUpdRing = 4;
+constexpr uint32_t kUpdL = 4 * 3 * kRows * kKb * 2;        // 96 KB
+constexpr uint32_t kUpdC = kRows * 2 * kUpdCols * 4;       // 128 rows (256 reals) x 32 columns
+constexpr uint32_t kUpdBpart = 2 * kUpdCols * kKb * 2;     // R rows then iR rows, one part
+constexpr uint32_t kUpdBslot = 3 * kUpdBpart;
+constexpr size_t kUpdSmem = (size_t)kUpdL + 2 * (size_t)kUpdC + (size_t)kUpdRing * kUpdBslot + 1024 + 512;
 static_assert(kHemmSmem <= 232448 && kUpdSmem <= 232448, "shared memory per CTA");
-static_assert(kHemmStage % 1024 == 0 && kUpdStage % 1024 == 0 && kUpdC % 1024 == 0, "1024-byte aligned blocks");
+static_assert(kHemmSlot % 1024 == 0 && kHemmPartSlot % 1024 == 0 && kUpdC % 1024 == 0 && kUpdBslot % 1024 == 0 &&
+                  kUpdL % 1024 == 0 && kUpdBpart % 512 == 0,
+              "block alignment");
 
 // ---------------------------------------------------------------------------------------------
 // PTX wrappers
@@ -200,9 +204,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// The six BF16 products of one 32-element K block (two MMAs of K = 16 each): parts (0,0), (0,1),
-// (1,0), (0,2), (2,0), (1,1) of A = a0 + a1 + a2 and B = b0 + b1 + b2.
-__device__ __forceinline__ void mma_block6(uint32_t tmem, const unsigned char* a0, uint32_t a_stride,
+// The six BF16 products of one 32-element K block (two MMAs of K = 16 each) of A = a0 + a1 + a2
+// and B = b0 + b1 + b2: a0 b0 into the "big" accumulator, the five smaller terms a0 b1, a1 b0,
+// a0 b2, a2 b0, a1 b1 into the "small" one.  The tensor pipe's FP32 accumulation truncates, and
+// with the small terms kept apart their truncation is relative to their own size; the epilogue
+// adds the two in FP32.
+__device__ __forceinline__ void mma_block6(uint32_t t_big, uint32_t t_small, const unsigned char* a0, uint32_t a_stride,
                                            const unsigned char* b0, uint32_t b_stride, uint32_t idesc, bool first) {
     constexpr int pa[6] = {0, 0, 1, 0, 2, 1}, pb[6] = {0, 1, 0, 2, 0, 1};
 #pragma unroll
@@ -211,7 +218,8 @@ __device__ __forceinline__ void mma_block6(uint32_t tmem, const unsigned char* a
         for (int q = 0; q < 6; q++) {
             const uint64_t ad = desc_sw64(a0 + pa[q] * a_stride) + (uint64_t)(k * 2);   // +32 bytes per K step
             const uint64_t bd = desc_sw64(b0 + pb[q] * b_stride) + (uint64_t)(k * 2);
-            mma_bf16(tmem, ad, bd, idesc, (first && k == 0 && q == 0) ? 0u : 1u);
+            const bool init = first && k == 0 && (q == 0 || q == 1);
+            mma_bf16(q == 0 ? t_big : t_small, ad, bd, idesc, init ? 0u : 1u);
         }
     }
 }
@@ -269,36 +277,53 @@ __device__ __forceinline__ unsigned char* align1024(unsigned char* p) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// hemm: partial sums P[split][i][0..63] = (Re, Im) of sum over this split's K range
+// hemm, persistent stream-K: the work units are (column tile t of A22, K block kb), t-major, and
+// CTA g takes units [lo(g), lo(g + 1)), lo(g) = g W / G, so every SM gets the same number of K
+// blocks whatever the tile count.  A CTA ends its tiles' partial sums at tile boundaries:
+// P[g][t - first tile of g][row][0..63] = (Re | Im) over its K blocks of tile t.
 // ---------------------------------------------------------------------------------------------
+struct HemmArgs {
+    int m, kb_per_tile, ntiles, slots;
+    int64_t units;        // ntiles * kb_per_tile
+    float* P;
+    int* err;
+};
+
 __global__ void __launch_bounds__(kThreads, 1)
-    tc_hemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int m, int kb_total,
-                   float* __restrict__ P, int64_t ldp, int* err) {
+    tc_hemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, HemmArgs h) {
     extern __shared__ unsigned char smraw[];
     unsigned char* sm = align1024(smraw);
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm + kHemmStages * kHemmStage);
-    uint64_t* conv = full + kHemmStages;
-    uint64_t* empty = conv + kHemmStages;
-    uint64_t* tfull = empty + kHemmStages;   // [2] accumulator buffer b holds a finished chunk
-    uint64_t* tempty = tfull + 2;            // [2] accumulator buffer b drained
+    unsigned char* parts = sm + kHemmRing * kHemmSlot;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(parts + kHemmParts * kHemmPartSlot);
+    uint64_t* rfull = bars;                      // [ring] A block and B parts landed (TMA)
+    uint64_t* rconv = rfull + kHemmRing;         // [ring] A block converted (converters)
+    uint64_t* rmma = rconv + kHemmRing;          // [ring] B parts consumed (MMA)
+    uint64_t* pfull = rmma + kHemmRing;          // [parts] A parts written (converters)
+    uint64_t* pempty = pfull + kHemmParts;       // [parts] A parts consumed (MMA)
+    uint64_t* tfull = pempty + kHemmParts;       // [2] accumulator pair b holds a finished chain
+    uint64_t* tempty = tfull + 2;                // [2] accumulator pair b drained
     uint32_t* tslot = reinterpret_cast<uint32_t*>(tempty + 2);
     __shared__ int s_abort;
-    auto raw = [&](int s) { return sm + s * kHemmStage; };                            // FP32 A block
-    auto apart = [&](int s) { return sm + s * kHemmStage + kHemmRaw; };               // 3 parts, kHemmA apart
-    auto bpart = [&](int s) { return sm + s * kHemmStage + kHemmRaw + 3 * kHemmA; };  // 3 parts, kHemmB apart
+    auto raw = [&](int s) { return sm + s * kHemmSlot; };
+    auto bpart = [&](int s) { return sm + s * kHemmSlot + kHemmRaw; };     // 3 parts, kHemmB apart
+    auto apart = [&](int s) { return parts + s * kHemmPartSlot; };           // 3 parts, kHemmA apart
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i0 = blockIdx.x * kRows;
-    const int split = blockIdx.y, nsplit = gridDim.y;
-    const int kb0 = (int)((int64_t)kb_total * split / nsplit);
-    const int nkb = (int)((int64_t)kb_total * (split + 1) / nsplit) - kb0;
-    const int nchunk = (nkb + kHemmChunk - 1) / kHemmChunk;
+    const int64_t G = gridDim.x, g = blockIdx.x;
+    const int64_t u0 = g * h.units / G, u1 = (g + 1) * h.units / G;
+    const int nu = (int)(u1 - u0);
+    const int KB = h.kb_per_tile;
+    const int t_first = (int)(u0 / KB);
     if (threadIdx.x == 0) {
         s_abort = 0;
-        for (int s = 0; s < kHemmStages; s++) {
-            mbar_init(full + s, 1);
-            mbar_init(conv + s, 128);
-            mbar_init(empty + s, 1);
+        for (int s = 0; s < kHemmRing; s++) {
+            mbar_init(rfull + s, 1);
+            mbar_init(rconv + s, 128);
+            mbar_init(rmma + s, 1);
+        }
+        for (int s = 0; s < kHemmParts; s++) {
+            mbar_init(pfull + s, 128);
+            mbar_init(pempty + s, 1);
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(tfull + b, 1);
@@ -306,116 +331,155 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         fence_mbar_init();
     }
-    if (warp == 1) tmem_alloc(tslot, 128);
+    if (warp == 1) tmem_alloc(tslot, 256);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
+    // a chain ends at a multiple of kHemmChunk K blocks, at a tile's last K block, or at the range end
+    auto chain_end = [&](int64_t u) {
+        const int kb = (int)(u % KB);
+        return kb % kHemmChunk == kHemmChunk - 1 || kb == KB - 1 || u == u1 - 1;
+    };
+    auto chain_start = [&](int64_t u) { return u == u0 || (int)(u % KB) % kHemmChunk == 0; };
 
     if (warp == 0) {
         if (lane == 0) {
             prefetch_map(&tmA);
             prefetch_map(&tmB);
             int issued = 0;
-            for (int kb = 0; kb < nkb; kb++) {
-                const int s = kb % kHemmStages;
-                const uint32_t ph = (uint32_t)(kb / kHemmStages) & 1u;
-                if (!mbar_wait(empty + s, ph ^ 1u, &s_abort, err)) break;
-                mbar_arrive_tx(full + s, kHemmRaw + 3 * kHemmB);
-                const int x = (kb0 + kb) * kKb;
-                tma_load_2d(raw(s), &tmA, x, i0, full + s);
-                for (int p = 0; p < 3; p++) tma_load_2d(bpart(s) + p * kHemmB, &tmB, x, 64 * p, full + s);
-                issued = kb + 1;
+            for (int j = 0; j < nu; j++) {
+                const int64_t u = u0 + j;
+                const int s = j % kHemmRing;
+                const uint32_t ph = (uint32_t)(j / kHemmRing) & 1u;
+                // the slot is free once its A block is converted and its B parts are consumed
+                if (!mbar_wait(rconv + s, ph ^ 1u, &s_abort, h.err) || !mbar_wait(rmma + s, ph ^ 1u, &s_abort, h.err)) break;
+                mbar_arrive_tx(rfull + s, kHemmRaw + 3 * kHemmB);
+                const int x = (int)(u % KB) * kKb, i0 = (int)(u / KB) * kRows;
+                tma_load_2d(raw(s), &tmA, x, i0, rfull + s);
+                for (int p = 0; p < 3; p++) tma_load_2d(bpart(s) + p * kHemmB, &tmB, x, 64 * p, rfull + s);
+                issued = j + 1;
             }
-            for (int s = 0; s < kHemmStages; s++)
-                mbar_drain(full + s, s < issued ? (issued - 1 - s) / kHemmStages : -1);
+            for (int s = 0; s < kHemmRing; s++)
+                mbar_drain(rfull + s, s < issued ? (issued - 1 - s) / kHemmRing : -1);
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            // chains of kHemmChunk K blocks: the tensor pipe's FP32 accumulation truncates, so
-            // each chain starts from zero in one of two accumulator buffers and the epilogue adds
-            // the finished chains in FP32 registers
             constexpr uint32_t idesc = idesc_bf16(kRows, 64);
-            for (int kb = 0; kb < nkb; kb++) {
-                const int s = kb % kHemmStages;
-                const uint32_t ph = (uint32_t)(kb / kHemmStages) & 1u;
-                const int c = kb / kHemmChunk, b = c & 1;
-                const bool first = kb % kHemmChunk == 0;
-                if (first && c >= 2) {
-                    if (!mbar_wait(tempty + b, (uint32_t)(c / 2 - 1) & 1u, &s_abort, err)) break;
-                    tc_fence_after();
+            int c = -1;
+            for (int j = 0; j < nu; j++) {
+                const int64_t u = u0 + j;
+                const int s = j % kHemmRing, ps = j % kHemmParts;
+                const uint32_t ph = (uint32_t)(j / kHemmRing) & 1u, pph = (uint32_t)(j / kHemmParts) & 1u;
+                const bool first = chain_start(u);
+                if (first) {
+                    c++;
+                    if (c >= 2) {
+                        if (!mbar_wait(tempty + (c & 1), (uint32_t)(c / 2 - 1) & 1u, &s_abort, h.err)) break;
+                        tc_fence_after();
+                    }
                 }
-                if (!mbar_wait(conv + s, ph, &s_abort, err)) break;
+                if (!mbar_wait(rfull + s, ph, &s_abort, h.err) || !mbar_wait(pfull + ps, pph, &s_abort, h.err)) break;
                 tc_fence_after();
-                mma_block6(tmem + (uint32_t)(64 * b), apart(s), kHemmA, bpart(s), kHemmB, idesc, first);
-                mma_commit(empty + s);
-                if (kb % kHemmChunk == kHemmChunk - 1 || kb == nkb - 1) mma_commit(tfull + b);
+                const uint32_t tb = tmem + (uint32_t)(128 * (c & 1));
+                mma_block6(tb, tb + 64, apart(ps), kHemmA, bpart(s), kHemmB, idesc, first);
+                mma_commit(rmma + s);
+                mma_commit(pempty + ps);
+                if (chain_end(u)) mma_commit(tfull + (c & 1));
             }
         }
     } else {
         const int ct = threadIdx.x - 64;
         const int q = warp & 3;
         const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
+        const int r = q * 32 + lane;
         float acc[64];
 #pragma unroll
-        for (int u = 0; u < 64; u++) acc[u] = 0.f;
+        for (int e = 0; e < 64; e++) acc[e] = 0.f;
         bool ok = true;
-        auto drain = [&](int c) {
-            const int b = c & 1;
-            if (!mbar_wait(tfull + b, (uint32_t)(c / 2) & 1u, &s_abort, err)) ok = false;
+        // chains are drained in order, one behind the conversion; a chain that ends a tile (or
+        // the range) writes the tile's partial sums and clears the accumulator
+        int drained = 0, nchain = 0;
+        int chain_tile[2] = {0, 0}, chain_last[2] = {0, 0};
+        auto drain = [&]() {
+            const int cc = drained, b = cc & 1;
+            if (!mbar_wait(tfull + b, (uint32_t)(cc / 2) & 1u, &s_abort, h.err)) ok = false;
             __syncwarp();
             tc_fence_after();
 #pragma unroll
-            for (int cc = 0; cc < 64; cc += 16) {
-                float v[16];
-                tmem_ld16(tq + (uint32_t)(64 * b + cc), v);
+            for (int e = 0; e < 64; e += 16) {
+                float vb[16], vs[16];
+                tmem_ld16(tq + (uint32_t)(128 * b + e), vb);
+                tmem_ld16(tq + (uint32_t)(128 * b + 64 + e), vs);
 #pragma unroll
-                for (int u = 0; u < 16; u++) acc[cc + u] += v[u];
+                for (int x = 0; x < 16; x++) acc[e + x] += vb[x] + vs[x];
             }
             tc_fence_before();
             mbar_arrive(tempty + b);
+            if (chain_last[b]) {
+                const int t = chain_tile[b], i = t * kRows + r;
+                if (ok && !s_abort && i < h.m) {
+                    float* out = h.P + (((int64_t)g * h.slots + (t - t_first)) * kRows + r) * 64;
+#pragma unroll
+                    for (int e = 0; e < 64; e += 4)
+                        *reinterpret_cast<float4*>(out + e) = make_float4(acc[e], acc[e + 1], acc[e + 2], acc[e + 3]);
+                }
+#pragma unroll
+                for (int e = 0; e < 64; e++) acc[e] = 0.f;
+            }
+            drained++;
         };
-        int drained = 0;
-        for (int kb = 0; kb < nkb; kb++) {
-            const int s = kb % kHemmStages;
-            const uint32_t ph = (uint32_t)(kb / kHemmStages) & 1u;
-            if (!mbar_wait(full + s, ph, &s_abort, err)) {
+        for (int j = 0; j < nu && ok; j++) {
+            const int64_t u = u0 + j;
+            const int s = j % kHemmRing, ps = j % kHemmParts;
+            const uint32_t ph = (uint32_t)(j / kHemmRing) & 1u, pph = (uint32_t)(j / kHemmParts) & 1u;
+            if (!mbar_wait(rfull + s, ph, &s_abort, h.err) || !mbar_wait(pempty + ps, pph ^ 1u, &s_abort, h.err)) {
                 ok = false;
                 break;
             }
-            convert_block(reinterpret_cast<const float*>(raw(s)), kRows, apart(s), kHemmA, nullptr, ct, 128);
+            convert_block(reinterpret_cast<const float*>(raw(s)), kRows, apart(ps), kHemmA, nullptr, ct, 128);
             fence_async_smem();
-            mbar_arrive(conv + s);
-            // chain c - 1 is finished by the time chain c has been converted
-            if (kb % kHemmChunk == kHemmChunk - 1 && kb / kHemmChunk >= 1 && ok) drain(drained++);
+            mbar_arrive(rconv + s);
+            mbar_arrive(pfull + ps);
+            if (chain_start(u)) {
+                chain_tile[nchain & 1] = (int)(u / KB);
+                nchain++;
+            }
+            if (chain_end(u)) {
+                const int kb = (int)(u % KB);
+                chain_last[(nchain - 1) & 1] = (kb == KB - 1 || u == u1 - 1) ? 1 : 0;
+                // the chain before this one has finished by now
+                if (nchain >= 2 && drained < nchain - 1) drain();
+            }
         }
-        while (ok && drained < nchunk) drain(drained++);
-        const int i = i0 + q * 32 + lane;
-        if (ok && !s_abort && i < m) {
-            float* out = P + ((int64_t)split * ldp + i) * 64;
-#pragma unroll
-            for (int u = 0; u < 64; u += 4) *reinterpret_cast<float4*>(out + u) = make_float4(acc[u], acc[u + 1], acc[u + 2], acc[u + 3]);
-        }
+        while (ok && drained < nchain) drain();
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, 128);
+        tmem_dealloc(tmem, 256);
     }
 }
 
-// Y (m x kk complex, column-major, ld m) = sum over splits, in split order
-__global__ void tc_hemm_reduce_kernel(int m, int kk, int nsplit, const float* __restrict__ P, int64_t ldp,
-                                      float2* __restrict__ Y) {
+// Y (m x kk complex, column-major, ld m): for each row, the partial sums of the CTAs whose range
+// covers its tile, in CTA order (bit-reproducible)
+__global__ void tc_hemm_reduce_kernel(int m, int kk, HemmArgs h, int64_t G, float2* __restrict__ Y) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= (int64_t)m * kk) return;
     const int i = (int)(t % m), p = (int)(t / m);
+    const int tile = i / kRows, r = i % kRows;
+    const int64_t KB = h.kb_per_tile, W = h.units;
+    const int64_t ua = (int64_t)tile * KB, ub = ua + KB - 1;
+    const int64_t ga = ((ua + 1) * G - 1) / W, gb = ((ub + 1) * G - 1) / W;   // CTAs holding units ua, ub
     float re = 0.f, im = 0.f;
-    for (int s = 0; s < nsplit; s++) {
-        const float* r = P + ((int64_t)s * ldp + i) * 64;
-        re += r[p];
-        im += r[32 + p];
+    for (int64_t g = ga; g <= gb; g++) {
+        const int64_t lo = g * W / G, hi = (g + 1) * W / G;
+        if (hi <= ua || lo > ub) continue;   // an empty range
+        const int64_t slot = tile - lo / KB;
+        const float* v = h.P + ((g * h.slots + slot) * kRows + r) * 64;
+        re += v[p];
+        im += v[32 + p];
     }
     Y[t] = make_float2(re, im);
 }
@@ -437,132 +501,196 @@ __global__ void tc_prep_hemm_kernel(int m, int kk, const float2* __restrict__ V,
 }
 
 // ---------------------------------------------------------------------------------------------
-// update: A22 -= L R^H, one 128 x 64 complex tile per CTA
+// update, persistent: tiles of 128 rows x kUpdCols complex columns in row-strip-major order, CTA g
+// taking tiles [g T / G, (g + 1) T / G).  The strip's L parts stay resident while its column
+// tiles stream; the C tiles and the accumulator pairs are double-buffered, so the TMA load / store
+// of one tile overlaps the MMAs of the next.
 // ---------------------------------------------------------------------------------------------
+struct UpdArgs {
+    int m, nstrips, ncols;
+    int64_t ntiles;
+    int* err;
+};
+
 __global__ void __launch_bounds__(kThreads, 1)
     tc_update_kernel(const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmL,
-                     const __grid_constant__ CUtensorMap tmR, int* err) {
+                     const __grid_constant__ CUtensorMap tmR, const __grid_constant__ CUtensorMap tmRi, UpdArgs a) {
     extern __shared__ unsigned char smraw[];
     unsigned char* sm = align1024(smraw);
-    float* Cs = reinterpret_cast<float*>(sm);   // [64 columns][256 reals]
-    unsigned char* stg = sm + kUpdC;
-    uint64_t* full = reinterpret_cast<uint64_t*>(stg + kUpdStages * kUpdStage);
-    uint64_t* conv = full + kUpdStages;
-    uint64_t* empty = conv + kUpdStages;
-    uint64_t* done = empty + kUpdStages;
-    uint64_t* cfull = done + 1;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(cfull + 1);
+    unsigned char* Ls = sm;                                   // [kb][part] 128 rows x 64 B
+    float* Cs0 = reinterpret_cast<float*>(sm + kUpdL);        // 2 x [kUpdCols columns][256 reals]
+    unsigned char* ring = sm + kUpdL + 2 * kUpdC;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(ring + kUpdRing * kUpdBslot);
+    uint64_t* bfull = bars;                     // [ring] B parts landed
+    uint64_t* bempty = bfull + kUpdRing;        // [ring] B parts consumed
+    uint64_t* cfull = bempty + kUpdRing;        // [2] C tile landed
+    uint64_t* cempty = cfull + 2;               // [2] C tile stored (its shared memory read out)
+    uint64_t* tfull = cempty + 2;               // [2] accumulator pair holds a finished tile
+    uint64_t* tempty = tfull + 2;               // [2] accumulator pair drained
+    uint64_t* lfull = tempty + 2;               // L parts of a strip landed
+    uint64_t* lfree = lfull + 1;                // MMAs of the previous strip done
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(lfree + 1);
     __shared__ int s_abort;
-    auto rawL = [&](int s) { return stg + s * kUpdStage; };
-    auto rawR = [&](int s) { return stg + s * kUpdStage + kUpdRawL; };
-    auto lpart = [&](int s) { return stg + s * kUpdStage + kUpdRawL + kUpdRawR; };                  // 3 parts
-    auto bpart = [&](int s) { return stg + s * kUpdStage + kUpdRawL + kUpdRawR + 3 * kUpdPart; };   // 3 parts: R | iR
-    constexpr int nkb = 128 / kKb;   // K = 128 reals: 2 kk complex pairs
+    auto lpart = [&](int kb) { return Ls + kb * 3 * (kRows * kKb * 2); };   // 3 parts, kRows*64 apart
+    auto bslot = [&](int s) { return ring + s * kUpdBslot; };             // 3 parts, kUpdBpart apart
+    auto Cs = [&](int b) { return Cs0 + b * (kUpdC / 4); };
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i0 = blockIdx.x * kRows, j0 = blockIdx.y * kUpdCols;
+    const int64_t G = gridDim.x, g = blockIdx.x;
+    const int64_t t0 = g * a.ntiles / G, t1 = (g + 1) * a.ntiles / G;
+    const int nt = (int)(t1 - t0);
     if (threadIdx.x == 0) {
         s_abort = 0;
-        for (int s = 0; s < kUpdStages; s++) {
-            mbar_init(full + s, 1);
-            mbar_init(conv + s, 128);
-            mbar_init(empty + s, 1);
+        for (int s = 0; s < kUpdRing; s++) {
+            mbar_init(bfull + s, 1);
+            mbar_init(bempty + s, 1);
         }
-        mbar_init(done, 1);
-        mbar_init(cfull, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(cfull + b, 1);
+            mbar_init(cempty + b, 1);
+            mbar_init(tfull + b, 1);
+            mbar_init(tempty + b, 128);
+        }
+        mbar_init(lfull, 1);
+        mbar_init(lfree, 1);
         fence_mbar_init();
     }
-    if (warp == 1) tmem_alloc(tslot, 128);
+    if (warp == 1) tmem_alloc(tslot, 256);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
+    auto strip_of = [&](int j) { return (int)((t0 + j) / a.ncols); };
+    auto col_of = [&](int j) { return (int)((t0 + j) % a.ncols); };
 
     if (warp == 0) {
         if (lane == 0) {
             prefetch_map(&tmC);
             prefetch_map(&tmL);
             prefetch_map(&tmR);
-            mbar_arrive_tx(cfull, kUpdC);
-            tma_load_2d(Cs, &tmC, 2 * i0, j0, cfull);
-            int issued = 0;
-            for (int kb = 0; kb < nkb; kb++) {
-                const int s = kb % kUpdStages;
-                const uint32_t ph = (uint32_t)(kb / kUpdStages) & 1u;
-                if (!mbar_wait(empty + s, ph ^ 1u, &s_abort, err)) break;
-                mbar_arrive_tx(full + s, kUpdRawL + kUpdRawR);
-                tma_load_2d(rawL(s), &tmL, kb * kKb, i0, full + s);
-                tma_load_2d(rawR(s), &tmR, kb * kKb, j0, full + s);
-                issued = kb + 1;
+            prefetch_map(&tmRi);
+            int nstrip = 0, issued = 0, lissued = 0, cissued[2] = {0, 0};
+            for (int j = 0; j < nt; j++) {
+                const int strip = strip_of(j), col = col_of(j);
+                if (j == 0 || strip != strip_of(j - 1)) {
+                    if (nstrip > 0 && !mbar_wait(lfree, (uint32_t)(nstrip - 1) & 1u, &s_abort, a.err)) break;
+                    mbar_arrive_tx(lfull, kUpdL);
+                    for (int kb = 0; kb < 4; kb++)
+                        for (int p = 0; p < 3; p++)
+                            tma_load_2d(lpart(kb) + p * (kRows * kKb * 2), &tmL, kb * kKb, p * a.m + strip * kRows, lfull);
+                    nstrip++;
+                    lissued = nstrip;
+                }
+                const int cb = j & 1;
+                if (j >= 2 && !mbar_wait(cempty + cb, (uint32_t)(j / 2 - 1) & 1u, &s_abort, a.err)) break;
+                mbar_arrive_tx(cfull + cb, kUpdC);
+                tma_load_2d(Cs(cb), &tmC, 2 * strip * kRows, col * kUpdCols, cfull + cb);
+                cissued[cb] = j / 2 + 1;
+                bool okb = true;
+                for (int kb = 0; kb < 4; kb++) {
+                    const int n = 4 * j + kb, s = n % kUpdRing;
+                    const uint32_t ph = (uint32_t)(n / kUpdRing) & 1u;
+                    if (!mbar_wait(bempty + s, ph ^ 1u, &s_abort, a.err)) { okb = false; break; }
+                    mbar_arrive_tx(bfull + s, kUpdBslot);
+                    for (int p = 0; p < 3; p++) {
+                        tma_load_2d(bslot(s) + p * kUpdBpart, &tmR, kb * kKb, p * a.m + col * kUpdCols, bfull + s);
+                        tma_load_2d(bslot(s) + p * kUpdBpart + kUpdCols * 64, &tmRi, kb * kKb, p * a.m + col * kUpdCols,
+                                    bfull + s);
+                    }
+                    issued = n + 1;
+                }
+                if (!okb) break;
             }
-            mbar_drain(cfull, 0);
-            for (int s = 0; s < kUpdStages; s++)
-                mbar_drain(full + s, s < issued ? (issued - 1 - s) / kUpdStages : -1);
+            for (int s = 0; s < kUpdRing; s++) mbar_drain(bfull + s, s < issued ? (issued - 1 - s) / kUpdRing : -1);
+            for (int b = 0; b < 2; b++) mbar_drain(cfull + b, cissued[b] - 1);
+            mbar_drain(lfull, lissued - 1);
         }
     } else if (warp == 1) {
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_bf16(kRows, 2 * kUpdCols);
-            for (int kb = 0; kb < nkb; kb++) {
-                const int s = kb % kUpdStages;
-                const uint32_t ph = (uint32_t)(kb / kUpdStages) & 1u;
-                if (!mbar_wait(conv + s, ph, &s_abort, err)) break;
+            int nstrip = 0;
+            for (int j = 0; j < nt; j++) {
+                const int strip = strip_of(j);
+                if (j == 0 || strip != strip_of(j - 1)) {
+                    if (!mbar_wait(lfull, (uint32_t)nstrip & 1u, &s_abort, a.err)) break;
+                    nstrip++;
+                }
+                const int b = j & 1;
+                if (j >= 2 && !mbar_wait(tempty + b, (uint32_t)(j / 2 - 1) & 1u, &s_abort, a.err)) break;
                 tc_fence_after();
-                mma_block6(tmem, lpart(s), kUpdPart, bpart(s), kUpdPart, idesc, kb == 0);
-                mma_commit(empty + s);
+                const uint32_t tb = tmem + (uint32_t)(128 * b);
+                bool okb = true;
+                for (int kb = 0; kb < 4; kb++) {
+                    const int n = 4 * j + kb, s = n % kUpdRing;
+                    const uint32_t ph = (uint32_t)(n / kUpdRing) & 1u;
+                    if (!mbar_wait(bfull + s, ph, &s_abort, a.err)) { okb = false; break; }
+                    tc_fence_after();
+                    mma_block6(tb, tb + 64, lpart(kb), kRows * kKb * 2, bslot(s), kUpdBpart, idesc, kb == 0);
+                    mma_commit(bempty + s);
+                }
+                if (!okb) break;
+                mma_commit(tfull + b);
+                if (j == nt - 1 || strip_of(j + 1) != strip) mma_commit(lfree);
             }
-            mma_commit(done);
         }
     } else {
         const int ct = threadIdx.x - 64;
-        for (int kb = 0; kb < nkb; kb++) {
-            const int s = kb % kUpdStages;
-            const uint32_t ph = (uint32_t)(kb / kUpdStages) & 1u;
-            if (!mbar_wait(full + s, ph, &s_abort, err)) break;
-            convert_block(reinterpret_cast<const float*>(rawL(s)), kRows, lpart(s), kUpdPart, nullptr, ct, 128);
-            // rows 0..63 of each B part: R; rows 64..127: iR (64 rows of 64 bytes further on)
-            convert_block(reinterpret_cast<const float*>(rawR(s)), kUpdCols, bpart(s), kUpdPart, bpart(s) + kUpdCols * 64, ct, 128);
-            fence_async_smem();
-            mbar_arrive(conv + s);
-        }
-        const bool ok = mbar_wait(done, 0, &s_abort, err) && mbar_wait(cfull, 0, &s_abort, err);
-        __syncwarp();
-        tc_fence_after();
         const int q = warp & 3;
         const int r = q * 32 + lane;   // row of the tile
-#pragma unroll 1
-        for (int c = 0; c < kUpdCols; c += 16) {
-            float re[16], im[16];
-            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, re);
-            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(kUpdCols + c), im);
-            if (ok) {
+        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
+        for (int j = 0; j < nt; j++) {
+            const int b = j & 1;
+            const bool ok = mbar_wait(tfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err) &&
+                            mbar_wait(cfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err);
+            __syncwarp();
+            tc_fence_after();
+            float* C = Cs(b);
 #pragma unroll
-                for (int u = 0; u < 16; u++) {
-                    float2* cp = reinterpret_cast<float2*>(Cs + (c + u) * 2 * kRows) + r;
-                    const float2 x = *cp;
-                    *cp = make_float2(x.x - re[u], x.y - im[u]);
+            for (int c = 0; c < kUpdCols; c += 16) {
+                float rb[16], ib[16], rs[16], is[16];
+                tmem_ld16(tq + (uint32_t)(128 * b + c), rb);
+                tmem_ld16(tq + (uint32_t)(128 * b + kUpdCols + c), ib);
+                tmem_ld16(tq + (uint32_t)(128 * b + 64 + c), rs);
+                tmem_ld16(tq + (uint32_t)(128 * b + 64 + kUpdCols + c), is);
+                if (ok) {
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        float2* cp = reinterpret_cast<float2*>(C + (c + u) * 2 * kRows) + r;
+                        const float2 x = *cp;
+                        *cp = make_float2(x.x - (rb[u] + rs[u]), x.y - (ib[u] + is[u]));
+                    }
                 }
             }
-        }
-        fence_async_smem();
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        if (ct == 0 && ok && !s_abort) {
-            tma_store_2d(&tmC, 2 * i0, j0, Cs);
-            tma_store_drain();
+            tc_fence_before();
+            mbar_arrive(tempty + b);
+            fence_async_smem();
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            // leave together: a failed wait set s_abort before the barrier
+            if (*reinterpret_cast<volatile int*>(&s_abort)) break;
+            if (ct == 0) {
+                const int strip = strip_of(j), col = col_of(j);
+                tma_store_2d(&tmC, 2 * strip * kRows, col * kUpdCols, C);
+                tma_store_drain();
+                mbar_arrive(cempty + b);
+            }
         }
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, 128);
+        tmem_dealloc(tmem, 256);
     }
 }
 
-// L, R row-major (m rows x 64 complex, FP32): L = [V W], R = [W V], zero beyond kk
+// L, R, iR parts [3][m][128] (BF16, row-major: 64 complex per row): L = [V W], R = [W V], zero
+// beyond kk
 __global__ void tc_prep_update_kernel(int m, int kk, const float2* __restrict__ V, const float2* __restrict__ W,
-                                      float2* __restrict__ L, float2* __restrict__ R) {
+                                      __nv_bfloat16* __restrict__ L, __nv_bfloat16* __restrict__ R,
+                                      __nv_bfloat16* __restrict__ Ri) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= (int64_t)m * 64) return;
+    const int64_t n = (int64_t)m * 64;
+    if (t >= n) return;
     const int i = (int)(t >> 6), p = (int)(t & 63), pp = p & 31;
     float2 l = make_float2(0.f, 0.f), rr = l;
     if (pp < kk) {
@@ -570,8 +698,13 @@ __global__ void tc_prep_update_kernel(int m, int kk, const float2* __restrict__ 
         l = p < 32 ? v : w;
         rr = p < 32 ? w : v;
     }
-    L[t] = l;
-    R[t] = rr;
+    const int64_t e = 2 * t, np = 2 * n;   // real index of the pair, part stride
+    split3(l.x, L[e], L[np + e], L[2 * np + e]);
+    split3(l.y, L[e + 1], L[np + e + 1], L[2 * np + e + 1]);
+    split3(rr.x, R[e], R[np + e], R[2 * np + e]);
+    split3(rr.y, R[e + 1], R[np + e + 1], R[2 * np + e + 1]);
+    split3(-rr.y, Ri[e], Ri[np + e], Ri[2 * np + e]);
+    split3(rr.x, Ri[e + 1], Ri[np + e + 1], Ri[2 * np + e + 1]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -622,21 +755,17 @@ cudaError_t set_attributes() {
 
 size_t al256(size_t x) { return (x + 255) / 256 * 256; }
 int kpad_of(int m) { return (2 * m + kKb - 1) / kKb * kKb; }
-int hemm_splits(int m, int nsm) {
-    const int tiles = (m + kRows - 1) / kRows, kbt = kpad_of(m) / kKb;
-    return std::max(1, std::min(kbt, (nsm + tiles - 1) / tiles));
-}
 
 }  // namespace tc
 
 size_t tc_workspace(int n, int nsm) {
     using namespace tc;
-    // the hemm (B1 parts, split partials) and the update (L, R) use the same region in turn;
-    // nsplit * tiles <= nsm + tiles for every panel
+    // the hemm (B1 parts, stream-K partial sums) and the update (L, R, iR parts) use the same
+    // region in turn; a CTA's partial sums cover at most ceil(tiles / G) + 2 tiles
     const size_t tiles = (size_t)(n + kRows - 1) / kRows;
     const size_t hemm = al256((size_t)3 * 64 * kpad_of(n) * sizeof(__nv_bfloat16)) +
-                        al256((nsm + tiles) * kRows * 64 * sizeof(float));
-    const size_t upd = 2 * al256((size_t)n * 64 * sizeof(float2));
+                        al256((tiles + 3 * (size_t)nsm) * kRows * 64 * sizeof(float));
+    const size_t upd = 3 * al256((size_t)3 * n * 128 * sizeof(__nv_bfloat16));
     return std::max(hemm, upd) + 1024;
 }
 
@@ -647,10 +776,18 @@ int tc_hemm(cudaStream_t st, int nsm, int m, int kk, const float2* A22, int64_t 
             int* err, int* launches, cudaEvent_t* ev) {
     using namespace tc;
     if (set_attributes() != cudaSuccess) return 1;
-    const int kpad = kpad_of(m), tiles = (m + kRows - 1) / kRows, nsplit = hemm_splits(m, nsm);
+    const int kpad = kpad_of(m), tiles = (m + kRows - 1) / kRows, KB = kpad / kKb;
+    HemmArgs h;
+    h.m = m;
+    h.kb_per_tile = KB;
+    h.ntiles = tiles;
+    h.units = (int64_t)tiles * KB;
+    const int64_t G = std::min<int64_t>(nsm, h.units);
+    const int64_t per = (h.units + G - 1) / G;
+    h.slots = (int)((per + KB - 1) / KB + 1);
+    h.err = err;
     __nv_bfloat16* B = reinterpret_cast<__nv_bfloat16*>(ws);
-    float* P = reinterpret_cast<float*>(ws + al256((size_t)3 * 64 * kpad * sizeof(__nv_bfloat16)));
-    const int64_t ldp = (int64_t)tiles * kRows;
+    h.P = reinterpret_cast<float*>(ws + al256((size_t)3 * 64 * kpad * sizeof(__nv_bfloat16)));
     CUtensorMap mA, mB;
     if (!make_map(&mA, A22, 2 * (uint64_t)m, (uint64_t)m, 2 * (uint64_t)lda * sizeof(float), kKb, kRows, MapKind::f32_sw128) ||
         !make_map(&mB, B, (uint64_t)kpad, 3 * 64, (uint64_t)kpad * sizeof(__nv_bfloat16), kKb, 64, MapKind::bf16_sw64))
@@ -658,31 +795,39 @@ int tc_hemm(cudaStream_t st, int nsm, int m, int kk, const float2* A22, int64_t 
     const int64_t nb = (int64_t)64 * kpad;
     tc_prep_hemm_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(m, kk, V, kpad, B);
     if (ev) cudaEventRecord(ev[0], st);
-    tc_hemm_kernel<<<dim3((unsigned)tiles, (unsigned)nsplit), kThreads, kHemmSmem, st>>>(mA, mB, m, kpad / kKb, P, ldp, err);
+    tc_hemm_kernel<<<(unsigned)G, kThreads, kHemmSmem, st>>>(mA, mB, h);
     if (ev) cudaEventRecord(ev[1], st);
-    tc_hemm_reduce_kernel<<<(unsigned)(((int64_t)m * kk + 255) / 256), 256, 0, st>>>(m, kk, nsplit, P, ldp, Y);
+    tc_hemm_reduce_kernel<<<(unsigned)(((int64_t)m * kk + 255) / 256), 256, 0, st>>>(m, kk, h, G, Y);
     *launches += 3;
     return cudaGetLastError() == cudaSuccess ? 0 : 3;
 }
 
 // A22 -= V W^H + W V^H (full storage) with the tensor cores.
-int tc_rank2k(cudaStream_t st, int m, int kk, float2* A22, int64_t lda, const float2* V, const float2* W, char* ws, int* err,
-              int* launches, cudaEvent_t* ev) {
+int tc_rank2k(cudaStream_t st, int nsm, int m, int kk, float2* A22, int64_t lda, const float2* V, const float2* W, char* ws,
+              int* err, int* launches, cudaEvent_t* ev) {
     using namespace tc;
     if (set_attributes() != cudaSuccess) return 1;
-    const size_t blk = al256((size_t)m * 64 * sizeof(float2));
-    float2* L = reinterpret_cast<float2*>(ws);
-    float2* R = reinterpret_cast<float2*>(ws + blk);
-    CUtensorMap mC, mL, mR;
+    const size_t blk = al256((size_t)3 * m * 128 * sizeof(__nv_bfloat16));
+    __nv_bfloat16* L = reinterpret_cast<__nv_bfloat16*>(ws);
+    __nv_bfloat16* R = reinterpret_cast<__nv_bfloat16*>(ws + blk);
+    __nv_bfloat16* Ri = reinterpret_cast<__nv_bfloat16*>(ws + 2 * blk);
+    CUtensorMap mC, mL, mR, mRi;
     if (!make_map(&mC, A22, 2 * (uint64_t)m, (uint64_t)m, 2 * (uint64_t)lda * sizeof(float), 2 * kRows, kUpdCols,
                   MapKind::f32_plain) ||
-        !make_map(&mL, L, 128, (uint64_t)m, 128 * sizeof(float), kKb, kRows, MapKind::f32_sw128) ||
-        !make_map(&mR, R, 128, (uint64_t)m, 128 * sizeof(float), kKb, kUpdCols, MapKind::f32_sw128))
+        !make_map(&mL, L, 128, 3 * (uint64_t)m, 128 * sizeof(__nv_bfloat16), kKb, kRows, MapKind::bf16_sw64) ||
+        !make_map(&mR, R, 128, 3 * (uint64_t)m, 128 * sizeof(__nv_bfloat16), kKb, kUpdCols, MapKind::bf16_sw64) ||
+        !make_map(&mRi, Ri, 128, 3 * (uint64_t)m, 128 * sizeof(__nv_bfloat16), kKb, kUpdCols, MapKind::bf16_sw64))
         return 2;
-    tc_prep_update_kernel<<<(unsigned)(((int64_t)m * 64 + 255) / 256), 256, 0, st>>>(m, kk, V, W, L, R);
-    const dim3 grid((unsigned)((m + kRows - 1) / kRows), (unsigned)((m + kUpdCols - 1) / kUpdCols));
+    tc_prep_update_kernel<<<(unsigned)(((int64_t)m * 64 + 255) / 256), 256, 0, st>>>(m, kk, V, W, L, R, Ri);
+    UpdArgs a;
+    a.m = m;
+    a.nstrips = (m + kRows - 1) / kRows;
+    a.ncols = (m + kUpdCols - 1) / kUpdCols;
+    a.ntiles = (int64_t)a.nstrips * a.ncols;
+    a.err = err;
+    const int64_t G = std::min<int64_t>(nsm, a.ntiles);
     if (ev) cudaEventRecord(ev[0], st);
-    tc_update_kernel<<<grid, kThreads, kUpdSmem, st>>>(mC, mL, mR, err);
+    tc_update_kernel<<<(unsigned)G, kThreads, kUpdSmem, st>>>(mC, mL, mR, mRi, a);
     if (ev) cudaEventRecord(ev[1], st);
     *launches += 2;
     return cudaGetLastError() == cudaSuccess ? 0 : 3;
@@ -717,7 +862,7 @@ int run_test(int op, int m, int kk, void* A, long long lda, const void* V, const
     if (W) cudaMemcpy(dW, W, v_bytes, cudaMemcpyHostToDevice);
     cudaMemset(derr, 0, sizeof(int));
     const int r = op == 0 ? bse::tc_hemm(0, nsm, m, kk, dA, lda, dV, dY, ws, derr, &launches)
-                          : bse::tc_rank2k(0, m, kk, dA, lda, dV, dW, ws, derr, &launches);
+                          : bse::tc_rank2k(0, nsm, m, kk, dA, lda, dV, dW, ws, derr, &launches);
     if (r != 0) st = BSE_ERR_CUDA;
     if (cudaDeviceSynchronize() != cudaSuccess) st = BSE_ERR_CUDA;
     cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
