@@ -53,7 +53,8 @@
 namespace bse {
 namespace tc {
 
-constexpr int kThreads = 192;
+constexpr int kThreads = 320;                 // warp 0 TMA, warp 1 MMA, warps 2-9 workers
+constexpr int kWorkers = kThreads - 64;       // two warps per tensor-memory lane quarter
 constexpr int kRows = 128;                 // MMA M: accumulator lanes
 constexpr int kKb = 32;                    // K elements per block: 128 bytes of FP32, 64 of BF16
 constexpr uint32_t kWaitPolls = 1u << 22;  // try_wait polls before a wait gives up
@@ -175,17 +176,28 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar)) : "memory");
 }
-// 16 consecutive 32-bit columns of this thread's tensor-memory lane
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
+// 16 consecutive 32-bit columns of this thread's tensor-memory lane at each of four addresses,
+// one wait for all four loads
+__device__ __forceinline__ void tmem_ld4x16(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, float (&v)[64]) {
+    uint32_t r[64];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%64];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%65];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47}, [%66];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%67];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]),
+          "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]),
+          "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
+          "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
+          "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3)
+        : "memory");
 #pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 64; i++) v[i] = __uint_as_float(r[i]);
 }
 
 // Shared-memory matrix descriptor of a K-major BF16 block in the 64-byte swizzled layout (rows of
@@ -256,6 +268,7 @@ __host__ __device__ constexpr uint32_t sw128_to_sw64(uint32_t q) {
 __device__ __forceinline__ void convert_block(const float* raw, int rows, unsigned char* parts, uint32_t part_stride,
                                               unsigned char* rot_parts, int t, int nt) {
     const float4* r4 = reinterpret_cast<const float4*>(raw);
+#pragma unroll 4
     for (int q = t; q < rows * 8; q += nt) {
         const float4 v = r4[q];
         const uint32_t off = sw128_to_sw64((uint32_t)q);
@@ -318,16 +331,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         s_abort = 0;
         for (int s = 0; s < kHemmRing; s++) {
             mbar_init(rfull + s, 1);
-            mbar_init(rconv + s, 128);
+            mbar_init(rconv + s, kWorkers);
             mbar_init(rmma + s, 1);
         }
         for (int s = 0; s < kHemmParts; s++) {
-            mbar_init(pfull + s, 128);
+            mbar_init(pfull + s, kWorkers);
             mbar_init(pempty + s, 1);
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(tfull + b, 1);
-            mbar_init(tempty + b, 128);
+            mbar_init(tempty + b, kWorkers);
         }
         fence_mbar_init();
     }
@@ -389,13 +402,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
     } else {
+        // workers: warp w reads tensor-memory lanes 32 (w % 4) ..; warps 2-5 own accumulator
+        // columns 0..31 (Re), warps 6-9 columns 32..63 (Im)
         const int ct = threadIdx.x - 64;
-        const int q = warp & 3;
-        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
+        const int q = warp & 3, half = (warp - 2) >> 2;
+        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(32 * half);
         const int r = q * 32 + lane;
-        float acc[64];
+        float acc[32];
 #pragma unroll
-        for (int e = 0; e < 64; e++) acc[e] = 0.f;
+        for (int e = 0; e < 32; e++) acc[e] = 0.f;
         bool ok = true;
         // chains are drained in order, one behind the conversion; a chain that ends a tile (or
         // the range) writes the tile's partial sums and clears the accumulator
@@ -406,26 +421,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (!mbar_wait(tfull + b, (uint32_t)(cc / 2) & 1u, &s_abort, h.err)) ok = false;
             __syncwarp();
             tc_fence_after();
+            float v[64];   // big 0..15, big 16..31, small 0..15, small 16..31 of this warp's columns
+            const uint32_t tb = tq + (uint32_t)(128 * b);
+            tmem_ld4x16(tb, tb + 16, tb + 64, tb + 80, v);
 #pragma unroll
-            for (int e = 0; e < 64; e += 16) {
-                float vb[16], vs[16];
-                tmem_ld16(tq + (uint32_t)(128 * b + e), vb);
-                tmem_ld16(tq + (uint32_t)(128 * b + 64 + e), vs);
-#pragma unroll
-                for (int x = 0; x < 16; x++) acc[e + x] += vb[x] + vs[x];
-            }
+            for (int x = 0; x < 32; x++) acc[x] += v[x] + v[32 + x];
             tc_fence_before();
             mbar_arrive(tempty + b);
             if (chain_last[b]) {
                 const int t = chain_tile[b], i = t * kRows + r;
                 if (ok && !s_abort && i < h.m) {
-                    float* out = h.P + (((int64_t)g * h.slots + (t - t_first)) * kRows + r) * 64;
+                    float* out = h.P + (((int64_t)g * h.slots + (t - t_first)) * kRows + r) * 64 + 32 * half;
 #pragma unroll
-                    for (int e = 0; e < 64; e += 4)
+                    for (int e = 0; e < 32; e += 4)
                         *reinterpret_cast<float4*>(out + e) = make_float4(acc[e], acc[e + 1], acc[e + 2], acc[e + 3]);
                 }
 #pragma unroll
-                for (int e = 0; e < 64; e++) acc[e] = 0.f;
+                for (int e = 0; e < 32; e++) acc[e] = 0.f;
             }
             drained++;
         };
@@ -437,7 +449,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ok = false;
                 break;
             }
-            convert_block(reinterpret_cast<const float*>(raw(s)), kRows, apart(ps), kHemmA, nullptr, ct, 128);
+            convert_block(reinterpret_cast<const float*>(raw(s)), kRows, apart(ps), kHemmA, nullptr, ct, kWorkers);
             fence_async_smem();
             mbar_arrive(rconv + s);
             mbar_arrive(pfull + ps);
@@ -549,7 +561,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_init(cfull + b, 1);
             mbar_init(cempty + b, 1);
             mbar_init(tfull + b, 1);
-            mbar_init(tempty + b, 128);
+            mbar_init(tempty + b, kWorkers);
         }
         mbar_init(lfull, 1);
         mbar_init(lfree, 1);
@@ -634,10 +646,12 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
     } else {
+        // workers: warp w reads tensor-memory lanes 32 (w % 4) ..; warps 2-5 take complex columns
+        // 0..15 of the tile, warps 6-9 columns 16..31
         const int ct = threadIdx.x - 64;
-        const int q = warp & 3;
+        const int q = warp & 3, half = (warp - 2) >> 2;
         const int r = q * 32 + lane;   // row of the tile
-        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
+        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(16 * half);
         for (int j = 0; j < nt; j++) {
             const int b = j & 1;
             const bool ok = mbar_wait(tfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err) &&
@@ -645,26 +659,21 @@ __global__ void __launch_bounds__(kThreads, 1)
             __syncwarp();
             tc_fence_after();
             float* C = Cs(b);
+            float v[64];   // big Re, big Im, small Re, small Im of this warp's 16 columns
+            const uint32_t tb = tq + (uint32_t)(128 * b);
+            tmem_ld4x16(tb, tb + kUpdCols, tb + 64, tb + 64 + kUpdCols, v);
+            if (ok) {
 #pragma unroll
-            for (int c = 0; c < kUpdCols; c += 16) {
-                float rb[16], ib[16], rs[16], is[16];
-                tmem_ld16(tq + (uint32_t)(128 * b + c), rb);
-                tmem_ld16(tq + (uint32_t)(128 * b + kUpdCols + c), ib);
-                tmem_ld16(tq + (uint32_t)(128 * b + 64 + c), rs);
-                tmem_ld16(tq + (uint32_t)(128 * b + 64 + kUpdCols + c), is);
-                if (ok) {
-#pragma unroll
-                    for (int u = 0; u < 16; u++) {
-                        float2* cp = reinterpret_cast<float2*>(C + (c + u) * 2 * kRows) + r;
-                        const float2 x = *cp;
-                        *cp = make_float2(x.x - (rb[u] + rs[u]), x.y - (ib[u] + is[u]));
-                    }
+                for (int u = 0; u < 16; u++) {
+                    float2* cp = reinterpret_cast<float2*>(C + (16 * half + u) * 2 * kRows) + r;
+                    const float2 x = *cp;
+                    *cp = make_float2(x.x - (v[u] + v[32 + u]), x.y - (v[16 + u] + v[48 + u]));
                 }
             }
             tc_fence_before();
             mbar_arrive(tempty + b);
             fence_async_smem();
-            asm volatile("bar.sync 1, 128;" ::: "memory");
+            asm volatile("bar.sync 1, %0;" ::"n"(kWorkers) : "memory");
             // leave together: a failed wait set s_abort before the barrier
             if (*reinterpret_cast<volatile int*>(&s_abort)) break;
             if (ct == 0) {
@@ -775,6 +784,7 @@ bool tc_supported(int64_t lda) { return (lda % 2) == 0 && tc::encode_fn() != nul
 int tc_hemm(cudaStream_t st, int nsm, int m, int kk, const float2* A22, int64_t lda, const float2* V, float2* Y, char* ws,
             int* err, int* launches, cudaEvent_t* ev) {
     using namespace tc;
+    if (m % 2) return 4;   // TMA clips the 2m-real columns at 16-byte granules: m even
     if (set_attributes() != cudaSuccess) return 1;
     const int kpad = kpad_of(m), tiles = (m + kRows - 1) / kRows, KB = kpad / kKb;
     HemmArgs h;
@@ -806,6 +816,7 @@ int tc_hemm(cudaStream_t st, int nsm, int m, int kk, const float2* A22, int64_t 
 int tc_rank2k(cudaStream_t st, int nsm, int m, int kk, float2* A22, int64_t lda, const float2* V, const float2* W, char* ws,
               int* err, int* launches, cudaEvent_t* ev) {
     using namespace tc;
+    if (m % 2) return 4;   // the TMA store of a C tile clips at 16-byte granules: 2m reals, m even
     if (set_attributes() != cudaSuccess) return 1;
     const size_t blk = al256((size_t)3 * m * 128 * sizeof(__nv_bfloat16));
     __nv_bfloat16* L = reinterpret_cast<__nv_bfloat16*>(ws);
@@ -840,7 +851,8 @@ int tc_rank2k(cudaStream_t st, int nsm, int m, int kk, float2* A22, int64_t lda,
 // ---------------------------------------------------------------------------------------------
 namespace {
 int run_test(int op, int m, int kk, void* A, long long lda, const void* V, const void* W, void* Y) {
-    if (m < 1 || kk < 1 || kk > 32 || lda < m || (lda % 2) != 0 || !bse::tc_supported(lda)) return BSE_ERR_BAD_INPUT;
+    if (m < 2 || (m % 2) != 0 || kk < 1 || kk > 32 || lda < m || (lda % 2) != 0 || !bse::tc_supported(lda))
+        return BSE_ERR_BAD_INPUT;
     int nsm = 0, dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return BSE_ERR_NO_DEVICE;

@@ -56,7 +56,7 @@ def test_tc_hemm_matches_fp64(gpu, m, kk, pad):
     assert err.max() < 1e-6, err.max()
 
 
-@pytest.mark.parametrize("m,kk,pad", [(128, 32, 0), (70, 32, 2), (300, 5, 4), (1000, 32, 0), (513, 31, 1)])
+@pytest.mark.parametrize("m,kk,pad", [(128, 32, 0), (70, 32, 2), (300, 5, 4), (1000, 32, 0), (514, 31, 2)])
 def test_tc_update_matches_fp64(gpu, m, kk, pad):
     L = _lib(gpu)
     rng = np.random.default_rng(10 * m + kk)
@@ -79,11 +79,15 @@ def test_tc_update_matches_fp64(gpu, m, kk, pad):
     assert not np.any(Abuf[:, m:])
 
 
-def test_tc_rejects_odd_leading_dimension(gpu):
+def test_tc_rejects_odd_sizes(gpu):
+    """The TMA tiles need whole 16-byte granules of the 2m-real columns: odd orders and odd leading
+    dimensions are refused before any device work (the reduction's orders are all even)."""
     L = _lib(gpu)
-    A = np.zeros((8, 9), np.complex64)
-    V = np.zeros((8, 2), np.complex64)
+    A = np.zeros((10, 10), np.complex64)
+    V = np.zeros((10, 2), np.complex64)
     assert L.bse_test_tc_hemm(8, 2, A.ctypes.data, 9, V.ctypes.data, V.ctypes.data) != 0
+    assert L.bse_test_tc_hemm(9, 2, A.ctypes.data, 10, V.ctypes.data, V.ctypes.data) != 0
+    assert L.bse_test_tc_rank2k(9, 2, A.ctypes.data, 10, V.ctypes.data, V.ctypes.data) != 0
 
 
 @pytest.mark.parametrize("m", [512, 2048, 4096])
