@@ -616,14 +616,14 @@ int band_tridiag_t(bse_ctx* c, int n, T2* A, int64_t lda, typename Real<T2>::t* 
             }
         }
     }
-    // complex64: BSE_BAND_UPDATE=tc puts both products of the trailing update on the tensor cores
-    // (tc_update.cu); otherwise cuBLAS hemm / her2k (or the full-storage GEMMs of "gemm" / "emul")
+    // complex64: both products of the trailing update on the tensor cores (tc_update.cu) by default;
+    // BSE_BAND_UPDATE=cublas keeps cuBLAS hemm / her2k, "gemm" / "emul" the full-storage GEMMs
     bool use_tc = false, tc_h = false, tc_u = false;
     if constexpr (sizeof(T2) == sizeof(float2)) {
         const char* v = std::getenv("BSE_BAND_UPDATE");
         // every trailing order m = n - 32 (j + 1) is even when n is (the TMA tiles need 2m reals
         // in whole 16-byte granules)
-        use_tc = !full_update && v && std::string(v) == "tc" && n % 2 == 0 && tc_supported(lda);
+        use_tc = !full_update && (!v || std::string(v) == "tc") && n % 2 == 0 && tc_supported(lda);
         // BSE_TC (sweeps): "hemm" or "update" keeps only that product on the tensor cores
         const char* w = std::getenv("BSE_TC");
         const std::string tw = w ? w : "both";

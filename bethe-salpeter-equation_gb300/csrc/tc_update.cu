@@ -18,24 +18,34 @@
 //   hemm   (A22 Hermitian: row i of A22 = conj(column i), and column i is contiguous):
 //          Re Y[i,p] = col_i . V_p,   Im Y[i,p] = col_i . V'_p     (K = 2m reals, (re, im) of each j)
 //          with V_p the p-th column of V as 2m reals and V'_p = (Im V, -Re V) per element.
-//          MMA: M = 128 columns i of A22 (TMA-loaded straight from the matrix, split in shared
-//          memory), N = 64 = [V_0..V_31 | V'_0..V'_31] (prepared and split in global memory),
-//          K in 32-real blocks;
-//          the K range is split over CTAs when there are few column tiles, with partial sums
-//          added in a fixed order (bit-reproducible).
+//          MMA: M = 128 columns i of A22 (TMA-loaded in FP32 straight from the matrix, split in
+//          shared memory), N = 64 = [V_0..V_31 | V'_0..V'_31] (prepared and split in global
+//          memory), K in 32-real blocks.  Persistent stream-K: the (column tile, K block) units
+//          are dealt evenly to one CTA per SM; partial sums end at tile boundaries and are added
+//          per tile in CTA order (bit-reproducible).
 //   update: Re (L R^H)[i,j] = Lrow_i . Rrow_j,   Im = Lrow_i . (i R)row_j   (K = 2 * 2kk = 128 reals)
-//          MMA: M = 128 rows i (L row-major), N = 128 = [64 rows of R | the same 64 rows of iR],
-//          so one accumulator holds the real parts (columns 0..63) and the imaginary parts
-//          (64..127) of a 128 x 64 complex tile; L and R are TMA-loaded in FP32 and split in
-//          shared memory, iR formed there from R.  The tile of A22 is loaded by TMA into shared
-//          memory while the operands stream in, the accumulator is subtracted in place and the
-//          tile goes back by a TMA store.
+//          MMA: M = 128 rows i (L), N = 64 = [32 rows of R | the same 32 rows of iR], so one
+//          accumulator holds the real parts (columns 0..31) and the imaginary parts (32..63) of a
+//          128 x 32 complex tile.  L, R and iR are split into BF16 parts in global memory by a
+//          small kernel.  Persistent: one CTA per SM walks its share of the tiles in row-strip
+//          order with the strip's L resident; the A22 tiles come in and go back by TMA,
+//          double-buffered together with the accumulators, so the transfers of one tile overlap
+//          the MMAs of the next.
 //
-// Roles (192 threads): warp 0 issues the TMA loads (one elected thread), warp 1 allocates the
-// tensor memory and issues the MMAs (one elected thread), warps 2-5 split the FP32 operands in
-// shared memory and run the epilogue (tensor memory -> registers; warp w reads lanes 32 (w % 4)).
-// Stages are handed over through mbarriers; every wait is bounded: after kWaitPolls failed polls
-// the waiting thread raises the error word and the CTA drains and returns (no hang).
+// Accumulation: the tensor pipe's FP32 accumulation truncates.  The x0 y0 products and the five
+// smaller ones go to separate accumulators, and the hemm restarts its accumulators every 128 K
+// and adds the finished chains in FP32 registers, so the error stays that of an FP32 product
+// (no drift with K).
+//
+// Roles (320 threads): warp 0 issues the TMA loads (one elected thread), warp 1 allocates the
+// tensor memory and issues the MMAs (one elected thread), warps 2-9 split the FP32 operands in
+// shared memory and run the epilogue (tensor memory -> registers; warp w reads lanes 32 (w % 4),
+// two warps per lane quarter, each with half of the accumulator columns).  Stages are handed over
+// through mbarriers; every wait is bounded: after kWaitPolls failed polls the waiting thread
+// raises the error word and the CTA drains and returns (no hang).
+//
+// TMA works in 16-byte granules of the 2m-real columns, so the order m must be even (every
+// trailing order of the reduction is, for even n).
 //
 // The reference computes the whole eigendecomposition with LAPACK zheevd (bse.version13.cpp:3195,
 // 3204, 3330); these products are the BLAS-3 part of its Householder reduction, restated as a
@@ -418,8 +428,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         int chain_tile[2] = {0, 0}, chain_last[2] = {0, 0};
         auto drain = [&]() {
             const int cc = drained, b = cc & 1;
-            if (!mbar_wait(tfull + b, (uint32_t)(cc / 2) & 1u, &s_abort, h.err)) ok = false;
-            __syncwarp();
+            const bool got = mbar_wait(tfull + b, (uint32_t)(cc / 2) & 1u, &s_abort, h.err);
+            ok = __all_sync(0xffffffffu, got) && ok;   // warp-uniform: the tensor-memory loads need all lanes
             tc_fence_after();
             float v[64];   // big 0..15, big 16..31, small 0..15, small 16..31 of this warp's columns
             const uint32_t tb = tq + (uint32_t)(128 * b);
@@ -445,7 +455,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int64_t u = u0 + j;
             const int s = j % kHemmRing, ps = j % kHemmParts;
             const uint32_t ph = (uint32_t)(j / kHemmRing) & 1u, pph = (uint32_t)(j / kHemmParts) & 1u;
-            if (!mbar_wait(rfull + s, ph, &s_abort, h.err) || !mbar_wait(pempty + ps, pph ^ 1u, &s_abort, h.err)) {
+            const bool got = mbar_wait(rfull + s, ph, &s_abort, h.err) && mbar_wait(pempty + ps, pph ^ 1u, &s_abort, h.err);
+            if (!__all_sync(0xffffffffu, got)) {
                 ok = false;
                 break;
             }
@@ -654,9 +665,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(16 * half);
         for (int j = 0; j < nt; j++) {
             const int b = j & 1;
-            const bool ok = mbar_wait(tfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err) &&
-                            mbar_wait(cfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err);
-            __syncwarp();
+            bool ok = mbar_wait(tfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err) &&
+                      mbar_wait(cfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err);
+            ok = __all_sync(0xffffffffu, ok);   // the warp stays converged for the tensor-memory loads
             tc_fence_after();
             float* C = Cs(b);
             float v[64];   // big Re, big Im, small Re, small Im of this warp's 16 columns

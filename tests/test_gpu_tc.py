@@ -111,15 +111,18 @@ def test_tc_hemm_no_accumulation_bias(gpu, m):
     assert np.abs(rel).max() < 1e-6, np.abs(rel).max()
 
 
-@pytest.mark.parametrize("tc", ["both", "hemm", "update"])
+@pytest.mark.parametrize("tc", ["both", "hemm", "update", "cublas"])
 def test_two_stage_with_tensor_core_products(synth, oracle, gpu, monkeypatch, tc):
-    """The two-stage reduction with its trailing-update products on the tensor cores
-    (BSE_BAND_UPDATE=tc; BSE_TC selects both or one of them), mixed precision, orb8 12x12
-    (N_BSE = 2304): every eigenvalue within the FP32 class 1e-6 * ||H||_2 of the FP64 oracle,
-    the refined lowest 64 within 1e-6 eV, eps2 within 1e-4."""
+    """The two-stage reduction with its trailing-update products on the tensor cores (the
+    default; BSE_TC selects both or one of them) or on cuBLAS (BSE_BAND_UPDATE=cublas), mixed
+    precision, orb8 12x12 (N_BSE = 2304): every eigenvalue within the FP32 class 1e-6 * ||H||_2
+    of the FP64 oracle, the refined lowest 64 within 1e-6 eV, eps2 within 1e-4."""
     monkeypatch.setenv("BSE_TRIDIAG_MODE", "twostage")
-    monkeypatch.setenv("BSE_BAND_UPDATE", "tc")
-    monkeypatch.setenv("BSE_TC", tc)
+    if tc == "cublas":
+        monkeypatch.setenv("BSE_BAND_UPDATE", "cublas")
+    else:
+        monkeypatch.setenv("BSE_BAND_UPDATE", "tc")
+        monkeypatch.setenv("BSE_TC", tc)
     omega = np.arange(2000) * 8.0 / 2000
     prob = synth.orb8_problem(grid=12)
     ref = oracle.solve(prob, omega, 0.05)
