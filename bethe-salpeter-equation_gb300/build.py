@@ -6,6 +6,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -35,8 +36,21 @@ def _stale(obj, deps):
     return not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(d) for d in deps)
 
 
+def _host_stamp(cc: str) -> str:
+    """Machine and compiler the objects were built for: a tree built elsewhere (another CPU
+    architecture, another toolkit) is rebuilt from scratch rather than trusted by mtime."""
+    r = subprocess.run([cc, "--version"], capture_output=True, text=True)
+    return platform.machine() + "\n" + r.stdout.strip().splitlines()[-1] + "\n"
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
+    stamp_path = os.path.join(OUT, "host.txt")
+    stamp = _host_stamp(nvcc())
+    try:
+        force = force or open(stamp_path).read() != stamp
+    except OSError:
+        force = True
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
     headers.append(os.path.join(INCLUDE, "bse_gpu.h"))
     srcs = sources()
@@ -61,6 +75,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         tmp = LIB + ".tmp"
         run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcublas", "-lcusolver", "-lcudart", "-Xlinker", "--no-undefined"])
         os.replace(tmp, LIB)
+    with open(stamp_path, "w") as f:
+        f.write(stamp)
     return LIB
 
 

@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(ChaseArgs<T2> a) {
                     unsigned it = 0;
                     while (*vp < need) {
                         if (*verr != 0) break;
-                        if (++it > kSpinLimit) {
+                        if (++it > spin_limit(a.err)) {
                             atomicExch(a.err, 2);
                             break;
                         }

@@ -20,14 +20,14 @@ __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -
 __device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
 
 // Cyclic Jacobi on the n x n Hermitian matrix A (column-major, destroyed), eigenvectors in V.
-// Returns the number of sweeps used, or -1 when the 60-sweep cap is hit.
+// Returns the number of sweeps used, or -1 when the cap of max_sweeps (60) is hit.
 template <int NW>
-__device__ int jacobi_herm(int n, double2* A, double2* V) {
+__device__ int jacobi_herm(int n, double2* A, double2* V, int max_sweeps) {
     for (int i = 0; i < n * n; i++) V[i] = make_double2(0, 0);
     for (int i = 0; i < n; i++) V[i + i * n] = make_double2(1, 0);
     double fro = 0;
     for (int i = 0; i < n * n; i++) fro += cabs2(A[i]);
-    for (int sweep = 0; sweep < 60; sweep++) {
+    for (int sweep = 0; sweep < max_sweeps; sweep++) {
         double off = 0;
         for (int q = 0; q < n; q++)
             for (int p = 0; p < q; p++) off += cabs2(A[p + q * n]);
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(64) band_subset_kernel(
     const double2* __restrict__ hr, const double* __restrict__ kcart,
     double q0, double q1, double q2, double ef, double scissor,
     double* __restrict__ ec, double* __restrict__ ev,
-    double2* __restrict__ cc, double2* __restrict__ cv, int* __restrict__ status) {
+    double2* __restrict__ cc, double2* __restrict__ cv, int* __restrict__ status, int max_sweeps) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 2 * nk) return;
     const int k = t >> 1, which = t & 1;     // 0: conduction bands at k; 1: valence at k - q
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(64) band_subset_kernel(
                 A[i].y += wr * (hv.y * cs + hv.x * sn);
             }
         }
-        int sw = jacobi_herm<NW>(nw, A, V);
+        int sw = jacobi_herm<NW>(nw, A, V, max_sweeps);
         if (sw < 0) { atomicMin(status, (int)BSE_ERR_NOT_CONVERGED); return; }
         // ascending order (stable), unit columns, gauge
         int ord[NW];
@@ -154,7 +154,7 @@ void launch_bands(bse_ctx* c, const double* q, double* ec, double* ev, double2* 
     const int threads = 64, blocks = (2 * c->nk + threads - 1) / threads;
     band_subset_kernel<NW><<<blocks, threads, 0, c->stream>>>(
         c->nk, c->nw, c->ns, c->nr, c->nv, c->nc, c->d_rcart, c->d_weights, c->d_hr, c->d_k,
-        q[0], q[1], q[2], c->p.fermi_energy, c->p.scissor, ec, ev, cc, cv, c->d_status);
+        q[0], q[1], q[2], c->p.fermi_energy, c->p.scissor, ec, ev, cc, cv, c->d_status, c->jacobi_sweeps);
     c->launches++;
 }
 

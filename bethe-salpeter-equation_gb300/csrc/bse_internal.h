@@ -130,6 +130,11 @@ struct bse_ctx {
         double bytes = 0, flops = 0;
     };
     int build_k_lo = 0, build_k_hi = 0;   // k tile of the next build (rows k1 in [lo, hi)); hi = 0: all
+    // test overrides read at bse_create: the polling limit of the solver's bounded waits
+    // (BSE_TEST_SPIN_LIMIT, 0 = the built-in limit) and the H(k) Jacobi sweep cap
+    // (BSE_TEST_JACOBI_SWEEPS, default 60)
+    unsigned spin_limit = 0;
+    int jacobi_sweeps = 60;
     bool ktime = false;
     std::vector<KernelTime> kt;
     size_t kt_used = 0;

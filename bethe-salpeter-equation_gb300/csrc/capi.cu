@@ -380,6 +380,8 @@ int bse_create(const bse_model* m, const bse_params* p, bse_ctx** out) {
     CK(cuda_check(c, cudaEventCreateWithFlags(&c->ev_h64, cudaEventDisableTiming), "event"));
     for (auto& e : c->ev) CK(cuda_check(c, cudaEventCreate(&e), "event"));
     c->ktime = std::getenv("BSE_KERNEL_TIMING") != nullptr;
+    if (const char* v = std::getenv("BSE_TEST_SPIN_LIMIT")) c->spin_limit = (unsigned)std::max(1L, std::atol(v));
+    if (const char* v = std::getenv("BSE_TEST_JACOBI_SWEEPS")) c->jacobi_sweeps = std::max(0, std::atoi(v));
     if (cublasCreate(&c->cublas) != CUBLAS_STATUS_SUCCESS) CK(fail(c, BSE_ERR_CUDA, "cublasCreate"));
     if (cusolverDnCreate(&c->cusolver) != CUSOLVER_STATUS_SUCCESS) CK(fail(c, BSE_ERR_CUDA, "cusolverDnCreate"));
     cublasSetStream(c->cublas, c->stream);

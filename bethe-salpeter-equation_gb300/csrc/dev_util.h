@@ -35,6 +35,14 @@ template <typename T2> __device__ __forceinline__ T2 cinv(T2 a) {
 
 constexpr unsigned kSpinLimit = 1u << 26;   // ~seconds of polling before a barrier gives up
 
+// The polling limit of the waits that report through the error word err[0]: err[1] when it is
+// nonzero (a test override, BSE_TEST_SPIN_LIMIT at bse_create), else kSpinLimit.  The solver's
+// error word always has the second int beside it.
+__device__ __forceinline__ unsigned spin_limit(const int* err) {
+    const unsigned v = reinterpret_cast<const volatile unsigned*>(err)[1];
+    return v ? v : kSpinLimit;
+}
+
 // Grid-wide barrier for a cooperative launch.  bar[0] holds the arrivals of the current
 // barrier in its low 16 bits and a generation number in its high 16 bits: each block adds 1
 // (acquire-release, so its writes are published and the earlier arrivals' are seen); the last
@@ -63,6 +71,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
+        const unsigned lim = spin_limit(err);
         const unsigned old = atom_add_acq_rel(bar, 1u);
         const unsigned gen = old >> 16;
         if ((old & 0xffffu) == gridDim.x - 1) {
@@ -72,7 +81,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
             while ((ld_acquire(bar) >> 16) == gen) {
                 if ((++it & 255u) == 0) {
                     if (*(volatile int*)err != 0) { ok = 0; break; }
-                    if (it > kSpinLimit) { atomicExch(err, 1); ok = 0; break; }
+                    if (it > lim) { atomicExch(err, 1); ok = 0; break; }
                     __nanosleep(64);
                 }
             }
@@ -100,6 +109,7 @@ template <bool WIDE>
 __device__ __forceinline__ bool flag_barrier(unsigned* flags, unsigned epoch, int* err, int* s_fail) {
     __syncthreads();
     if (threadIdx.x == 0) st_release(flags + 32 * blockIdx.x, epoch);
+    const unsigned lim = spin_limit(err);
     if (WIDE) {
         for (unsigned t = threadIdx.x; t < gridDim.x; t += blockDim.x) {
             const unsigned* f = flags + 32 * t;
@@ -107,7 +117,7 @@ __device__ __forceinline__ bool flag_barrier(unsigned* flags, unsigned epoch, in
             while ((int)(ld_acquire(f) - epoch) < 0) {
                 if ((++it & 255u) == 0) {
                     if (*(volatile int*)err != 0) { *s_fail = 1; break; }
-                    if (it > kSpinLimit) { atomicExch(err, 1); *s_fail = 1; break; }
+                    if (it > lim) { atomicExch(err, 1); *s_fail = 1; break; }
                     __nanosleep(64);
                 }
             }
@@ -126,7 +136,7 @@ __device__ __forceinline__ bool flag_barrier(unsigned* flags, unsigned epoch, in
             if (__all_sync(0xffffffffu, pending == 0)) break;
             if ((++it & 63u) == 0) {
                 int bad = *(volatile int*)err != 0;
-                if (it > kSpinLimit) {
+                if (it > lim) {
                     if (lane == 0) atomicExch(err, 1);
                     bad = 1;
                 }

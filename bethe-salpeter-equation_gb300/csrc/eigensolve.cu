@@ -999,6 +999,11 @@ int mixed_coupled_block(bse_ctx* c, int64_t n, double2* M64, float2* L, float2* 
     return cuda_check(c, cudaGetLastError(), "mixed coupled refinement");
 }
 
+// collinear full BSE: the two 4N x 4N blocks are solved in turn and each must be positive
+// definite; an error names the block (rows of the 8N matrix in the reference's layout)
+constexpr const char* kBlockM0 = "collinear full BSE, spin-flip block M0 (exciton spin blocks 1, 2: rows N..3N-1 and 5N..7N-1): ";
+constexpr const char* kBlockM1 = "collinear full BSE, optically active block M1 (exciton spin blocks 0, 3: rows 0..N-1, 3N..5N-1, 7N..8N-1): ";
+
 int run_eig_coupled_mixed(bse_ctx* c) {
     int st;
     const double2* rho0 = c->d_rho + (size_t)c->n_rho * (c->ng / 2);
@@ -1015,8 +1020,12 @@ int run_eig_coupled_mixed(bse_ctx* c) {
     double2* M0 = (double2*)c->d_blk;
     double2* M1 = M0 + n4 * n4;
     float2* L = (float2*)(M1 + n4 * n4);
-    if ((st = mixed_coupled_block(c, n4, M0, L, L + n4 * n4, nullptr, c->d_E, nullptr))) return st;
-    return mixed_coupled_block(c, n4, M1, L, L + n4 * n4, rho0, c->d_E + n4, c->d_f);
+    if ((st = mixed_coupled_block(c, n4, M0, L, L + n4 * n4, nullptr, c->d_E, nullptr))) {
+        c->err = std::string(kBlockM0) + c->err;
+        return st;
+    }
+    if ((st = mixed_coupled_block(c, n4, M1, L, L + n4 * n4, rho0, c->d_E + n4, c->d_f))) c->err = std::string(kBlockM1) + c->err;
+    return st;
 }
 
 int run_eig_coupled(bse_ctx* c, bool want_vectors) {
@@ -1039,8 +1048,14 @@ int run_eig_coupled(bse_ctx* c, bool want_vectors) {
     double2* M0 = (double2*)c->d_blk;
     double2* M1 = M0 + n4 * n4;
     double2* W = M1 + n4 * n4;
-    if ((st = solve_coupled_block(c, n4, M0, W, nullptr, c->d_E, nullptr, false))) return st;
-    if ((st = solve_coupled_block(c, n4, M1, W, rho0, c->d_E + n4, c->d_f, want_vectors))) return st;
+    if ((st = solve_coupled_block(c, n4, M0, W, nullptr, c->d_E, nullptr, false))) {
+        c->err = std::string(kBlockM0) + c->err;
+        return st;
+    }
+    if ((st = solve_coupled_block(c, n4, M1, W, rho0, c->d_E + n4, c->d_f, want_vectors))) {
+        c->err = std::string(kBlockM1) + c->err;
+        return st;
+    }
     c->d_A = W;
     return BSE_OK;
 }

@@ -1,19 +1,22 @@
 // Allocation-free evaluation of the dielectric function from eigenvalues and oscillator
 // strengths (no counterpart in the reference).
 //
-// Some callers cannot call cudaMalloc: code embedded in a framework that has already
-// reserved the device memory for its own pool (a JAX/XLA preallocation, a PyTorch caching
-// allocator at its limit), or a pipeline that must not synchronise the device -- cudaMalloc
-// and cudaFree can synchronise.  bse_eps_noalloc serves them: it stages its inputs and
-// outputs in one file-scope device array of fixed size instead of allocating.
+// Some callers cannot call cudaMalloc: code embedded in a framework that has already reserved
+// the device memory for its own pool (a JAX/XLA preallocation, a PyTorch caching allocator at its
+// limit) gets no memory from the CUDA allocator, however small the request.  bse_eps_noalloc
+// serves them: it stages its inputs and outputs in one file-scope device array of fixed size
+// instead of allocating.
 //
 //   - Limits: n_exc <= BSE_EPS_NOALLOC_MAX_EXCITONS (131072) and
 //     n_omega <= BSE_EPS_NOALLOC_MAX_OMEGA (16384); larger requests return
 //     BSE_ERR_BAD_INPUT.  The array is 3.4 MiB, and every GPU that loads this library
 //     holds it until the process exits.
 //   - Set-up: the first call on a device, with that device current, resolves the array's
-//     device address (cudaGetSymbolAddress); make that first call before any stream
-//     capture.
+//     device address (cudaGetSymbolAddress) and keeps it for the rest of the process; make that
+//     first call before any stream capture.  A cudaDeviceReset reloads the module and leaves
+//     the kept address stale: do not call this entry point again after resetting the device.
+//   - Each call copies its inputs to the array, runs the kernel and copies the outputs back on
+//     `stream`, and returns once the outputs are on the host (it waits for the stream).
 //   - Sharing: every call uses the same array, which keeps the last call's contents.
 //     Every output element is written by the kernel, so nothing has to start at zero.
 //     Calls that overlap on the GPU (other streams, other host threads) race on the

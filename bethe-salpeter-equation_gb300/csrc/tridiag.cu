@@ -1688,6 +1688,10 @@ int own_heevd_t(bse_ctx* c, int n, T2* A, int64_t lda, double* dW, int n_vec, co
     unsigned* flags = (unsigned*)(w + o_flags);
     int* err = (int*)(w + o_bar + 16);
     if ((st = cuda_check(c, cudaMemsetAsync(bar, 0, 64, c->stream), "barrier reset"))) return st;
+    if (c->spin_limit &&
+        (st = cuda_check(c, cudaMemcpyAsync(err + 1, &c->spin_limit, sizeof(unsigned), cudaMemcpyHostToDevice, c->stream),
+                         "polling limit")))
+        return st;
     if ((st = cuda_check(c, cudaMemsetAsync(flags, 0, (size_t)B * 128, c->stream), "barrier flags reset"))) return st;
     if ((st = cuda_check(c, cudaMemsetAsync(w + o_v, 0, nbuf * n * sizeof(T2), c->stream), "v reset"))) return st;
     if ((st = cuda_check(c, cudaMemsetAsync(w + o_p, 0, nbuf * n * sizeof(T2), c->stream), "p reset"))) return st;

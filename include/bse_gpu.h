@@ -214,14 +214,16 @@ int bse_solve_many(bse_ctx** ctxs, int32_t n_ctx, const double* omega, int32_t n
 int bse_stage_times(const bse_ctx* ctx, double* ms, int32_t n);
 
 /* Allocation-free dielectric function (no counterpart in the reference).  For callers that
- * cannot call cudaMalloc -- a framework that has reserved the device memory for its own pool,
- * or a pipeline that must not synchronise the device (cudaMalloc/cudaFree can) -- this computes
+ * cannot call cudaMalloc -- code inside a framework that has reserved the device memory for its
+ * own pool gets nothing from the CUDA allocator -- this computes
  * eps(w) = 1 - prefactor * sum_l |f_l|^2 / (w - e_l + i gamma) from HOST arrays e[n_exc],
  * f[n_exc] (complex128) and omega[n_omega] into eps2/eps1 (host, either nullable), staging them
  * in one fixed 3.4 MiB file-scope device array that every GPU loading the library keeps until
  * exit.  Limits below; larger sizes return BSE_ERR_BAD_INPUT.  The first call on a device
- * resolves the array's address: make it before any stream capture.  Calls share the array:
- * calls that overlap on the GPU race.  stream: a cudaStream_t, or NULL for the default stream.
+ * resolves the array's address and keeps it for the process (not valid across a
+ * cudaDeviceReset): make that first call before any stream capture.  Each call returns once its
+ * outputs are on the host (it waits for `stream`).  Calls share the array: calls that overlap on
+ * the GPU race.  stream: a cudaStream_t, or NULL for the default stream.
  * prefactor is F = conv / (V nk) of bse_eps.  The Tamm-Dancoff form: a full-BSE spectrum (signed
  * anti-resonant pairs) goes through bse_eps. */
 #define BSE_EPS_NOALLOC_MAX_EXCITONS 131072
