@@ -37,7 +37,8 @@ constexpr unsigned kSpinLimit = 1u << 26;   // ~seconds of polling before a barr
 
 // The polling limit of the waits that report through the error word err[0]: err[1] when it is
 // nonzero (a test override, BSE_TEST_SPIN_LIMIT at bse_create), else kSpinLimit.  The solver's
-// error word always has the second int beside it.
+// error word always has the second int beside it.  The waits check the error word every few
+// hundred polls, and at once when a poll count passes the limit.
 __device__ __forceinline__ unsigned spin_limit(const int* err) {
     const unsigned v = reinterpret_cast<const volatile unsigned*>(err)[1];
     return v ? v : kSpinLimit;
@@ -79,7 +80,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
         } else {
             unsigned it = 0;
             while ((ld_acquire(bar) >> 16) == gen) {
-                if ((++it & 255u) == 0) {
+                if ((++it & 255u) == 0 || it > lim) {
                     if (*(volatile int*)err != 0) { ok = 0; break; }
                     if (it > lim) { atomicExch(err, 1); ok = 0; break; }
                     __nanosleep(64);
@@ -115,7 +116,7 @@ __device__ __forceinline__ bool flag_barrier(unsigned* flags, unsigned epoch, in
             const unsigned* f = flags + 32 * t;
             unsigned it = 0;
             while ((int)(ld_acquire(f) - epoch) < 0) {
-                if ((++it & 255u) == 0) {
+                if ((++it & 255u) == 0 || it > lim) {
                     if (*(volatile int*)err != 0) { *s_fail = 1; break; }
                     if (it > lim) { atomicExch(err, 1); *s_fail = 1; break; }
                     __nanosleep(64);
@@ -134,7 +135,7 @@ __device__ __forceinline__ bool flag_barrier(unsigned* flags, unsigned epoch, in
                     if ((int)(ld_acquire(flags + 32 * (lane + 32 * q)) - epoch) < 0) still |= 1u << q;
             pending = still;
             if (__all_sync(0xffffffffu, pending == 0)) break;
-            if ((++it & 63u) == 0) {
+            if ((++it & 63u) == 0 || it > lim) {
                 int bad = *(volatile int*)err != 0;
                 if (it > lim) {
                     if (lane == 0) atomicExch(err, 1);
