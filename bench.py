@@ -41,6 +41,8 @@ WORKLOAD = "orb8_48x48_4v4c"          # N_BSE = 36864
 WORKLOAD_SMALL = "magnetic4_24x24_2v2c"  # N_BSE = 2304
 METRIC = "BSE build+diag wall time and eps2 grad time at N_BSE; error vs FP64"
 FP64_LARGE_PROFILE = os.path.join(ROOT, "profiles", "fp64_vs_mixed_orb8_48x48.md")
+# DRAM traffic / algorithmic bytes of tc_update_kernel, one ncu-captured launch at m = 8192
+UPD_TRAFFIC_RATIO = (609.853952 + 478.409216) / (16 * 8192 ** 2 / 1e6)
 
 
 def _dist_env():
@@ -334,7 +336,11 @@ def run_gpu(args):
         tflops = 6.0 * upd_flops / (upd_ms * 1e-3) / 1e12
         roof = {"kernel": "tc_update_kernel (tcgen05 kind::f16, TMA)", "bound": "hbm", "achieved": gbs, "peak": hbm,
                 "peak_source": src, "unit": "GB/s", "frac": gbs / hbm,
-                "traffic": None, "alg_bytes_per_launch": upd_bytes / upd_n, "avg_launch_ms": upd_ms / upd_n,
+                "traffic": UPD_TRAFFIC_RATIO * upd_bytes / upd_n,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at m = 8192 "
+                                  "(profiles/tc_update_hemm_kernels_m8192.md): 1.014 x the algorithmic bytes, "
+                                  "scaled to the average launch here (traffic grows with the 16 m^2 bytes)",
+                "alg_bytes_per_launch": upd_bytes / upd_n, "avg_launch_ms": upd_ms / upd_n,
                 "launches_per_solve": upd_n / args.steps,
                 "alg_bytes_unit": "16 m^2 per launch: the m x m complex64 trailing matrix read and written once",
                 "tensor": {"achieved": tflops, "peak": bf16, "unit": "TFLOP/s", "frac": tflops / bf16,
