@@ -63,8 +63,13 @@
 namespace bse {
 namespace tc {
 
-constexpr int kThreads = 320;                 // warp 0 TMA, warp 1 MMA, warps 2-9 workers
-constexpr int kWorkers = kThreads - 64;       // two warps per tensor-memory lane quarter
+// warp 0 issues the TMA loads, warp 1 the MMAs; the workers follow.  hemm: 16 worker warps (four
+// per tensor-memory lane quarter) convert the streamed A22 blocks and drain the accumulators;
+// update: 8 worker warps (warps 2-9) and warp 10, which loads the A22 tiles
+constexpr int kHemmWorkers = 512;
+constexpr int kHemmThreads = 64 + kHemmWorkers;
+constexpr int kWorkers = 256;
+constexpr int kUpdThreads = 64 + kWorkers + 32;
 constexpr int kRows = 128;                 // MMA M: accumulator lanes
 constexpr int kKb = 32;                    // K elements per block: 128 bytes of FP32, 64 of BF16
 constexpr uint32_t kWaitPolls = 1u << 22;  // try_wait polls before a wait gives up
@@ -79,15 +84,21 @@ constexpr uint32_t kHemmRaw = kRows * kKb * 4, kHemmA = kRows * kKb * 2, kHemmB 
 constexpr uint32_t kHemmSlot = kHemmRaw + 3 * kHemmB, kHemmPartSlot = 3 * kHemmA;
 constexpr size_t kHemmSmem = (size_t)kHemmRing * kHemmSlot + (size_t)kHemmParts * kHemmPartSlot + 1024 + 512;
 // update (persistent, row strips): the strip's L parts resident (4 K blocks x 3 parts x 8 KB),
-// two C tiles of 128 rows x kUpdCols complex columns, a ring of B slots per K block (3 parts x
-// [kUpdCols rows of R | kUpdCols rows of iR] x 64 bytes)
+// kUpdCbuf C tiles of 128 rows x kUpdCols complex columns in flight, a ring of B slots per K block
+// (3 parts x [kUpdCols rows of R | kUpdCols rows of iR] x 64 bytes), kUpdAcc accumulator pairs
 constexpr int kUpdCols = 32;                               // complex columns per tile
+constexpr int kUpdCbuf = 2;
+constexpr int kUpdAcc = 2;
 constexpr int kUpdRing = 4;
 constexpr uint32_t kUpdL = 4 * 3 * kRows * kKb * 2;        // 96 KB
-constexpr uint32_t kUpdC = kRows * 2 * kUpdCols * 4;       // 128 rows (256 reals) x 32 columns
+constexpr uint32_t kUpdC = kRows * 2 * kUpdCols * 4;       // 128 rows (256 reals) x kUpdCols columns
 constexpr uint32_t kUpdBpart = 2 * kUpdCols * kKb * 2;     // R rows then iR rows, one part
 constexpr uint32_t kUpdBslot = 3 * kUpdBpart;
-constexpr size_t kUpdSmem = (size_t)kUpdL + 2 * (size_t)kUpdC + (size_t)kUpdRing * kUpdBslot + 1024 + 512;
+constexpr uint32_t kUpdAccCols = 256;                      // per accumulator: 3 groups x (Re | Im) x kUpdCols
+constexpr size_t kUpdSmem = (size_t)kUpdL + (size_t)kUpdCbuf * kUpdC + (size_t)kUpdRing * kUpdBslot + 1024 + 512;
+constexpr uint32_t kTmemCols = 512;                        // two accumulators of 3 x 64 columns, 256 apart
+static_assert(kUpdAcc * kUpdAccCols <= kTmemCols && 6 * kUpdCols <= (int)kUpdAccCols, "update accumulators");
+static_assert(kUpdBpart == 2 * kUpdCols * 64 && kHemmB == 64 * 64, "B parts back to back (NB rows of 64 bytes)");
 static_assert(kHemmSmem <= 232448 && kUpdSmem <= 232448, "shared memory per CTA");
 static_assert(kHemmSlot % 1024 == 0 && kHemmPartSlot % 1024 == 0 && kUpdC % 1024 == 0 && kUpdBslot % 1024 == 0 &&
                   kUpdL % 1024 == 0 && kUpdBpart % 512 == 0,
@@ -107,6 +118,11 @@ __device__ __forceinline__ void mbar_arrive_tx(uint64_t* b, uint32_t bytes) {
 }
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
+}
+// one arrival per warp, after every lane's preceding work (the barrier counts warps)
+__device__ __forceinline__ void mbar_arrive_warp(uint64_t* b) {
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(b);
 }
 __device__ __forceinline__ bool mbar_test(uint64_t* b, uint32_t parity) {
     uint32_t done;
@@ -158,6 +174,8 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 __device__ __forceinline__ void tma_store_drain() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// every bulk store group of this thread has completed (its writes performed)
+__device__ __forceinline__ void tma_store_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void prefetch_map(const CUtensorMap* m) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
@@ -186,28 +204,39 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar)) : "memory");
 }
-// 16 consecutive 32-bit columns of this thread's tensor-memory lane at each of four addresses,
-// one wait for all four loads
-__device__ __forceinline__ void tmem_ld4x16(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, float (&v)[64]) {
-    uint32_t r[64];
+// 16 consecutive 32-bit columns of this thread's tensor-memory lane at each of 3 addresses,
+// one wait for all the loads
+__device__ __forceinline__ void tmem_ld3x16(uint32_t a0, uint32_t a1, uint32_t a2, float (&v)[48]) {
+    uint32_t r[48];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%64];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%65];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47}, [%66];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%67];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%48];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%49];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47}, [%50];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]),
-          "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]),
-          "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
-          "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
-          "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3)
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47])
+        : "r"(a0), "r"(a1), "r"(a2)
         : "memory");
 #pragma unroll
-    for (int i = 0; i < 64; i++) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 48; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// 16 consecutive 32-bit columns of this thread's tensor-memory lane at each of 6 addresses,
+// one wait for all the loads
+__device__ __forceinline__ void tmem_ld6x16(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t a4, uint32_t a5, float (&v)[96]) {
+    uint32_t r[96];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%96];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%97];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47}, [%98];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%99];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%64, %65, %66, %67, %68, %69, %70, %71, %72, %73, %74, %75, %76, %77, %78, %79}, [%100];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%80, %81, %82, %83, %84, %85, %86, %87, %88, %89, %90, %91, %92, %93, %94, %95}, [%101];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63]), "=r"(r[64]), "=r"(r[65]), "=r"(r[66]), "=r"(r[67]), "=r"(r[68]), "=r"(r[69]), "=r"(r[70]), "=r"(r[71]), "=r"(r[72]), "=r"(r[73]), "=r"(r[74]), "=r"(r[75]), "=r"(r[76]), "=r"(r[77]), "=r"(r[78]), "=r"(r[79]), "=r"(r[80]), "=r"(r[81]), "=r"(r[82]), "=r"(r[83]), "=r"(r[84]), "=r"(r[85]), "=r"(r[86]), "=r"(r[87]), "=r"(r[88]), "=r"(r[89]), "=r"(r[90]), "=r"(r[91]), "=r"(r[92]), "=r"(r[93]), "=r"(r[94]), "=r"(r[95])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(a4), "r"(a5)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 96; i++) v[i] = __uint_as_float(r[i]);
 }
 
 // Shared-memory matrix descriptor of a K-major BF16 block in the 64-byte swizzled layout (rows of
@@ -226,23 +255,24 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// The six BF16 products of one 32-element K block (two MMAs of K = 16 each) of A = a0 + a1 + a2
-// and B = b0 + b1 + b2: a0 b0 into the "big" accumulator, the five smaller terms a0 b1, a1 b0,
-// a0 b2, a2 b0, a1 b1 into the "small" one.  The tensor pipe's FP32 accumulation truncates, and
-// with the small terms kept apart their truncation is relative to their own size; the epilogue
-// adds the two in FP32.
-__device__ __forceinline__ void mma_block6(uint32_t t_big, uint32_t t_small, const unsigned char* a0, uint32_t a_stride,
-                                           const unsigned char* b0, uint32_t b_stride, uint32_t idesc, bool first) {
-    constexpr int pa[6] = {0, 0, 1, 0, 2, 1}, pb[6] = {0, 1, 0, 2, 0, 1};
+// The six BF16 products of one 32-element K block (two K = 16 steps) of A = a0 + a1 + a2 and
+// B = b0 + b1 + b2, in three MMAs per step: the B parts lie one after the other (NB rows each, the
+// same 64-byte swizzled layout), so a0 [b0 b1 b2] writes columns [0, 3 NB) of t, a1 [b0 b1] adds to
+// [NB, 3 NB) and a2 b0 to [NB, 2 NB).  Columns [0, NB) hold a0 b0 ("big"), [NB, 2 NB) a0 b1 + a1 b0
+// + a2 b0, [2 NB, 3 NB) a0 b2 + a1 b1.  The tensor pipe's FP32 accumulation truncates: with the
+// smaller terms kept apart from a0 b0 their truncation is relative to their own size; the epilogue
+// adds the three groups in FP32.  Reading each A part once per step (instead of once per product)
+// cuts the shared-memory operand traffic from 36 KB to 24 KB per step at NB = 64.
+template <int NB>
+__device__ __forceinline__ void mma_block_cat(uint32_t t, const unsigned char* a0, uint32_t a_stride,
+                                              const unsigned char* b0, bool first) {
+    constexpr uint32_t i3 = idesc_bf16(kRows, 3 * NB), i2 = idesc_bf16(kRows, 2 * NB), i1 = idesc_bf16(kRows, NB);
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-#pragma unroll
-        for (int q = 0; q < 6; q++) {
-            const uint64_t ad = desc_sw64(a0 + pa[q] * a_stride) + (uint64_t)(k * 2);   // +32 bytes per K step
-            const uint64_t bd = desc_sw64(b0 + pb[q] * b_stride) + (uint64_t)(k * 2);
-            const bool init = first && k == 0 && (q == 0 || q == 1);
-            mma_bf16(q == 0 ? t_big : t_small, ad, bd, idesc, init ? 0u : 1u);
-        }
+        const uint64_t bd = desc_sw64(b0) + (uint64_t)(k * 2);   // +32 bytes per K step
+        mma_bf16(t, desc_sw64(a0) + (uint64_t)(k * 2), bd, i3, (first && k == 0) ? 0u : 1u);
+        mma_bf16(t + NB, desc_sw64(a0 + a_stride) + (uint64_t)(k * 2), bd, i2, 1u);
+        mma_bf16(t + NB, desc_sw64(a0 + 2 * a_stride) + (uint64_t)(k * 2), bd, i1, 1u);
     }
 }
 
@@ -253,17 +283,25 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16& x0, __nv_bfloat16
     x1 = __float2bfloat16_rn(r1);
     x2 = __float2bfloat16_rn(r1 - __bfloat162float(x1));
 }
+// two floats -> packed BF16 pair (round to nearest even), a in the low half, b in the high half
+__device__ __forceinline__ uint32_t cvt_bf16x2(float a, float b) {
+    uint32_t d;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+    return d;
+}
+// split3 of a pair at once, packed: parts o[0..2] (low half a, high half b)
+__device__ __forceinline__ void split3x2(float a, float b, uint32_t (&o)[3]) {
+    o[0] = cvt_bf16x2(a, b);
+    const float ra = a - __uint_as_float(o[0] << 16), rb = b - __uint_as_float(o[0] & 0xffff0000u);
+    o[1] = cvt_bf16x2(ra, rb);
+    o[2] = cvt_bf16x2(ra - __uint_as_float(o[1] << 16), rb - __uint_as_float(o[1] & 0xffff0000u));
+}
 __device__ __forceinline__ void split3x4(float4 v, uint2 (&o)[3]) {
-    __nv_bfloat16 p[3][4];
-    split3(v.x, p[0][0], p[1][0], p[2][0]);
-    split3(v.y, p[0][1], p[1][1], p[2][1]);
-    split3(v.z, p[0][2], p[1][2], p[2][2]);
-    split3(v.w, p[0][3], p[1][3], p[2][3]);
+    uint32_t lo[3], hi[3];
+    split3x2(v.x, v.y, lo);
+    split3x2(v.z, v.w, hi);
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-        o[q].x = (uint32_t)__bfloat16_as_ushort(p[q][0]) | ((uint32_t)__bfloat16_as_ushort(p[q][1]) << 16);
-        o[q].y = (uint32_t)__bfloat16_as_ushort(p[q][2]) | ((uint32_t)__bfloat16_as_ushort(p[q][3]) << 16);
-    }
+    for (int q = 0; q < 3; q++) o[q] = make_uint2(lo[q], hi[q]);
 }
 // float4 q of an FP32 block as TMA writes it (row r = q / 8; its stored 16-byte chunk q % 8 holds
 // elements 4c..4c+3 with c = (q % 8) ^ (r % 8)) -> byte offset of those four elements in the BF16
@@ -312,7 +350,7 @@ struct HemmArgs {
     int* err;
 };
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kHemmThreads, 1)
     tc_hemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, HemmArgs h) {
     extern __shared__ unsigned char smraw[];
     unsigned char* sm = align1024(smraw);
@@ -341,20 +379,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         s_abort = 0;
         for (int s = 0; s < kHemmRing; s++) {
             mbar_init(rfull + s, 1);
-            mbar_init(rconv + s, kWorkers);
+            mbar_init(rconv + s, kHemmWorkers / 32);
             mbar_init(rmma + s, 1);
         }
         for (int s = 0; s < kHemmParts; s++) {
-            mbar_init(pfull + s, kWorkers);
+            mbar_init(pfull + s, kHemmWorkers / 32);
             mbar_init(pempty + s, 1);
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(tfull + b, 1);
-            mbar_init(tempty + b, kWorkers);
+            mbar_init(tempty + b, kHemmWorkers / 32);
         }
         fence_mbar_init();
     }
-    if (warp == 1) tmem_alloc(tslot, 256);
+    if (warp == 1) tmem_alloc(tslot, kTmemCols);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -388,7 +426,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_bf16(kRows, 64);
             int c = -1;
             for (int j = 0; j < nu; j++) {
                 const int64_t u = u0 + j;
@@ -404,23 +441,23 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 if (!mbar_wait(rfull + s, ph, &s_abort, h.err) || !mbar_wait(pfull + ps, pph, &s_abort, h.err)) break;
                 tc_fence_after();
-                const uint32_t tb = tmem + (uint32_t)(128 * (c & 1));
-                mma_block6(tb, tb + 64, apart(ps), kHemmA, bpart(s), kHemmB, idesc, first);
+                const uint32_t tb = tmem + (uint32_t)(256 * (c & 1));
+                mma_block_cat<64>(tb, apart(ps), kHemmA, bpart(s), first);
                 mma_commit(rmma + s);
                 mma_commit(pempty + ps);
                 if (chain_end(u)) mma_commit(tfull + (c & 1));
             }
         }
     } else {
-        // workers: warp w reads tensor-memory lanes 32 (w % 4) ..; warps 2-5 own accumulator
-        // columns 0..31 (Re), warps 6-9 columns 32..63 (Im)
+        // workers: warp w reads tensor-memory lanes 32 (w % 4) ..; warps 2-5, 6-9, 10-13, 14-17
+        // own accumulator columns 0..15, 16..31 (Re), 32..47, 48..63 (Im)
         const int ct = threadIdx.x - 64;
-        const int q = warp & 3, half = (warp - 2) >> 2;
-        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(32 * half);
+        const int q = warp & 3, cg = (warp - 2) >> 2;
+        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(16 * cg);
         const int r = q * 32 + lane;
-        float acc[32];
+        float acc[16];
 #pragma unroll
-        for (int e = 0; e < 32; e++) acc[e] = 0.f;
+        for (int e = 0; e < 16; e++) acc[e] = 0.f;
         bool ok = true;
         // chains are drained in order, one behind the conversion; a chain that ends a tile (or
         // the range) writes the tile's partial sums and clears the accumulator
@@ -431,23 +468,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             const bool got = mbar_wait(tfull + b, (uint32_t)(cc / 2) & 1u, &s_abort, h.err);
             ok = __all_sync(0xffffffffu, got) && ok;   // warp-uniform: the tensor-memory loads need all lanes
             tc_fence_after();
-            float v[64];   // big 0..15, big 16..31, small 0..15, small 16..31 of this warp's columns
-            const uint32_t tb = tq + (uint32_t)(128 * b);
-            tmem_ld4x16(tb, tb + 16, tb + 64, tb + 80, v);
+            float v[48];   // the three column groups of this warp's 16 columns
+            const uint32_t tb = tq + (uint32_t)(256 * b);
+            tmem_ld3x16(tb, tb + 64, tb + 128, v);
 #pragma unroll
-            for (int x = 0; x < 32; x++) acc[x] += v[x] + v[32 + x];
+            for (int x = 0; x < 16; x++) acc[x] += v[x] + (v[16 + x] + v[32 + x]);
             tc_fence_before();
-            mbar_arrive(tempty + b);
+            mbar_arrive_warp(tempty + b);
             if (chain_last[b]) {
                 const int t = chain_tile[b], i = t * kRows + r;
                 if (ok && !s_abort && i < h.m) {
-                    float* out = h.P + (((int64_t)g * h.slots + (t - t_first)) * kRows + r) * 64 + 32 * half;
+                    float* out = h.P + (((int64_t)g * h.slots + (t - t_first)) * kRows + r) * 64 + 16 * cg;
 #pragma unroll
-                    for (int e = 0; e < 32; e += 4)
+                    for (int e = 0; e < 16; e += 4)
                         *reinterpret_cast<float4*>(out + e) = make_float4(acc[e], acc[e + 1], acc[e + 2], acc[e + 3]);
                 }
 #pragma unroll
-                for (int e = 0; e < 32; e++) acc[e] = 0.f;
+                for (int e = 0; e < 16; e++) acc[e] = 0.f;
             }
             drained++;
         };
@@ -460,10 +497,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ok = false;
                 break;
             }
-            convert_block(reinterpret_cast<const float*>(raw(s)), kRows, apart(ps), kHemmA, nullptr, ct, kWorkers);
+            convert_block(reinterpret_cast<const float*>(raw(s)), kRows, apart(ps), kHemmA, nullptr, ct, kHemmWorkers);
             fence_async_smem();
-            mbar_arrive(rconv + s);
-            mbar_arrive(pfull + ps);
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(rconv + s);
+                mbar_arrive(pfull + ps);
+            }
             if (chain_start(u)) {
                 chain_tile[nchain & 1] = (int)(u / KB);
                 nchain++;
@@ -481,7 +521,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, 256);
+        tmem_dealloc(tmem, kTmemCols);
     }
 }
 
@@ -535,22 +575,22 @@ struct UpdArgs {
     int* err;
 };
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kUpdThreads, 1)
     tc_update_kernel(const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmL,
                      const __grid_constant__ CUtensorMap tmR, const __grid_constant__ CUtensorMap tmRi, UpdArgs a) {
     extern __shared__ unsigned char smraw[];
     unsigned char* sm = align1024(smraw);
     unsigned char* Ls = sm;                                   // [kb][part] 128 rows x 64 B
-    float* Cs0 = reinterpret_cast<float*>(sm + kUpdL);        // 2 x [kUpdCols columns][256 reals]
-    unsigned char* ring = sm + kUpdL + 2 * kUpdC;
+    float* Cs0 = reinterpret_cast<float*>(sm + kUpdL);        // kUpdCbuf x [kUpdCols columns][256 reals]
+    unsigned char* ring = sm + kUpdL + kUpdCbuf * kUpdC;
     uint64_t* bars = reinterpret_cast<uint64_t*>(ring + kUpdRing * kUpdBslot);
     uint64_t* bfull = bars;                     // [ring] B parts landed
     uint64_t* bempty = bfull + kUpdRing;        // [ring] B parts consumed
-    uint64_t* cfull = bempty + kUpdRing;        // [2] C tile landed
-    uint64_t* cempty = cfull + 2;               // [2] C tile stored (its shared memory read out)
-    uint64_t* tfull = cempty + 2;               // [2] accumulator pair holds a finished tile
-    uint64_t* tempty = tfull + 2;               // [2] accumulator pair drained
-    uint64_t* lfull = tempty + 2;               // L parts of a strip landed
+    uint64_t* cfull = bempty + kUpdRing;        // [kUpdCbuf] C tile landed
+    uint64_t* cempty = cfull + kUpdCbuf;        // [kUpdCbuf] C tile stored (its shared memory read out)
+    uint64_t* tfull = cempty + kUpdCbuf;        // [kUpdAcc] accumulator pair holds a finished tile
+    uint64_t* tempty = tfull + kUpdAcc;         // [kUpdAcc] accumulator pair drained
+    uint64_t* lfull = tempty + kUpdAcc;         // L parts of a strip landed
     uint64_t* lfree = lfull + 1;                // MMAs of the previous strip done
     uint32_t* tslot = reinterpret_cast<uint32_t*>(lfree + 1);
     __shared__ int s_abort;
@@ -568,17 +608,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_init(bfull + s, 1);
             mbar_init(bempty + s, 1);
         }
-        for (int b = 0; b < 2; b++) {
+        for (int b = 0; b < kUpdCbuf; b++) {
             mbar_init(cfull + b, 1);
             mbar_init(cempty + b, 1);
+        }
+        for (int b = 0; b < kUpdAcc; b++) {
             mbar_init(tfull + b, 1);
-            mbar_init(tempty + b, kWorkers);
+            mbar_init(tempty + b, kWorkers / 32);
         }
         mbar_init(lfull, 1);
         mbar_init(lfree, 1);
         fence_mbar_init();
     }
-    if (warp == 1) tmem_alloc(tslot, 256);
+    if (warp == 1) tmem_alloc(tslot, kTmemCols);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -588,11 +630,11 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            prefetch_map(&tmC);
             prefetch_map(&tmL);
             prefetch_map(&tmR);
             prefetch_map(&tmRi);
-            int nstrip = 0, issued = 0, lissued = 0, cissued[2] = {0, 0};
+            // L parts and B operands; the A22 tiles are loaded by warp 10, independently
+            int nstrip = 0, issued = 0, lissued = 0;
             for (int j = 0; j < nt; j++) {
                 const int strip = strip_of(j), col = col_of(j);
                 if (j == 0 || strip != strip_of(j - 1)) {
@@ -604,11 +646,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                     nstrip++;
                     lissued = nstrip;
                 }
-                const int cb = j & 1;
-                if (j >= 2 && !mbar_wait(cempty + cb, (uint32_t)(j / 2 - 1) & 1u, &s_abort, a.err)) break;
-                mbar_arrive_tx(cfull + cb, kUpdC);
-                tma_load_2d(Cs(cb), &tmC, 2 * strip * kRows, col * kUpdCols, cfull + cb);
-                cissued[cb] = j / 2 + 1;
                 bool okb = true;
                 for (int kb = 0; kb < 4; kb++) {
                     const int n = 4 * j + kb, s = n % kUpdRing;
@@ -625,12 +662,24 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (!okb) break;
             }
             for (int s = 0; s < kUpdRing; s++) mbar_drain(bfull + s, s < issued ? (issued - 1 - s) / kUpdRing : -1);
-            for (int b = 0; b < 2; b++) mbar_drain(cfull + b, cissued[b] - 1);
             mbar_drain(lfull, lissued - 1);
+        }
+    } else if (warp == 10) {
+        if (lane == 0) {
+            // the A22 tiles: tile j into buffer j % kUpdCbuf once tile j - kUpdCbuf has been stored
+            prefetch_map(&tmC);
+            int issued = 0;
+            for (int j = 0; j < nt; j++) {
+                const int cb = j % kUpdCbuf;
+                if (j >= kUpdCbuf && !mbar_wait(cempty + cb, (uint32_t)(j / kUpdCbuf - 1) & 1u, &s_abort, a.err)) break;
+                mbar_arrive_tx(cfull + cb, kUpdC);
+                tma_load_2d(Cs(cb), &tmC, 2 * strip_of(j) * kRows, col_of(j) * kUpdCols, cfull + cb);
+                issued = j + 1;
+            }
+            for (int b = 0; b < kUpdCbuf; b++) mbar_drain(cfull + b, b < issued ? (issued - 1 - b) / kUpdCbuf : -1);
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_bf16(kRows, 2 * kUpdCols);
             int nstrip = 0;
             for (int j = 0; j < nt; j++) {
                 const int strip = strip_of(j);
@@ -638,17 +687,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (!mbar_wait(lfull, (uint32_t)nstrip & 1u, &s_abort, a.err)) break;
                     nstrip++;
                 }
-                const int b = j & 1;
-                if (j >= 2 && !mbar_wait(tempty + b, (uint32_t)(j / 2 - 1) & 1u, &s_abort, a.err)) break;
+                const int b = j % kUpdAcc;
+                if (j >= kUpdAcc && !mbar_wait(tempty + b, (uint32_t)(j / kUpdAcc - 1) & 1u, &s_abort, a.err)) break;
                 tc_fence_after();
-                const uint32_t tb = tmem + (uint32_t)(128 * b);
+                const uint32_t tb = tmem + (uint32_t)(kUpdAccCols * b);
                 bool okb = true;
                 for (int kb = 0; kb < 4; kb++) {
                     const int n = 4 * j + kb, s = n % kUpdRing;
                     const uint32_t ph = (uint32_t)(n / kUpdRing) & 1u;
                     if (!mbar_wait(bfull + s, ph, &s_abort, a.err)) { okb = false; break; }
                     tc_fence_after();
-                    mma_block6(tb, tb + 64, lpart(kb), kRows * kKb * 2, bslot(s), kUpdBpart, idesc, kb == 0);
+                    mma_block_cat<2 * kUpdCols>(tb, lpart(kb), kRows * kKb * 2, bslot(s), kb == 0);
                     mma_commit(bempty + s);
                 }
                 if (!okb) break;
@@ -656,50 +705,54 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (j == nt - 1 || strip_of(j + 1) != strip) mma_commit(lfree);
             }
         }
-    } else {
+    } else if (warp >= 2 && warp < 10) {
         // workers: warp w reads tensor-memory lanes 32 (w % 4) ..; warps 2-5 take complex columns
-        // 0..15 of the tile, warps 6-9 columns 16..31
+        // 0 .. kUpdCols / 2 - 1 of the tile, warps 6-9 the rest
+        constexpr int kHalf = kUpdCols / 2;
         const int ct = threadIdx.x - 64;
         const int q = warp & 3, half = (warp - 2) >> 2;
         const int r = q * 32 + lane;   // row of the tile
-        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(16 * half);
+        const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(kHalf * half);
         for (int j = 0; j < nt; j++) {
-            const int b = j & 1;
-            bool ok = mbar_wait(tfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err) &&
-                      mbar_wait(cfull + b, (uint32_t)(j / 2) & 1u, &s_abort, a.err);
+            const int b = j % kUpdAcc, cb = j % kUpdCbuf;
+            bool ok = mbar_wait(tfull + b, (uint32_t)(j / kUpdAcc) & 1u, &s_abort, a.err) &&
+                      mbar_wait(cfull + cb, (uint32_t)(j / kUpdCbuf) & 1u, &s_abort, a.err);
             ok = __all_sync(0xffffffffu, ok);   // the warp stays converged for the tensor-memory loads
             tc_fence_after();
-            float* C = Cs(b);
-            float v[64];   // big Re, big Im, small Re, small Im of this warp's 16 columns
-            const uint32_t tb = tq + (uint32_t)(128 * b);
-            tmem_ld4x16(tb, tb + kUpdCols, tb + 64, tb + 64 + kUpdCols, v);
+            float* C = Cs(cb);
+            static_assert(kHalf == 16, "two column halves of 16 per tile");
+            float v[6 * kHalf];   // Re, Im of each column group, this warp's columns
+            const uint32_t tb = tq + (uint32_t)(kUpdAccCols * b);
+            tmem_ld6x16(tb, tb + kUpdCols, tb + 2 * kUpdCols, tb + 3 * kUpdCols, tb + 4 * kUpdCols, tb + 5 * kUpdCols, v);
             if (ok) {
 #pragma unroll
-                for (int u = 0; u < 16; u++) {
-                    float2* cp = reinterpret_cast<float2*>(C + (16 * half + u) * 2 * kRows) + r;
+                for (int u = 0; u < kHalf; u++) {
+                    float2* cp = reinterpret_cast<float2*>(C + (kHalf * half + u) * 2 * kRows) + r;
                     const float2 x = *cp;
-                    *cp = make_float2(x.x - (v[u] + v[32 + u]), x.y - (v[16 + u] + v[48 + u]));
+                    *cp = make_float2(x.x - (v[u] + (v[2 * kHalf + u] + v[4 * kHalf + u])),
+                                      x.y - (v[kHalf + u] + (v[3 * kHalf + u] + v[5 * kHalf + u])));
                 }
             }
             tc_fence_before();
-            mbar_arrive(tempty + b);
+            mbar_arrive_warp(tempty + b);
             fence_async_smem();
             asm volatile("bar.sync 1, %0;" ::"n"(kWorkers) : "memory");
             // leave together: a failed wait set s_abort before the barrier
             if (*reinterpret_cast<volatile int*>(&s_abort)) break;
             if (ct == 0) {
-                const int strip = strip_of(j), col = col_of(j);
-                tma_store_2d(&tmC, 2 * strip * kRows, col * kUpdCols, C);
+                // the buffer may be refilled once the store has read it out
+                tma_store_2d(&tmC, 2 * strip_of(j) * kRows, col_of(j) * kUpdCols, C);
                 tma_store_drain();
-                mbar_arrive(cempty + b);
+                mbar_arrive(cempty + cb);
             }
         }
+        if (ct == 0) tma_store_wait_all();
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, 256);
+        tmem_dealloc(tmem, kTmemCols);
     }
 }
 
@@ -816,7 +869,7 @@ int tc_hemm(cudaStream_t st, int nsm, int m, int kk, const float2* A22, int64_t 
     const int64_t nb = (int64_t)64 * kpad;
     tc_prep_hemm_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(m, kk, V, kpad, B);
     if (ev) cudaEventRecord(ev[0], st);
-    tc_hemm_kernel<<<(unsigned)G, kThreads, kHemmSmem, st>>>(mA, mB, h);
+    tc_hemm_kernel<<<(unsigned)G, kHemmThreads, kHemmSmem, st>>>(mA, mB, h);
     if (ev) cudaEventRecord(ev[1], st);
     tc_hemm_reduce_kernel<<<(unsigned)(((int64_t)m * kk + 255) / 256), 256, 0, st>>>(m, kk, h, G, Y);
     *launches += 3;
@@ -849,7 +902,7 @@ int tc_rank2k(cudaStream_t st, int nsm, int m, int kk, float2* A22, int64_t lda,
     a.err = err;
     const int64_t G = std::min<int64_t>(nsm, a.ntiles);
     if (ev) cudaEventRecord(ev[0], st);
-    tc_update_kernel<<<(unsigned)G, kThreads, kUpdSmem, st>>>(mC, mL, mR, mRi, a);
+    tc_update_kernel<<<(unsigned)G, kUpdThreads, kUpdSmem, st>>>(mC, mL, mR, mRi, a);
     if (ev) cudaEventRecord(ev[1], st);
     *launches += 2;
     return cudaGetLastError() == cudaSuccess ? 0 : 3;
