@@ -689,10 +689,10 @@ __device__ __forceinline__ F tri_solve(int n, const F* __restrict__ Ur, const F*
 // from global memory row by row each step waits for a load (long-scoreboard stalls dominated).  Here
 // the warp copies chunks of SCH rows of its interleaved [k][32] arrays into shared memory with
 // cp.async, SNS chunks ahead, so every step reads shared memory.  All 32 lanes must call these.
-constexpr int SCH = 32;                                  // rows per staged chunk
+constexpr int SCH = 16;                                  // rows per staged chunk
 constexpr int SNS = 4;                                   // chunks in flight
 constexpr int SRW = SCH * 32;                            // elements of one array in one chunk
-constexpr size_t kStageSmem = (size_t)SNS * 4 * SRW * sizeof(float) + (size_t)SNS * SRW;   // 68 KB
+constexpr size_t kStageSmem = (size_t)SNS * 4 * SRW * sizeof(float) + (size_t)SNS * SRW;   // 34 KB: several warps per SM
 
 __device__ __forceinline__ void cp16(void* sdst, const void* gsrc) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
@@ -904,6 +904,9 @@ __global__ void __launch_bounds__(32) invit_kernel(int n, const double* __restri
     // lanes past the batch or on cluster members run the sweeps on a dummy right-hand side (the
     // staged sweeps need the whole warp) and write nothing
     const bool act = t < count && !cl[i];
+    // a warp whose eigenvalues all belong to clusters (most of them, where the spectrum is dense)
+    // has nothing to do: the block is this one warp
+    if (!__any_sync(0xffffffffu, act)) return;
     // this warp's scratch: [array][k][32 lanes], one 128-byte line per row in FP32
     const size_t W32 = (size_t)n * 32;
     const size_t lane = threadIdx.x & 31;
@@ -1166,10 +1169,22 @@ __global__ void __launch_bounds__(32) cluster64_kernel(int n, const double* __re
 // gives the eigenpairs.  The iterations run in FP32, as the tridiagonal of the mixed path carries
 // FP32 rounding itself.  Members outside [cout[2t], cout[2t+1]) are guards, solved but not written.
 // Scratch: interleaved [k][32] arrays per lane group.  A block of kClusterWarps warps serves one
-// lane group: warp 0 runs the (sequential) triangular solves, and all warps split the rows of the
-// Gram, orthonormalisation and output passes, which are row-parallel.
+// lane group: warp 0 runs the (sequential) triangular solves, and the warps split the rows of the
+// Gram, orthonormalisation and output passes, which are row-parallel.  One warp per block: the
+// sequential sweeps set the pace, and with one warp per lane group an SM runs several groups'
+// sweeps at once instead of one group's sweep while the other warps wait at a barrier.
 constexpr int CMAX = 32;
-constexpr int kClusterWarps = 8;
+constexpr int kClusterWarps = 1;
+
+// (hi, lo) += v: Knuth's TwoSum keeps the rounding error of each addition in lo (FP32 adds; FP64
+// adds run at a small fraction of the FP32 rate on this part).  hi + lo carries ~48 bits.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
+    const float s = __fadd_rn(hi, v);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(v, bp));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
 
 // this warp's share of rows [kb, ke) of the block's row-parallel passes (multiples of 16 rows)
 __device__ __forceinline__ void warp_rows(int n, int& kb, int& ke) {
@@ -1181,17 +1196,30 @@ __device__ __forceinline__ void warp_rows(int n, int& kb, int& ke) {
 
 // out[b][a] = sum_k u_b(k) z_a(k) over the columns z_a = X[k * 32 + a] of lane b's segment
 // [slo, slo + sc); lane b accumulates row b; u = z (Gram matrix) or u = T z (projected T).
-// FP32 partial sums over 16 rows go into FP64.  The block's warps split the rows and add their
-// partial sums into out one warp after the other; every thread of the block calls this.
+// The row-parallel passes read every row of the lane group's 32 columns in every lane: the rows of a
+// chunk of 16 are staged in a per-warp shared tile (row q at tile[32 q ..]) and read back as
+// float4 broadcasts, 8 loads per row where a shuffle per column took 32.
+__device__ __forceinline__ void stage_tile(float* tile, const float (&v)[16]) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 16; q++) tile[q * 32 + lane] = v[q];
+    __syncwarp();
+}
+
+// FP32 partial sums over 16 rows go into compensated FP32 (hi, lo) pairs, added into out in FP64.
+// The block's warps split the rows and add their partial sums into out one warp after the other;
+// every thread of the block calls this.
 template <typename F, bool APPLY_T>
 __device__ void cluster_gram(int n, int slo, int sc, const F* __restrict__ X, const F* __restrict__ d,
-                             const F* __restrict__ e, double* __restrict__ out) {
+                             const F* __restrict__ e, double* __restrict__ out, float* tile) {
+    static_assert(sizeof(F) == sizeof(float), "FP32 lane groups");
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int kb, ke;
     warp_rows(n, kb, ke);
-    double acc[CMAX];
+    float acc[CMAX], accl[CMAX];
 #pragma unroll
-    for (int a = 0; a < CMAX; a++) acc[a] = 0;
+    for (int a = 0; a < CMAX; a++) acc[a] = accl[a] = 0.0f;
     F zprev = (APPLY_T && kb > 0 && kb < n) ? X[(size_t)(kb - 1) * 32] : F(0);
     for (int k0 = kb; k0 < ke; k0 += 16) {
         // the chunk's rows (and one row ahead for T z) are loaded before any is used, so the
@@ -1210,26 +1238,39 @@ __device__ void cluster_gram(int n, int slo, int sc, const F* __restrict__ X, co
         F part[CMAX];
 #pragma unroll
         for (int a = 0; a < CMAX; a++) part[a] = 0;
+        {
+            float zt[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) zt[q] = zb[q];
+            stage_tile(tile, zt);
+        }
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             if (k0 + q < ke) {
                 const F zc = zb[q];
                 F u = zc;
                 if (APPLY_T) u = db[q] * zc + (q > 0 ? eb[q - 1] : eprev) * zprev + eb[q] * zb[q + 1];
+                const float4* row = reinterpret_cast<const float4*>(tile + q * 32);
 #pragma unroll
-                for (int a = 0; a < CMAX; a++) part[a] += u * __shfl_sync(0xffffffffu, zc, a);
+                for (int a4 = 0; a4 < CMAX / 4; a4++) {
+                    const float4 v = row[a4];
+                    part[4 * a4] += u * v.x;
+                    part[4 * a4 + 1] += u * v.y;
+                    part[4 * a4 + 2] += u * v.z;
+                    part[4 * a4 + 3] += u * v.w;
+                }
                 zprev = zc;
             }
         }
 #pragma unroll
-        for (int a = 0; a < CMAX; a++) acc[a] += (double)part[a];
+        for (int a = 0; a < CMAX; a++) two_sum_acc(acc[a], accl[a], (float)part[a]);
     }
     for (int wq = 0; wq < nw; wq++) {
         if (wid == wq)
 #pragma unroll
             for (int a = 0; a < CMAX; a++)
                 if (sc > 0 && a >= slo && a < slo + sc)
-                    out[lane * CMAX + a] = (wq == 0 ? 0.0 : out[lane * CMAX + a]) + acc[a];
+                    out[lane * CMAX + a] = (wq == 0 ? 0.0 : out[lane * CMAX + a]) + ((double)acc[a] + (double)accl[a]);
         __syncthreads();
     }
 }
@@ -1268,9 +1309,9 @@ __device__ void inv_upper(int c, const double* R, double* Rinv) {
 // segment's first lane in warp 0 factoring its diagonal block; rows split over the block's warps.
 template <typename F>
 __device__ void cluster_cholqr(int n, int slo, int sc, F* __restrict__ X, double* __restrict__ Gs,
-                               double* __restrict__ Rinv) {
+                               double* __restrict__ Rinv, float* tile) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    cluster_gram<F, false>(n, slo, sc, X, (const F*)nullptr, (const F*)nullptr, Gs);
+    cluster_gram<F, false>(n, slo, sc, X, (const F*)nullptr, (const F*)nullptr, Gs, tile);
     if (wid == 0 && sc > 0 && lane == slo) {
         chol_upper(sc, Gs + slo * (CMAX + 1));
         inv_upper(sc, Gs + slo * (CMAX + 1), Rinv + slo * (CMAX + 1));
@@ -1282,15 +1323,20 @@ __device__ void cluster_cholqr(int n, int slo, int sc, F* __restrict__ X, double
     int kb, ke;
     warp_rows(n, kb, ke);
     for (int k0 = kb; k0 < ke; k0 += 16) {
-        F xb[16];
+        float xb[16];
 #pragma unroll
         for (int q = 0; q < 16; q++) xb[q] = k0 + q < ke ? X[(size_t)(k0 + q) * 32] : F(0);
+        stage_tile(tile, xb);
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             if (k0 + q < ke) {
+                const float4* row = reinterpret_cast<const float4*>(tile + q * 32);
                 F v = 0;
 #pragma unroll
-                for (int a = 0; a < CMAX; a++) v += __shfl_sync(0xffffffffu, xb[q], a) * rcol[a];
+                for (int a4 = 0; a4 < CMAX / 4; a4++) {
+                    const float4 x = row[a4];
+                    v += x.x * rcol[4 * a4] + x.y * rcol[4 * a4 + 1] + x.z * rcol[4 * a4 + 2] + x.w * rcol[4 * a4 + 3];
+                }
                 if (sc > 0) X[(size_t)(k0 + q) * 32] = v;
             }
         }
@@ -1299,73 +1345,114 @@ __device__ void cluster_cholqr(int n, int slo, int sc, F* __restrict__ X, double
     __syncthreads();
 }
 
-// Rayleigh-Ritz inside a cluster (one lane): M q = theta S q with S = Gs = Z^T Z = R^T R, Jacobi
-// on R^{-T} M R^{-1}; on return M's diagonal holds theta, Q (column-major) the coefficient vectors
-// R^{-1} q', ord the ascending order.  Gs and Rinv are overwritten.  All arrays relative to the
-// block's top-left corner, row stride CMAX.
-__device__ void cluster_rr(int c, double* Gs, double* Rinv, double* M, double* Q, int* ord) {
-    for (int a = 0; a < c; a++)
-        for (int b = 0; b < a; b++) M[a * CMAX + b] = M[b * CMAX + a] = 0.5 * (M[a * CMAX + b] + M[b * CMAX + a]);
-    chol_upper(c, Gs);
-    inv_upper(c, Gs, Rinv);
-    for (int a = 0; a < c; a++)            // Q = M Rinv (row-major scratch)
-        for (int b = 0; b < c; b++) {
-            double v = 0;
-            for (int q = 0; q <= b; q++) v += M[a * CMAX + q] * Rinv[q * CMAX + b];
-            Q[a * CMAX + b] = v;
+// FP32 counterparts of chol_upper / inv_upper (same layout and pivot floor)
+__device__ void chol_upper_f(int c, float* G) {
+    for (int j = 0; j < c; j++) {
+        const float g0 = G[j * CMAX + j];
+        float djj = g0;
+        for (int q = 0; q < j; q++) djj -= G[q * CMAX + j] * G[q * CMAX + j];
+        djj = sqrtf(fmaxf(djj, 1e-10f * fmaxf(g0, 1e-30f)));
+        G[j * CMAX + j] = djj;
+        for (int b = j + 1; b < c; b++) {
+            float v = G[j * CMAX + b];
+            for (int q = 0; q < j; q++) v -= G[q * CMAX + j] * G[q * CMAX + b];
+            G[j * CMAX + b] = v / djj;
         }
-    for (int a = 0; a < c; a++)            // M = Rinv^T Q (column-major from here on)
+    }
+}
+__device__ void inv_upper_f(int c, const float* R, float* Rinv) {
+    for (int jc = 0; jc < c; jc++) {
+        for (int r = jc; r >= 0; r--) {
+            float v = r == jc ? 1.0f : 0.0f;
+            for (int q = r + 1; q <= jc; q++) v -= R[r * CMAX + q] * Rinv[q * CMAX + jc];
+            Rinv[r * CMAX + jc] = v / R[r * CMAX + r];
+        }
+        for (int r = jc + 1; r < c; r++) Rinv[r * CMAX + jc] = 0;
+    }
+}
+
+// Rayleigh-Ritz inside a cluster of the mixed path (one lane), in FP32: M q = theta S q with
+// S = Gs = Z^T Z = R^T R, cyclic Jacobi on R^{-T} M R^{-1} until the off-diagonal part is below
+// FP32 resolution.  Z is FP32 and T is the FP32 tridiagonal, so the entries of M carry errors of a
+// few eps32 |T| already; FP32 arithmetic adds errors of the same size, where FP64 (a small
+// fraction of the FP32 rate on this part) made this step the most expensive of the cluster solve.
+// Inputs Gs, M: this segment's block, row stride CMAX (FP64, as the Gram passes write them).
+// Scratch Sf, Rf; outputs Mf (column-major, diagonal = theta), Qf (column-major, the coefficient
+// vectors R^{-1} q'), ord (ascending theta).  All float arrays at the segment's block offset.
+__device__ void cluster_rr32(int c, const double* Gs, const double* M, float* Sf, float* Rf, float* Mf, float* Qf,
+                             int* ord) {
+    for (int a = 0; a < c; a++)
         for (int b = 0; b < c; b++) {
-            double v = 0;
-            for (int q = 0; q <= a; q++) v += Rinv[q * CMAX + a] * Q[q * CMAX + b];
-            M[a + b * CMAX] = v;
+            Sf[a * CMAX + b] = (float)Gs[a * CMAX + b];
+            Mf[a * CMAX + b] = (float)(0.5 * (M[a * CMAX + b] + M[b * CMAX + a]));
+        }
+    chol_upper_f(c, Sf);
+    inv_upper_f(c, Sf, Rf);
+    for (int a = 0; a < c; a++)            // Qf = Mf Rf (row-major scratch)
+        for (int b = 0; b < c; b++) {
+            float v = 0;
+            for (int q = 0; q <= b; q++) v += Mf[a * CMAX + q] * Rf[q * CMAX + b];
+            Qf[a * CMAX + b] = v;
+        }
+    for (int a = 0; a < c; a++)            // Sf = Rf^T Qf (column-major)
+        for (int b = 0; b < c; b++) {
+            float v = 0;
+            for (int q = 0; q <= a; q++) v += Rf[q * CMAX + a] * Qf[q * CMAX + b];
+            Sf[a + b * CMAX] = v;
         }
     for (int a = 0; a < c; a++)
-        for (int b = 0; b < a; b++) M[a + b * CMAX] = M[b + a * CMAX] = 0.5 * (M[a + b * CMAX] + M[b + a * CMAX]);
-    for (int a = 0; a < c; a++)
-        for (int b = 0; b < c; b++) Q[a + b * CMAX] = a == b ? 1.0 : 0.0;
+        for (int b = 0; b < c; b++) {
+            Mf[a + b * CMAX] = a == b ? Sf[a + a * CMAX] : 0.5f * (Sf[a + b * CMAX] + Sf[b + a * CMAX]);
+            Qf[a + b * CMAX] = a == b ? 1.0f : 0.0f;
+        }
     for (int sweep = 0; sweep < 30; sweep++) {
-        double off = 0;
-        for (int a = 0; a < c; a++)
-            for (int b = a + 1; b < c; b++) off += M[a + b * CMAX] * M[a + b * CMAX];
-        if (off < 1e-60) break;
+        float off = 0, dg = 0;
+        for (int a = 0; a < c; a++) {
+            dg += Mf[a + a * CMAX] * Mf[a + a * CMAX];
+            for (int b = a + 1; b < c; b++) off += Mf[a + b * CMAX] * Mf[a + b * CMAX];
+        }
+        if (off == 0.0f || off <= 1e-16f * dg) break;
         for (int p = 0; p < c; p++)
             for (int q = p + 1; q < c; q++) {
-                const double apq = M[p + q * CMAX];
-                if (apq == 0.0) continue;
-                const double tau = (M[q + q * CMAX] - M[p + p * CMAX]) / (2.0 * apq);
-                const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                const double cs = 1.0 / sqrt(1.0 + tt * tt), sn = tt * cs;
+                const float apq = Mf[p + q * CMAX];
+                // below FP32 resolution of the diagonal: zero, no rotation (so the sweeps end)
+                if (fabsf(apq) <= 5.9604645e-8f * (fabsf(Mf[p + p * CMAX]) + fabsf(Mf[q + q * CMAX]))) {
+                    Mf[p + q * CMAX] = Mf[q + p * CMAX] = 0.0f;
+                    continue;
+                }
+                const float tau = (Mf[q + q * CMAX] - Mf[p + p * CMAX]) / (2.0f * apq);
+                const float tt = (tau >= 0 ? 1.0f : -1.0f) / (fabsf(tau) + sqrtf(1.0f + tau * tau));
+                const float cs = 1.0f / sqrtf(1.0f + tt * tt), sn = tt * cs;
                 for (int k = 0; k < c; k++) {
-                    const double mkp = M[k + p * CMAX], mkq = M[k + q * CMAX];
-                    M[k + p * CMAX] = cs * mkp - sn * mkq;
-                    M[k + q * CMAX] = sn * mkp + cs * mkq;
+                    const float mkp = Mf[k + p * CMAX], mkq = Mf[k + q * CMAX];
+                    Mf[k + p * CMAX] = cs * mkp - sn * mkq;
+                    Mf[k + q * CMAX] = sn * mkp + cs * mkq;
                 }
                 for (int k = 0; k < c; k++) {
-                    const double mpk = M[p + k * CMAX], mqk = M[q + k * CMAX];
-                    M[p + k * CMAX] = cs * mpk - sn * mqk;
-                    M[q + k * CMAX] = sn * mpk + cs * mqk;
+                    const float mpk = Mf[p + k * CMAX], mqk = Mf[q + k * CMAX];
+                    Mf[p + k * CMAX] = cs * mpk - sn * mqk;
+                    Mf[q + k * CMAX] = sn * mpk + cs * mqk;
                 }
                 for (int k = 0; k < c; k++) {
-                    const double qkp = Q[k + p * CMAX], qkq = Q[k + q * CMAX];
-                    Q[k + p * CMAX] = cs * qkp - sn * qkq;
-                    Q[k + q * CMAX] = sn * qkp + cs * qkq;
+                    const float qkp = Qf[k + p * CMAX], qkq = Qf[k + q * CMAX];
+                    Qf[k + p * CMAX] = cs * qkp - sn * qkq;
+                    Qf[k + q * CMAX] = sn * qkp + cs * qkq;
                 }
             }
     }
-    for (int a = 0; a < c; a++)            // Q <- Rinv Q
+    for (int a = 0; a < c; a++)            // Qf <- Rf Qf (through Sf)
         for (int b = 0; b < c; b++) {
-            double v = 0;
-            for (int q = a; q < c; q++) v += Rinv[a * CMAX + q] * Q[q + b * CMAX];
-            Gs[a + b * CMAX] = v;
+            float v = 0;
+            for (int q = a; q < c; q++) v += Rf[a * CMAX + q] * Qf[q + b * CMAX];
+            Sf[a + b * CMAX] = v;
         }
     for (int a = 0; a < c; a++)
-        for (int b = 0; b < c; b++) Q[a + b * CMAX] = Gs[a + b * CMAX];
+        for (int b = 0; b < c; b++) Qf[a + b * CMAX] = Sf[a + b * CMAX];
     for (int a = 0; a < c; a++) ord[a] = a;
     for (int a = 1; a < c; a++) {
         const int x = ord[a];
         int b = a - 1;
-        while (b >= 0 && M[ord[b] * (CMAX + 1)] > M[x * (CMAX + 1)]) { ord[b + 1] = ord[b]; b--; }
+        while (b >= 0 && Mf[ord[b] * (CMAX + 1)] > Mf[x * (CMAX + 1)]) { ord[b + 1] = ord[b]; b--; }
         ord[b + 1] = x;
     }
 }
@@ -1405,6 +1492,8 @@ __global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, cons
     float* Yw = Lcw + W32;
     signed char* pvw = piv + (size_t)blockIdx.x * W32;
     float* Y = Yw + lane;
+    // the passes' row tiles (16 rows x 32 floats per warp) live in the staging area between sweeps
+    float* tile = stage_sm + wid * 16 * 32;
     const float pert32 = 1.1920929e-7f * (float)fmax(tnorm, 1e-30);
     const double pert = 2.220446049250313e-16 * fmax(tnorm, 1e-300);
     // shifts: the FP32 estimates in increasing order within each cluster (distinct start vectors
@@ -1425,45 +1514,57 @@ __global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, cons
     for (int it = 0; it < 3; it++) {
         if (wid == 0) tri_solve_staged(n, Urw, Ubw, Udw, Lcw, pvw, Yw, 1.0f, stage_sm);
         __syncthreads();
-        cluster_cholqr<float>(n, slo, sc, Y, Gs, Rinv);
+        cluster_cholqr<float>(n, slo, sc, Y, Gs, Rinv, tile);
     }
-    cluster_gram<float, false>(n, slo, sc, Y, df, ef, Gs);
-    cluster_gram<float, true>(n, slo, sc, Y, df, ef, M);
+    cluster_gram<float, false>(n, slo, sc, Y, df, ef, Gs, tile);
+    cluster_gram<float, true>(n, slo, sc, Y, df, ef, M, tile);
     const int blk = slo * (CMAX + 1);
-    if (wid == 0 && act && lane == slo) cluster_rr(sc, Gs + blk, Rinv + blk, M + blk, Q + blk, ord + slo);
+    // FP32 scratch of the Rayleigh-Ritz step in the FP64 arrays Rinv and Q, which no segment reads
+    // after the orthonormalisation (every segment keeps to its own block of each array)
+    float* Sf = reinterpret_cast<float*>(Rinv);
+    float* Rf = Sf + CMAX * CMAX;
+    float* Mf = reinterpret_cast<float*>(Q);
+    float* Qf = Mf + CMAX * CMAX;
+    if (wid == 0 && act && lane == slo)
+        cluster_rr32(sc, Gs + blk, M + blk, Sf + blk, Rf + blk, Mf + blk, Qf + blk, ord + slo);
     __syncthreads();
     // member m (lane slo + m) = Z Q[:, ord[m]] of its segment, in FP32 (Z is FP32; FP64 arithmetic
     // is slow on this part); f = y^H z with FP64 sums of FP32 products
     float qcol[CMAX];
     const int col = act ? slo + ord[slo + m] : 0;
 #pragma unroll
-    for (int b = 0; b < CMAX; b++) qcol[b] = (act && b >= slo && b < slo + sc) ? (float)Q[b + col * CMAX] : 0.0f;
+    for (int b = 0; b < CMAX; b++) qcol[b] = (act && b >= slo && b < slo + sc) ? Qf[b + col * CMAX] : 0.0f;
     const int i = s0 + m;
     const bool outp = act && i >= cout[2 * t] && i < cout[2 * t + 1];
     const bool keep = outp && i < n_store;
-    double fx = 0, fy = 0;
+    float fx = 0, fxl = 0, fy = 0, fyl = 0;   // compensated sums of the FP32 products
     for (int k0 = kb; k0 < ke; k0 += 16) {
         float yb[16];
 #pragma unroll
         for (int q = 0; q < 16; q++) yb[q] = k0 + q < ke ? Y[(size_t)(k0 + q) * 32] : 0.0f;
+        stage_tile(tile, yb);
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             const int k = k0 + q;
             if (k < ke) {
+                const float4* row = reinterpret_cast<const float4*>(tile + q * 32);
                 float v = 0;
 #pragma unroll
-                for (int b = 0; b < CMAX; b++) v += __shfl_sync(0xffffffffu, yb[q], b) * qcol[b];
+                for (int b4 = 0; b4 < CMAX / 4; b4++) {
+                    const float4 x = row[b4];
+                    v += x.x * qcol[4 * b4] + x.y * qcol[4 * b4 + 1] + x.z * qcol[4 * b4 + 2] + x.w * qcol[4 * b4 + 3];
+                }
                 if (y && outp) {
                     const float2 yy = y[k];
-                    fx += (double)(yy.x * v);
-                    fy -= (double)(yy.y * v);
+                    two_sum_acc(fx, fxl, yy.x * v);
+                    two_sum_acc(fy, fyl, -(yy.y * v));
                 }
                 if (keep) z[(size_t)k + (size_t)i * ldz] = (TZ)v;
             }
         }
     }
-    fred[wid][lane][0] = fx;
-    fred[wid][lane][1] = fy;
+    fred[wid][lane][0] = (double)fx + (double)fxl;
+    fred[wid][lane][1] = (double)fy + (double)fyl;
     __syncthreads();
     if (wid == 0 && outp) {
         double sx = 0, sy = 0;
@@ -1471,7 +1572,7 @@ __global__ void __launch_bounds__(32 * kClusterWarps) cluster_kernel(int n, cons
             sx += fred[q][lane][0];
             sy += fred[q][lane][1];
         }
-        w[i] = M[col * (CMAX + 1)];
+        w[i] = (double)Mf[col * (CMAX + 1)];
         if (f) f[i] = make_double2(sx, sy);
     }
 }
