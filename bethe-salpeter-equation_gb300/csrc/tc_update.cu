@@ -397,41 +397,41 @@ __global__ void __launch_bounds__(kHemmThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    // a chain ends at a multiple of kHemmChunk K blocks, at a tile's last K block, or at the range end
-    auto chain_end = [&](int64_t u) {
-        const int kb = (int)(u % KB);
-        return kb % kHemmChunk == kHemmChunk - 1 || kb == KB - 1 || u == u1 - 1;
-    };
-    auto chain_start = [&](int64_t u) { return u == u0 || (int)(u % KB) % kHemmChunk == 0; };
+    // Every role walks the units u0 + j in order with a (tile, K block) cursor advanced one unit at
+    // a time: a 64-bit division per unit and thread cost more issue slots than the conversion.
+    // A chain starts at the range start or a multiple of kHemmChunk K blocks and ends at the
+    // block before the next multiple, at a tile's last K block, or at the range end.
+    const int tile0 = (int)(u0 / KB), kb0 = (int)(u0 % KB);
+    auto chain_start = [&](int j, int kb) { return j == 0 || kb % kHemmChunk == 0; };
+    auto chain_end = [&](int j, int kb) { return kb % kHemmChunk == kHemmChunk - 1 || kb == KB - 1 || j == nu - 1; };
 
     if (warp == 0) {
         if (lane == 0) {
             prefetch_map(&tmA);
             prefetch_map(&tmB);
-            int issued = 0;
+            int issued = 0, tile = tile0, kb = kb0;
             for (int j = 0; j < nu; j++) {
-                const int64_t u = u0 + j;
                 const int s = j % kHemmRing;
                 const uint32_t ph = (uint32_t)(j / kHemmRing) & 1u;
                 // the slot is free once its A block is converted and its B parts are consumed
                 if (!mbar_wait(rconv + s, ph ^ 1u, &s_abort, h.err) || !mbar_wait(rmma + s, ph ^ 1u, &s_abort, h.err)) break;
                 mbar_arrive_tx(rfull + s, kHemmRaw + 3 * kHemmB);
-                const int x = (int)(u % KB) * kKb, i0 = (int)(u / KB) * kRows;
+                const int x = kb * kKb, i0 = tile * kRows;
                 tma_load_2d(raw(s), &tmA, x, i0, rfull + s);
                 for (int p = 0; p < 3; p++) tma_load_2d(bpart(s) + p * kHemmB, &tmB, x, 64 * p, rfull + s);
                 issued = j + 1;
+                if (++kb == KB) { kb = 0; ++tile; }
             }
             for (int s = 0; s < kHemmRing; s++)
                 mbar_drain(rfull + s, s < issued ? (issued - 1 - s) / kHemmRing : -1);
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            int c = -1;
-            for (int j = 0; j < nu; j++) {
-                const int64_t u = u0 + j;
+            int c = -1, kb = kb0;
+            for (int j = 0; j < nu; j++, kb = kb + 1 == KB ? 0 : kb + 1) {
                 const int s = j % kHemmRing, ps = j % kHemmParts;
                 const uint32_t ph = (uint32_t)(j / kHemmRing) & 1u, pph = (uint32_t)(j / kHemmParts) & 1u;
-                const bool first = chain_start(u);
+                const bool first = chain_start(j, kb);
                 if (first) {
                     c++;
                     if (c >= 2) {
@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(kHemmThreads, 1)
                 mma_block_cat<64>(tb, apart(ps), kHemmA, bpart(s), first);
                 mma_commit(rmma + s);
                 mma_commit(pempty + ps);
-                if (chain_end(u)) mma_commit(tfull + (c & 1));
+                if (chain_end(j, kb)) mma_commit(tfull + (c & 1));
             }
         }
     } else {
@@ -488,8 +488,8 @@ __global__ void __launch_bounds__(kHemmThreads, 1)
             }
             drained++;
         };
+        int tile = tile0, kb = kb0;
         for (int j = 0; j < nu && ok; j++) {
-            const int64_t u = u0 + j;
             const int s = j % kHemmRing, ps = j % kHemmParts;
             const uint32_t ph = (uint32_t)(j / kHemmRing) & 1u, pph = (uint32_t)(j / kHemmParts) & 1u;
             const bool got = mbar_wait(rfull + s, ph, &s_abort, h.err) && mbar_wait(pempty + ps, pph ^ 1u, &s_abort, h.err);
@@ -504,16 +504,16 @@ __global__ void __launch_bounds__(kHemmThreads, 1)
                 mbar_arrive(rconv + s);
                 mbar_arrive(pfull + ps);
             }
-            if (chain_start(u)) {
-                chain_tile[nchain & 1] = (int)(u / KB);
+            if (chain_start(j, kb)) {
+                chain_tile[nchain & 1] = tile;
                 nchain++;
             }
-            if (chain_end(u)) {
-                const int kb = (int)(u % KB);
-                chain_last[(nchain - 1) & 1] = (kb == KB - 1 || u == u1 - 1) ? 1 : 0;
+            if (chain_end(j, kb)) {
+                chain_last[(nchain - 1) & 1] = (kb == KB - 1 || j == nu - 1) ? 1 : 0;
                 // the chain before this one has finished by now
                 if (nchain >= 2 && drained < nchain - 1) drain();
             }
+            if (++kb == KB) { kb = 0; ++tile; }
         }
         while (ok && drained < nchain) drain();
     }
@@ -625,8 +625,15 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    auto strip_of = [&](int j) { return (int)((t0 + j) / a.ncols); };
-    auto col_of = [&](int j) { return (int)((t0 + j) % a.ncols); };
+    // every role walks its tiles in order with a (strip, column tile) cursor (no 64-bit division
+    // per tile); a strip starts at j = 0 or where the column tile wraps to 0
+    const int strip0 = (int)(t0 / a.ncols), col0 = (int)(t0 % a.ncols);
+    auto advance = [&](int& strip, int& col) {
+        if (++col == a.ncols) {
+            col = 0;
+            ++strip;
+        }
+    };
 
     if (warp == 0) {
         if (lane == 0) {
@@ -634,10 +641,9 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
             prefetch_map(&tmR);
             prefetch_map(&tmRi);
             // L parts and B operands; the A22 tiles are loaded by warp 10, independently
-            int nstrip = 0, issued = 0, lissued = 0;
-            for (int j = 0; j < nt; j++) {
-                const int strip = strip_of(j), col = col_of(j);
-                if (j == 0 || strip != strip_of(j - 1)) {
+            int nstrip = 0, issued = 0, lissued = 0, strip = strip0, col = col0;
+            for (int j = 0; j < nt; j++, advance(strip, col)) {
+                if (j == 0 || col == 0) {
                     if (nstrip > 0 && !mbar_wait(lfree, (uint32_t)(nstrip - 1) & 1u, &s_abort, a.err)) break;
                     mbar_arrive_tx(lfull, kUpdL);
                     for (int kb = 0; kb < 4; kb++)
@@ -668,22 +674,21 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
         if (lane == 0) {
             // the A22 tiles: tile j into buffer j % kUpdCbuf once tile j - kUpdCbuf has been stored
             prefetch_map(&tmC);
-            int issued = 0;
-            for (int j = 0; j < nt; j++) {
+            int issued = 0, strip = strip0, col = col0;
+            for (int j = 0; j < nt; j++, advance(strip, col)) {
                 const int cb = j % kUpdCbuf;
                 if (j >= kUpdCbuf && !mbar_wait(cempty + cb, (uint32_t)(j / kUpdCbuf - 1) & 1u, &s_abort, a.err)) break;
                 mbar_arrive_tx(cfull + cb, kUpdC);
-                tma_load_2d(Cs(cb), &tmC, 2 * strip_of(j) * kRows, col_of(j) * kUpdCols, cfull + cb);
+                tma_load_2d(Cs(cb), &tmC, 2 * strip * kRows, col * kUpdCols, cfull + cb);
                 issued = j + 1;
             }
             for (int b = 0; b < kUpdCbuf; b++) mbar_drain(cfull + b, b < issued ? (issued - 1 - b) / kUpdCbuf : -1);
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            int nstrip = 0;
-            for (int j = 0; j < nt; j++) {
-                const int strip = strip_of(j);
-                if (j == 0 || strip != strip_of(j - 1)) {
+            int nstrip = 0, strip = strip0, col = col0;
+            for (int j = 0; j < nt; j++, advance(strip, col)) {
+                if (j == 0 || col == 0) {
                     if (!mbar_wait(lfull, (uint32_t)nstrip & 1u, &s_abort, a.err)) break;
                     nstrip++;
                 }
@@ -702,7 +707,7 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
                 }
                 if (!okb) break;
                 mma_commit(tfull + b);
-                if (j == nt - 1 || strip_of(j + 1) != strip) mma_commit(lfree);
+                if (j == nt - 1 || col == a.ncols - 1) mma_commit(lfree);
             }
         }
     } else if (warp >= 2 && warp < 10) {
@@ -713,7 +718,8 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
         const int q = warp & 3, half = (warp - 2) >> 2;
         const int r = q * 32 + lane;   // row of the tile
         const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(kHalf * half);
-        for (int j = 0; j < nt; j++) {
+        int strip = strip0, col = col0;
+        for (int j = 0; j < nt; j++, advance(strip, col)) {
             const int b = j % kUpdAcc, cb = j % kUpdCbuf;
             bool ok = mbar_wait(tfull + b, (uint32_t)(j / kUpdAcc) & 1u, &s_abort, a.err) &&
                       mbar_wait(cfull + cb, (uint32_t)(j / kUpdCbuf) & 1u, &s_abort, a.err);
@@ -741,7 +747,7 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
             if (*reinterpret_cast<volatile int*>(&s_abort)) break;
             if (ct == 0) {
                 // the buffer may be refilled once the store has read it out
-                tma_store_2d(&tmC, 2 * strip_of(j) * kRows, col_of(j) * kUpdCols, C);
+                tma_store_2d(&tmC, 2 * strip * kRows, col * kUpdCols, C);
                 tma_store_drain();
                 mbar_arrive(cempty + cb);
             }
