@@ -166,16 +166,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(saddr(bar))
         : "memory");
 }
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
-    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
-                     reinterpret_cast<uint64_t>(map)),
-                 "r"(x), "r"(y), "r"(saddr(src))
-                 : "memory");
-    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void tma_store_drain() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-// every bulk store group of this thread has completed (its writes performed)
-__device__ __forceinline__ void tma_store_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void prefetch_map(const CUtensorMap* m) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
@@ -566,12 +556,16 @@ __global__ void tc_prep_hemm_kernel(int m, int kk, const float2* __restrict__ V,
 // ---------------------------------------------------------------------------------------------
 // update, persistent: tiles of 128 rows x kUpdCols complex columns in row-strip-major order, CTA g
 // taking tiles [g T / G, (g + 1) T / G).  The strip's L parts stay resident while its column
-// tiles stream; the C tiles and the accumulator pairs are double-buffered, so the TMA load / store
-// of one tile overlaps the MMAs of the next.
+// tiles stream; the C tiles (TMA loads) and the accumulator pairs are double-buffered, so the
+// load of one tile overlaps the MMAs of the next.  The workers read their part of a C tile into
+// registers, release its buffer at once and store the updated values straight to A22 (coalesced,
+// 256 bytes per warp and column): no shared-memory write-back, no TMA store to wait for.
 // ---------------------------------------------------------------------------------------------
 struct UpdArgs {
     int m, nstrips, ncols;
     int64_t ntiles;
+    float2* A;      // A22 (the workers store the updated tiles directly)
+    int64_t lda;
     int* err;
 };
 
@@ -587,7 +581,7 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
     uint64_t* bfull = bars;                     // [ring] B parts landed
     uint64_t* bempty = bfull + kUpdRing;        // [ring] B parts consumed
     uint64_t* cfull = bempty + kUpdRing;        // [kUpdCbuf] C tile landed
-    uint64_t* cempty = cfull + kUpdCbuf;        // [kUpdCbuf] C tile stored (its shared memory read out)
+    uint64_t* cempty = cfull + kUpdCbuf;        // [kUpdCbuf] C tile read out by the workers
     uint64_t* tfull = cempty + kUpdCbuf;        // [kUpdAcc] accumulator pair holds a finished tile
     uint64_t* tempty = tfull + kUpdAcc;         // [kUpdAcc] accumulator pair drained
     uint64_t* lfull = tempty + kUpdAcc;         // L parts of a strip landed
@@ -610,7 +604,7 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
         }
         for (int b = 0; b < kUpdCbuf; b++) {
             mbar_init(cfull + b, 1);
-            mbar_init(cempty + b, 1);
+            mbar_init(cempty + b, kWorkers / 32);
         }
         for (int b = 0; b < kUpdAcc; b++) {
             mbar_init(tfull + b, 1);
@@ -714,45 +708,41 @@ __global__ void __launch_bounds__(kUpdThreads, 1)
         // workers: warp w reads tensor-memory lanes 32 (w % 4) ..; warps 2-5 take complex columns
         // 0 .. kUpdCols / 2 - 1 of the tile, warps 6-9 the rest
         constexpr int kHalf = kUpdCols / 2;
-        const int ct = threadIdx.x - 64;
         const int q = warp & 3, half = (warp - 2) >> 2;
         const int r = q * 32 + lane;   // row of the tile
         const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(kHalf * half);
         int strip = strip0, col = col0;
         for (int j = 0; j < nt; j++, advance(strip, col)) {
             const int b = j % kUpdAcc, cb = j % kUpdCbuf;
-            bool ok = mbar_wait(tfull + b, (uint32_t)(j / kUpdAcc) & 1u, &s_abort, a.err) &&
-                      mbar_wait(cfull + cb, (uint32_t)(j / kUpdCbuf) & 1u, &s_abort, a.err);
-            ok = __all_sync(0xffffffffu, ok);   // the warp stays converged for the tensor-memory loads
-            tc_fence_after();
-            float* C = Cs(cb);
             static_assert(kHalf == 16, "two column halves of 16 per tile");
+            // this warp's part of the A22 tile into registers; then the buffer may be refilled
+            bool ok = __all_sync(0xffffffffu, mbar_wait(cfull + cb, (uint32_t)(j / kUpdCbuf) & 1u, &s_abort, a.err));
+            float2 x[kHalf];
+            if (ok) {
+                const float* C = Cs(cb);
+#pragma unroll
+                for (int u = 0; u < kHalf; u++) x[u] = reinterpret_cast<const float2*>(C + (kHalf * half + u) * 2 * kRows)[r];
+            }
+            mbar_arrive_warp(cempty + cb);
+            ok = __all_sync(0xffffffffu, ok && mbar_wait(tfull + b, (uint32_t)(j / kUpdAcc) & 1u, &s_abort, a.err));
+            tc_fence_after();
             float v[6 * kHalf];   // Re, Im of each column group, this warp's columns
             const uint32_t tb = tq + (uint32_t)(kUpdAccCols * b);
             tmem_ld6x16(tb, tb + kUpdCols, tb + 2 * kUpdCols, tb + 3 * kUpdCols, tb + 4 * kUpdCols, tb + 5 * kUpdCols, v);
-            if (ok) {
-#pragma unroll
-                for (int u = 0; u < kHalf; u++) {
-                    float2* cp = reinterpret_cast<float2*>(C + (kHalf * half + u) * 2 * kRows) + r;
-                    const float2 x = *cp;
-                    *cp = make_float2(x.x - (v[u] + (v[2 * kHalf + u] + v[4 * kHalf + u])),
-                                      x.y - (v[kHalf + u] + (v[3 * kHalf + u] + v[5 * kHalf + u])));
-                }
-            }
             tc_fence_before();
             mbar_arrive_warp(tempty + b);
-            fence_async_smem();
-            asm volatile("bar.sync 1, %0;" ::"n"(kWorkers) : "memory");
-            // leave together: a failed wait set s_abort before the barrier
-            if (*reinterpret_cast<volatile int*>(&s_abort)) break;
-            if (ct == 0) {
-                // the buffer may be refilled once the store has read it out
-                tma_store_2d(&tmC, 2 * strip * kRows, col * kUpdCols, C);
-                tma_store_drain();
-                mbar_arrive(cempty + cb);
+            if (!ok) break;
+            // the updated tile straight to A22 (each column: 32 lanes, 256 contiguous bytes)
+            const int row = strip * kRows + r, c0 = col * kUpdCols + kHalf * half;
+            if (row < a.m) {
+                float2* out = a.A + (int64_t)c0 * a.lda + row;
+#pragma unroll
+                for (int u = 0; u < kHalf; u++)
+                    if (c0 + u < a.m)
+                        out[(int64_t)u * a.lda] = make_float2(x[u].x - (v[u] + (v[2 * kHalf + u] + v[4 * kHalf + u])),
+                                                              x[u].y - (v[kHalf + u] + (v[3 * kHalf + u] + v[5 * kHalf + u])));
             }
         }
-        if (ct == 0) tma_store_wait_all();
     }
     tc_fence_before();
     __syncthreads();
@@ -905,6 +895,8 @@ int tc_rank2k(cudaStream_t st, int nsm, int m, int kk, float2* A22, int64_t lda,
     a.nstrips = (m + kRows - 1) / kRows;
     a.ncols = (m + kUpdCols - 1) / kUpdCols;
     a.ntiles = (int64_t)a.nstrips * a.ncols;
+    a.A = A22;
+    a.lda = lda;
     a.err = err;
     const int64_t G = std::min<int64_t>(nsm, a.ntiles);
     if (ev) cudaEventRecord(ev[0], st);
