@@ -42,7 +42,7 @@ WORKLOAD_SMALL = "magnetic4_24x24_2v2c"  # N_BSE = 2304
 METRIC = "BSE build+diag wall time and eps2 grad time at N_BSE; error vs FP64"
 FP64_LARGE_PROFILE = os.path.join(ROOT, "profiles", "fp64_vs_mixed_orb8_48x48.md")
 # DRAM traffic / algorithmic bytes of tc_update_kernel, one ncu-captured launch at m = 8192
-UPD_TRAFFIC_RATIO = (609.853952 + 478.409216) / (16 * 8192 ** 2 / 1e6)
+UPD_TRAFFIC_RATIO = (613.634560 + 478.541824) / (16 * 8192 ** 2 / 1e6)
 
 
 def _dist_env():
