@@ -13,6 +13,8 @@
                  per frequency "(w,0) (eps_xx) (w,0) (eps_yy) (w,0) (eps_zz) Im(eps_avg)/3" with
                  complex numbers printed as "(re,im)"; only xx is computed, so yy = zz = (0,0) and the
                  last column is Im(eps_xx)/3 (quirk Q16)
+  *.xsf          real-space Wannier functions on a supercell grid (Real_space_wannier ctor,
+                 bse.version13.cpp:1081-1212): read_xsf_datagrid / read_wannier_xsf, write_xsf_datagrid
 
 The reader keeps the reference's semantics: the R vectors of a block are the ones given
 on the first line of each group of nw*nw lines, converted crystal->cartesian with the
@@ -237,3 +239,82 @@ def write_bands(path, e_v, e_c, n_spin: int):
             for s in range(n_spin):
                 row += [f"{x:.10g}" for x in e_v[s, k]] + [f"{x:.10g}" for x in e_c[s, k]]
             fh.write(" ".join(row) + " \n")
+
+
+# ------------------------------------------------------------------------------------------
+# Real-space Wannier functions on an XSF data grid (Real_space_wannier ctor, bse.version13.cpp:
+# 1081-1212).  File names: seedname + "_00001.xsf" (function w + 1, five digits); with spinor
+# functions seedname + "up_00001.xsf" / "down_00001.xsf" (1108-1117).  The reference skips the
+# first 22 lines of a file, then reads the grid dimensions, the origin, the three spanning vectors
+# of the (super)cell grid and the values, x fastest over the whole supercell grid (1121-1139).
+# The reader here finds the grid by its BEGIN_DATAGRID_3D keyword instead of a fixed line count
+# (the count depends on the number of atoms in the header: quirk Q31); the writer emits exactly 22
+# header lines before the dimensions, so the reference reads its files as they are.
+# ------------------------------------------------------------------------------------------
+def xsf_name(seedname: str, w: int, spinor: bool = False, spin: int = 0) -> str:
+    """The reference's file name of Wannier function w (0-based) of spin channel `spin`."""
+    tag = "" if not spinor else ("up" if spin == 0 else "down")
+    return f"{seedname}{tag}_{w + 1:05d}.xsf"
+
+
+def write_xsf_datagrid(path, data: np.ndarray, origin, axes, lattice: Optional[np.ndarray] = None) -> None:
+    """data [NX, NY, NZ] (real) on the grid r = origin + sum_p (X_p / N_p) axes[p]; axes[p] is
+    the p-th spanning vector of the whole grid (the supercell), lattice the unit cell (rows) for
+    the CRYSTAL block (defaults to axes)."""
+    data = np.asarray(data, dtype=float)
+    nx, ny, nz = data.shape
+    lat = np.asarray(axes if lattice is None else lattice, dtype=float).reshape(3, 3)
+    axes = np.asarray(axes, dtype=float).reshape(3, 3)
+    head = [" #", " # real-space Wannier function on a periodic grid", " #", "", "CRYSTAL", "PRIMVEC"]
+    head += ["  " + " ".join(f"{x:.10f}" for x in lat[p]) for p in range(3)]
+    head += ["CONVVEC"] + ["  " + " ".join(f"{x:.10f}" for x in lat[p]) for p in range(3)]
+    head += ["PRIMCOORD", "  1  1", "X  0.0 0.0 0.0", "", "BEGIN_BLOCK_DATAGRID_3D", "  wannier",
+             "BEGIN_DATAGRID_3D_wannier"]
+    while len(head) < 22:
+        head.insert(3, " #")
+    assert len(head) == 22
+    vals = data.transpose(2, 1, 0).reshape(-1)   # x fastest, then y, then z
+    with open(path, "w") as fh:
+        fh.write("\n".join(head) + "\n")
+        fh.write(f"  {nx} {ny} {nz}\n")
+        fh.write("  " + " ".join(f"{x:.10f}" for x in np.asarray(origin, dtype=float)) + "\n")
+        for p in range(3):
+            fh.write("  " + " ".join(f"{x:.10f}" for x in axes[p]) + "\n")
+        for i in range(0, vals.size, 6):
+            fh.write(" " + " ".join(f"{x:.8e}" for x in vals[i:i + 6]) + "\n")
+        fh.write("END_DATAGRID_3D\nEND_BLOCK_DATAGRID_3D\n")
+
+
+def read_xsf_datagrid(path):
+    """(data [NX, NY, NZ], origin (3,), axes (3, 3): row p = spanning vector p) of the first
+    DATAGRID_3D block of an XSF file."""
+    with open(path) as fh:
+        text = fh.read()
+    pos = text.find("BEGIN_DATAGRID_3D")
+    if pos < 0:
+        raise ValueError(f"{path}: no BEGIN_DATAGRID_3D block")
+    body = text[pos:].split("\n", 1)[1]
+    end = body.find("END_DATAGRID_3D")
+    tok = body[:end if end >= 0 else len(body)].split()
+    nx, ny, nz = (int(float(t)) for t in tok[:3])
+    origin = np.array([float(t) for t in tok[3:6]])
+    axes = np.array([float(t) for t in tok[6:15]]).reshape(3, 3)
+    vals = np.array([float(t) for t in tok[15:15 + nx * ny * nz]])
+    if vals.size != nx * ny * nz:
+        raise ValueError(f"{path}: {vals.size} grid values, {nx * ny * nz} expected")
+    return vals.reshape(nz, ny, nx).transpose(2, 1, 0).copy(), origin, axes
+
+
+def read_wannier_xsf(seedname: str, nw: int, spinor: bool = False):
+    """All functions of a seedname: (data [n_spin_files, nw, NX, NY, NZ], origin, axes), the files
+    in the reference's order (spin channel, then function)."""
+    out, origin, axes = [], None, None
+    for spin in range(2 if spinor else 1):
+        row = []
+        for w in range(nw):
+            d, o, a = read_xsf_datagrid(xsf_name(seedname, w, spinor, spin))
+            if origin is None:
+                origin, axes = o, a
+            row.append(d)
+        out.append(row)
+    return np.asarray(out), origin, axes
