@@ -28,21 +28,27 @@
 //          accumulator holds the real parts (columns 0..31) and the imaginary parts (32..63) of a
 //          128 x 32 complex tile.  L, R and iR are split into BF16 parts in global memory by a
 //          small kernel.  Persistent: one CTA per SM walks its share of the tiles in row-strip
-//          order with the strip's L resident; the A22 tiles come in and go back by TMA,
-//          double-buffered together with the accumulators, so the transfers of one tile overlap
-//          the MMAs of the next.
+//          order with the strip's L resident; the A22 tiles come in by TMA, double-buffered
+//          together with the accumulators, so the load of one tile overlaps the MMAs of the next,
+//          and the workers store the updated tiles straight to A22.
 //
-// Accumulation: the tensor pipe's FP32 accumulation truncates.  The x0 y0 products and the five
-// smaller ones go to separate accumulators, and the hemm restarts its accumulators every 128 K
-// and adds the finished chains in FP32 registers, so the error stays that of an FP32 product
-// (no drift with K).
+// MMAs: the three B parts lie back to back in shared memory, so the six products of a K = 16 step
+// take three MMAs, a0 [b0 b1 b2] (N = 192), a1 [b0 b1] (N = 128) and a2 b0 (N = 64), into three
+// column groups of the accumulator: a0 b0 | a0 b1 + a1 b0 + a2 b0 | a0 b2 + a1 b1.  Accumulation:
+// the tensor pipe's FP32 accumulation truncates; with the smaller products apart from a0 b0 their
+// truncation is relative to their own size, the epilogue adds the groups in FP32, and the hemm
+// restarts its accumulators every 128 K and adds the finished chains in FP32 registers, so the
+// error stays that of an FP32 product (no drift with K).
 //
-// Roles (320 threads): warp 0 issues the TMA loads (one elected thread), warp 1 allocates the
-// tensor memory and issues the MMAs (one elected thread), warps 2-9 split the FP32 operands in
-// shared memory and run the epilogue (tensor memory -> registers; warp w reads lanes 32 (w % 4),
-// two warps per lane quarter, each with half of the accumulator columns).  Stages are handed over
-// through mbarriers; every wait is bounded: after kWaitPolls failed polls the waiting thread
-// raises the error word and the CTA drains and returns (no hang).
+// Roles: warp 0 issues the TMA loads (one elected thread), warp 1 allocates the tensor memory (512
+// columns) and issues the MMAs (one elected thread), the worker warps run the rest (warp w reads
+// tensor-memory lanes 32 (w % 4)).  hemm: 576 threads, 16 worker warps (four per lane quarter)
+// split the streamed FP32 blocks into BF16 parts and drain the accumulators.  update: 352
+// threads, 8 worker warps (two per lane quarter, half of the tile's columns each) and warp 10,
+// which loads the A22 tiles.  Every role walks its units or tiles with an incrementally advanced
+// cursor (no 64-bit division per unit).  Stages are handed over through mbarriers (one arrival
+// per warp where a warp signals); every wait is bounded: after kWaitPolls failed polls the waiting
+// thread raises the error word and the CTA drains and returns (no hang).
 //
 // TMA works in 16-byte granules of the 2m-real columns, so the order m must be even (every
 // trailing order of the reduction is, for even n).
