@@ -25,7 +25,7 @@ EXPORTS = [
     "bse_create", "bse_destroy", "bse_compute_bands", "bse_get_bands", "bse_set_bands",
     "bse_build_kernel", "bse_diagonalize", "bse_oscillators", "bse_eps", "bse_solve",
     "bse_stage_times", "bse_kernel_launches", "bse_reset_kernel_launches", "bse_eps_noalloc",
-    "bse_solve_many", "bse_diagnostics", "bse_build_kernel_rows", "bse_set_kernel",
+    "bse_solve_many", "bse_diagnostics", "bse_build_kernel_rows", "bse_set_kernel", "bse_wannier_m",
 ]
 
 
@@ -77,6 +77,9 @@ def load(build_if_missing: bool = True):
     L.bse_eps_noalloc.argtypes = [C.c_int64, _dp, _dp, C.c_double, _dp, C.c_int32, C.c_double, _dp, _dp, C.c_void_p]
     L.bse_diagnostics.argtypes = [C.c_void_p, _dp, C.c_int32]
     L.bse_solve_many.argtypes = [C.POINTER(C.c_void_p), C.c_int32, _dp, C.c_int32, C.c_double, _dp, _dp, C.c_int32]
+    _ip = C.POINTER(C.c_int32)
+    L.bse_wannier_m.argtypes = [C.c_int32, C.c_int32, _ip, _ip, _dp, C.c_double, _dp, _dp, _dp, _ip, _dp, C.c_int32,
+                                _dp, C.c_int32, _dp]
     _LIB = L
     return L
 
@@ -209,6 +212,32 @@ def eps_noalloc(E, f, F, omega, gamma):
     if st != 0:
         raise BSEError(st, lib.bse_last_error(None).decode())
     return e2, e1
+
+
+def wannier_m(functions, cells, cell_volume, origin, axes, lattice, n_int, q, g_list=None, small_q=False):
+    """bse_wannier_m: real-space Wannier M [n_g, n_spin nw, n_spin nw] (complex128) from the
+    functions [n_spin, nw, NX, NY, NZ] on the supercell grid r = origin + sum_p (X_p / N_p) axes[p]
+    (axes, lattice: rows), for q + G over g_list (rows), or the small-q form."""
+    lib = load()
+    f = np.ascontiguousarray(functions, dtype=np.float64)
+    if f.ndim != 5:
+        raise ValueError("functions: [n_spin, nw, NX, NY, NZ]")
+    n_spin, nw = f.shape[0], f.shape[1]
+    i32 = lambda v: np.ascontiguousarray(v, dtype=np.int32)
+    grid, cl, ni = i32(f.shape[2:]), i32(cells), i32(n_int)
+    org = np.ascontiguousarray(origin, dtype=np.float64)
+    ax = np.ascontiguousarray(axes, dtype=np.float64).reshape(3, 3)
+    lat = np.ascontiguousarray(lattice, dtype=np.float64).reshape(3, 3)
+    qq = np.ascontiguousarray(q, dtype=np.float64)
+    g = None if g_list is None else np.ascontiguousarray(g_list, dtype=np.float64).reshape(-1, 3)
+    n_g = 1 if g is None else len(g)
+    out = np.zeros((n_g, n_spin * nw, n_spin * nw), dtype=np.complex128)
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+    st = lib.bse_wannier_m(n_spin, nw, ip(grid), ip(cl), ptr(f), float(cell_volume), ptr(org), ptr(ax), ptr(lat), ip(ni),
+                           ptr(qq), n_g, None if g is None else ptr(g), 1 if small_q else 0, ptr(out))
+    if st != 0:
+        raise BSEError(st, lib.bse_last_error(None).decode())
+    return out
 
 
 def solve_many(contexts, omega, gamma, n_workers=8):

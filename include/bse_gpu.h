@@ -232,6 +232,22 @@ int bse_eps_noalloc(int64_t n_exc, const double* e, const double* f, double pref
                     const double* omega, int32_t n_omega, double gamma,
                     double* eps2, double* eps1, void* stream);
 
+/* Real-space Wannier matrix elements (Real_space_wannier + Dipole_Elements, bse.version13.cpp:
+ * 1081-1212, 1441-1456, 1503-1650): M_ab(q + G) = sum_R exp(i q.(o + R)) A_ab(q + G; R),
+ * A = Nsc V / Npts sum over the supercell grid of exp(i (q + G).r) w_a(r - R) w_b(r), for the
+ * functions f [n_spin][nw][grid[0]][grid[1]][grid[2]] (last index fastest; normalised here on the
+ * grid) on r = origin + sum_p (X_p / grid[p]) axes[p] (axes: 3 rows, the supercell's spanning
+ * vectors; cells[p] unit cells per direction), R over n_int[p] cells centred on 0 in units of
+ * lattice (3 rows), o = the supercell cell nearest to zero as cell indices (quirk kept from the
+ * reference).  small_q != 0: the reference's q -> 0 form, i qhat.r in place of the phase, the same
+ * for every G (g_list may be null).  m_out: [n_g][n_spin nw][n_spin nw] complex128, zero between
+ * spin channels.  Allocates and frees its own device memory; synchronous.  The kernel build uses
+ * point-like M; this gives the real-space M for callers that need it. */
+int bse_wannier_m(int32_t n_spin, int32_t nw, const int32_t* grid, const int32_t* cells, const double* f,
+                  double cell_volume, const double* origin, const double* axes, const double* lattice,
+                  const int32_t* n_int, const double* q, int32_t n_g, const double* g_list, int32_t small_q,
+                  double* m_out);
+
 /* Diagnostics of the last solve: [0] max FP64 residual ||H x - theta x||_2 (eV) over the refined
  * eigenpairs (an eigenvalue error bound), [1] eigenvalue clusters the own solver solved together,
  * [2] refined eigenpairs, [3] eigenvector columns formed. */
